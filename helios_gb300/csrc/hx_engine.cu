@@ -1,0 +1,764 @@
+// Host side of the engine: PPP model, device state, the contraction plan of one
+// CCSD iteration, the iterator, and the C ABI of include/helios_cc.h.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/helios_cc.h"
+#include "hx_kernels.h"
+#include "hx_tc.h"
+
+// ---------------------------------------------------------------- errors
+static thread_local char g_err[1024];
+
+void hx_set_error(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+#define HX_TRY(expr)                                  \
+    do {                                              \
+        int rc_ = (expr);                             \
+        if (rc_ < 0) return rc_;                      \
+    } while (0)
+
+#define HX_CU(call)                                                                          \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess) {                                                             \
+            hx_set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
+            return HX_ERR_CUDA;                                                              \
+        }                                                                                    \
+    } while (0)
+
+// ---------------------------------------------------------------- PPP model
+// src/modules/mod_helios.f90:42-43
+static const double kBohr = 0.52917721067, kHartree = 27.21138602;
+
+struct HostModel {
+    int N = 0, nel = 0;
+    std::vector<double> coords, G, core, huckel;
+};
+
+// readMoleculeInformation.f90:20-159 + gamma :216-264 + perturbate
+// (mod_helios.f90:577-601) with the diagonal field of setCore/applyField.
+static int build_model(const hx_ppp_model *m, const hx_cc_params *p, HostModel &out)
+{
+    const int n = m->n_sites;
+    if (n < 2 || n > HX_MAX_MOL_N) {
+        hx_set_error("n_sites=%d outside 2..%d", n, HX_MAX_MOL_N);
+        return HX_ERR_ARG;
+    }
+    if (!m->coords || !m->alpha || !m->gamma || !m->nels || (m->n_bonds > 0 && (!m->bond_i || !m->bond_j || !m->beta))) {
+        hx_set_error("model with NULL arrays");
+        return HX_ERR_ARG;
+    }
+    out.N = n;
+    out.nel = 0;
+    for (int i = 0; i < n; ++i) out.nel += m->nels[i];
+    if (out.nel % 2 || out.nel <= 0 || out.nel >= 2 * n) {
+        hx_set_error("closed-shell r-ccsd needs an even electron count in 2..2N-2 (got %d for N=%d)", out.nel, n);
+        return HX_ERR_ARG;
+    }
+    out.coords.assign(m->coords, m->coords + 3 * n);
+    double cen[3] = {0, 0, 0};
+    for (int i = 0; i < n; ++i)
+        for (int k = 0; k < 3; ++k) cen[k] += out.coords[3 * i + k];
+    for (int k = 0; k < 3; ++k) cen[k] /= n;
+    for (int i = 0; i < n; ++i)
+        for (int k = 0; k < 3; ++k) out.coords[3 * i + k] -= cen[k];
+    const double tr = 1.0 / (kBohr * kHartree);
+    out.G.assign((size_t)n * n, 0.0);
+    for (int a = 0; a < n; ++a)
+        for (int b = a; b < n; ++b) {
+            double d2 = 0;
+            for (int k = 0; k < 3; ++k) {
+                double x = out.coords[3 * a + k] - out.coords[3 * b + k];
+                d2 += x * x;
+            }
+            double r = std::sqrt(d2), med = (m->gamma[a] + m->gamma[b]) / 2.0, g = 0.0;
+            if (p->coulomb == HX_COULOMB_OHNO_KLOPMAN) g = med / std::sqrt(1.0 + (tr * med * r) * (tr * med * r));
+            else if (p->coulomb == HX_COULOMB_MATAGA_NISHIMOTO) g = med / (1.0 + tr * med * r);
+            else if (p->coulomb == HX_COULOMB_HUBBARD) g = (a == b) ? m->gamma[a] : 0.0;
+            else { hx_set_error("unknown coulomb type %d", p->coulomb); return HX_ERR_ARG; }
+            out.G[(size_t)a * n + b] = out.G[(size_t)b * n + a] = g;
+        }
+    std::vector<double> connect((size_t)n * n, 0.0);
+    for (int i = 0; i < n; ++i) connect[(size_t)i * n + i] = m->alpha[i];
+    for (int k = 0; k < m->n_bonds; ++k) {
+        int i = m->bond_i[k], j = m->bond_j[k];
+        if (i < 0 || j < 0 || i >= n || j >= n) { hx_set_error("bond %d joins invalid sites", k); return HX_ERR_ARG; }
+        connect[(size_t)i * n + j] = connect[(size_t)j * n + i] = m->beta[k];
+    }
+    if (p->bond_alternation != 0.0) {
+        for (int k = 0; k < m->n_bonds; ++k) {
+            int i = m->bond_i[k], j = m->bond_j[k];
+            int kind = m->bond_kind ? m->bond_kind[k] : HX_BOND_NONSET;
+            if (kind == HX_BOND_NONSET) break;   // the reference leaves the rest unscaled
+            double f = (kind == HX_BOND_DOUBLE) ? 1.0 + p->bond_alternation : 1.0 - p->bond_alternation;
+            connect[(size_t)i * n + j] = connect[(size_t)j * n + i] = m->beta[k] * f;
+        }
+    }
+    out.core = connect;
+    for (int k = 0; k < n; ++k) {
+        double s = 0;
+        for (int l = 0; l < n; ++l)
+            if (l != k) s += m->nels[l] * out.G[(size_t)k * n + l];
+        out.core[(size_t)k * n + k] -= s;
+    }
+    out.huckel = connect;
+    for (int mu = 0; mu < n; ++mu) {
+        double pert = 0;
+        for (int k = 0; k < 3; ++k) pert += p->field[k] * out.coords[3 * mu + k];
+        out.core[(size_t)mu * n + mu] += pert;
+        out.huckel[(size_t)mu * n + mu] += pert;
+    }
+    return HX_OK;
+}
+
+// ---------------------------------------------------------------- arena
+struct Arena {
+    size_t used = 0;
+    char *base = nullptr;
+    // first pass counts (base == nullptr), second pass hands out pointers
+    template <class T> T *take(size_t count)
+    {
+        size_t bytes = (count * sizeof(T) + 255) & ~(size_t)255;
+        T *p = base ? reinterpret_cast<T *>(base + used) : nullptr;
+        used += bytes;
+        return p;
+    }
+};
+
+// ---------------------------------------------------------------- iterator rules
+struct Rules {   // gIterator.f90:88-210
+    int iteration = 0, successful = 1;
+    double current = 0.0;
+    int update(double acc, const hx_cc_params &p, int maxiter, double eps, bool cancel)
+    {
+        ++iteration;
+        double previous = current;
+        current = acc;
+        if (current < previous) ++successful;
+        if (cancel) return HX_INTERRUPTED;
+        if (current < eps) return HX_CONVERGED;
+        if (!(current == current)) return HX_DIVERGED;
+        if (p.check_divergence && current > p.divergence_threshold) return HX_DIVERGED;
+        if (iteration + 1 > maxiter) return HX_FAILED_MAXITER;
+        if (p.check_stagnation && iteration > p.stagnation_after &&
+            100.0 * successful / iteration <= p.stagnation_threshold) return HX_STAGNATED;
+        return 0;
+    }
+};
+
+struct Group {   // one grouped tgemm launch
+    std::vector<TgemmDesc> h;
+    TgemmDesc *d = nullptr;
+    long long tiles = 0;
+};
+
+struct hx_ccsd {
+    hx_cc_params p{};
+    int nmol = 0;
+    std::vector<HostModel> models;
+    std::vector<int> N, o, v;
+    cudaStream_t st = nullptr;
+    char *arena = nullptr;
+    size_t arena_bytes = 0;
+    // device views
+    std::vector<ScfMol> scf;
+    std::vector<CCMol> cc;
+    std::vector<DiisMol> diis;
+    ScfMol *d_scf = nullptr;
+    CCMol *d_cc = nullptr;
+    DiisMol *d_diis = nullptr;
+    int *d_active = nullptr;
+    std::vector<int> active;
+    double *d_part = nullptr;
+    double *d_res = nullptr;             // nmol x 8 iteration results (inside the arena)
+    int nblk = 64;
+    std::vector<Group> plan;             // GEMM groups of one iteration (in order)
+    std::vector<Group> setup_groups;
+    long long maxw_nn = 0, maxw_ov = 0, maxw_pair = 0, maxw_oNoN = 0;
+    bool initialized = false;
+    std::atomic<int> cancel{0};
+    // per molecule host results
+    std::vector<double> res;             // nmol x 6
+    std::vector<Rules> rules;
+    std::vector<int> status;
+    tc::Engine *tce = nullptr;           // tensor-core backend (mixed precision)
+};
+
+// ---------------------------------------------------------------- plan helpers
+static TgemmDesc tg(const double *A, const double *B, double *C, int batch, int M, int N, int K, int Mi,
+                    int Ni, int Ki, std::initializer_list<long long> a, std::initializer_list<long long> b,
+                    std::initializer_list<long long> c, double alpha, double beta, int mol)
+{
+    TgemmDesc d;
+    memset(&d, 0, sizeof(d));
+    d.A = A; d.B = B; d.C = C;
+    d.batch = batch; d.M = M; d.N = N; d.K = K; d.Mi = Mi; d.Ni = Ni; d.Ki = Ki;
+    std::copy(a.begin(), a.end(), d.a);
+    std::copy(b.begin(), b.end(), d.b);
+    std::copy(c.begin(), c.end(), d.c);
+    d.alpha = alpha; d.beta = beta; d.mol = mol;
+    return d;
+}
+
+static int upload_group(Group &g)
+{
+    g.tiles = hx_tgemm_f64_prepare(g.h.data(), (int)g.h.size());
+    if (g.h.empty()) return HX_OK;
+    HX_CU(cudaMalloc(&g.d, sizeof(TgemmDesc) * g.h.size()));
+    HX_CU(cudaMemcpy(g.d, g.h.data(), sizeof(TgemmDesc) * g.h.size(), cudaMemcpyHostToDevice));
+    return HX_OK;
+}
+
+static int run_group(hx_ccsd *h, Group &g)
+{
+    if (g.tiles == 0) return HX_OK;
+    if (h->p.precision == HX_PRECISION_MIXED && h->tce) {
+        cudaError_t e = tc::run_group(h->tce, g.h.data(), (int)g.h.size(), h->active.data(), h->st);
+        if (e != cudaSuccess) { hx_set_error("tensor-core group: %s", cudaGetErrorString(e)); return HX_ERR_CUDA; }
+        return HX_OK;
+    }
+    HX_CU(hx_tgemm_f64_launch(g.d, (int)g.h.size(), g.tiles, h->d_active, h->st));
+    return HX_OK;
+}
+
+// Descriptors of every contraction of one iteration, for every molecule.
+// Index conventions are spelled out in hx_plan.h; each block cites the term
+// of the T1-dressed closed-shell CCSD equations it evaluates.
+static void build_plan(hx_ccsd *h)
+{
+    enum { G_DRESS_XY, G_DRESS_P, G_FD1, G_FD2, G_GB, G_LEAD, G_LAD_A, G_LAD_B, G_LAD_D, G_LAD_E, G_W_D,
+           G_W_E, G_W_INT, G_HH, G_CINT1, G_CINT2, G_CTERM, G_DINT1, G_DINT2, G_DINT3, G_DTERM, G_FVOO,
+           G_E1, G_E2, G_S1, G_S_UG, G_S_V, G_S_R1, G_COUNT };
+    h->plan.assign(G_COUNT, Group());
+    auto &P = h->plan;
+    for (int mi = 0; mi < h->nmol; ++mi) {
+        const CCMol &m = h->cc[mi];
+        const int N = m.N, o = m.o, v = m.v, ov = o * v;
+        const double *Cmo = m.Cmo, *G = m.G;
+        // T1 dressing: X = [Co | Cv - Co t1], Y = [Co + Cv t1^T | Cv]
+        P[G_DRESS_XY].h.push_back(tg(Cmo, m.t1, m.X + o, 1, N, v, o, N, v, o, {0, N, 0, 1, 0}, {0, 1, 0, v, 0}, {0, N, 0, 1, 0}, -1.0, 1.0, mi));
+        P[G_DRESS_XY].h.push_back(tg(Cmo + o, m.t1, m.Y, 1, N, o, v, N, o, v, {0, N, 0, 1, 0}, {0, v, 0, 1, 0}, {0, N, 0, 1, 0}, 1.0, 1.0, mi));
+        // Pm = Yo Xo^T (dressed half density)
+        P[G_DRESS_P].h.push_back(tg(m.Y, m.X, m.Pm, 1, N, N, o, N, N, o, {0, N, 0, 1, 0}, {0, N, 0, 1, 0}, {0, N, 0, 1, 0}, 1.0, 0.0, mi));
+        // Fd = X^T H2 Y
+        P[G_FD1].h.push_back(tg(m.H2, m.Y, m.W1, 1, N, N, N, N, N, N, {0, N, 0, 1, 0}, {0, 1, 0, N, 0}, {0, N, 0, 1, 0}, 1.0, 0.0, mi));
+        P[G_FD2].h.push_back(tg(m.X, m.W1, m.Fd, 1, N, N, N, N, N, N, {0, 1, 0, N, 0}, {0, 1, 0, N, 0}, {0, N, 0, 1, 0}, 1.0, 0.0, mi));
+        // G . B for the dressed ZDO products
+        P[G_GB].h.push_back(tg(G, m.Bia, m.GBia, 1, N, ov, N, N, ov, N, {0, N, 0, 1, 0}, {0, 1, 0, ov, 0}, {0, ov, 0, 1, 0}, 1.0, 0.0, mi));
+        P[G_GB].h.push_back(tg(G, m.Boo, m.GBoo, 1, N, o * o, N, N, o * o, N, {0, N, 0, 1, 0}, {0, 1, 0, o * o, 0}, {0, o * o, 0, 1, 0}, 1.0, 0.0, mi));
+        P[G_GB].h.push_back(tg(G, m.Bvv, m.GBvv, 1, N, v * v, N, N, v * v, N, {0, N, 0, 1, 0}, {0, 1, 0, v * v, 0}, {0, v * v, 0, 1, 0}, 1.0, 0.0, mi));
+        // leading term (ai|bj)~ -> r2 (initialises r2)
+        P[G_LEAD].h.push_back(tg(m.Bia, m.GBia, m.r2, 1, ov, ov, N, ov, ov, N, {0, 1, 0, ov, 0}, {0, 1, 0, ov, 0}, {0, ov, 0, 1, 0}, 1.0, 0.0, mi));
+        // particle-particle ladder through the site basis:
+        //   sum_cd (ac|bd)~ t_ij^cd = sum_mu,nu X_mu,a X_nu,b G_mu,nu [sum_cd C_mu,c C_nu,d t_ij^cd]
+        P[G_LAD_A].h.push_back(tg(m.t2, Cmo + o, m.T1s, 1, o * v * o, N, v, o * v * o, N, v, {0, v, 0, 1, 0}, {0, N, 0, 1, 0}, {0, N, 0, 1, 0}, 1.0, 0.0, mi));
+        P[G_LAD_B].h.push_back(tg(Cmo + o, m.T1s, m.Ts, o, N, o * N, v, N, o * N, v, {0, N, 0, 1, 0}, {0, 1, 0, (long long)o * N, (long long)v * o * N}, {0, (long long)o * N, 0, 1, (long long)N * o * N}, 1.0, 0.0, mi));
+        P[G_LAD_D].h.push_back(tg(m.Ts, m.X + o, m.Z1, 1, o * N * o, v, N, o * N * o, v, N, {0, N, 0, 1, 0}, {0, 1, 0, N, 0}, {0, v, 0, 1, 0}, 1.0, 0.0, mi));
+        P[G_LAD_E].h.push_back(tg(m.X + o, m.Z1, m.r2, o, v, ov, N, v, ov, N, {0, 1, 0, N, 0}, {0, 1, 0, ov, (long long)N * ov}, {0, ov, 0, 1, (long long)v * ov}, 1.0, 1.0, mi));
+        // hole-hole ladder: W_klij = (ki|lj)~ + sum_cd t_ij^cd (kc|ld), the latter through the site basis
+        P[G_W_D].h.push_back(tg(m.Ts, Cmo, m.Zo, 1, o * N * o, o, N, o * N * o, o, N, {0, N, 0, 1, 0}, {0, 1, 0, N, 0}, {0, o, 0, 1, 0}, 1.0, 0.0, mi));
+        P[G_W_E].h.push_back(tg(Cmo, m.Zo, m.Woo, o, o, o * o, N, o, o * o, N, {0, 1, 0, N, 0}, {0, 1, 0, o * o, (long long)N * o * o}, {0, o * o, 0, 1, (long long)o * o * o}, 1.0, 0.0, mi));
+        P[G_W_INT].h.push_back(tg(m.Boo, m.GBoo, m.Woo, 1, o * o, o * o, N, o, o, N, {o, 1, 0, o * o, 0}, {o, 1, 0, o * o, 0}, {(long long)o * o, (long long)o * o * o, 1, o, 0}, 1.0, 1.0, mi));
+        P[G_HH].h.push_back(tg(m.Woo, m.t2, m.r2, 1, o * o, v * v, o * o, o, v, o, {(long long)o * o * o, o, (long long)o * o, 1, 0}, {ov, 1, (long long)v * ov, v, 0}, {(long long)v * ov, v, ov, 1, 0}, 1.0, 1.0, mi));
+        // C: Cint_kiac = (ki|ac)~ - 1/2 sum_ld t_li^ad (kd|lc);  C_ij^ab = -sum_kc t_kj^bc Cint_kiac
+        P[G_CINT1].h.push_back(tg(m.Boo, m.GBvv, m.Cint, 1, o * o, v * v, N, o * o, v * v, N, {0, 1, 0, o * o, 0}, {0, 1, 0, v * v, 0}, {0, v * v, 0, 1, 0}, 1.0, 0.0, mi));
+        P[G_CINT2].h.push_back(tg(m.t2, m.gov, m.Cint, 1, ov, ov, ov, v, v, v, {v, ov, (long long)v * ov, 1, 0}, {(long long)v * ov, 1, v, ov, 0}, {(long long)v * v, v, (long long)ov * v, 1, 0}, -0.5, 1.0, mi));
+        P[G_CTERM].h.push_back(tg(m.Cint, m.t2, m.Cp, 1, ov, ov, ov, v, v, v, {(long long)v * v, v, (long long)ov * v, 1, 0}, {v, ov, (long long)v * ov, 1, 0}, {(long long)v * ov, ov, v, 1, 0}, -1.0, 0.0, mi));
+        // D: Dint_aikc = L_aikc + 1/2 sum_ld u_il^ad L_ldkc;  D_ij^ab = 1/2 sum_kc u_jk^bc Dint_aikc
+        P[G_DINT1].h.push_back(tg(m.Bia, m.GBov0, m.Dint, 1, ov, ov, N, ov, ov, N, {0, 1, 0, ov, 0}, {0, 1, 0, ov, 0}, {0, ov, 0, 1, 0}, 2.0, 0.0, mi));
+        P[G_DINT2].h.push_back(tg(m.Bvv, m.GBoo, m.Dint, 1, v * v, o * o, N, v, o, N, {v, 1, 0, v * v, 0}, {o, 1, 0, o * o, 0}, {ov, 1, v, (long long)v * ov, 0}, -1.0, 1.0, mi));
+        P[G_DINT3].h.push_back(tg(m.u, m.Lov, m.Dint, 1, ov, ov, ov, ov, ov, ov, {0, ov, 0, 1, 0}, {0, ov, 0, 1, 0}, {0, ov, 0, 1, 0}, 0.5, 1.0, mi));
+        P[G_DTERM].h.push_back(tg(m.Dint, m.u, m.X2, 1, ov, ov, ov, ov, ov, ov, {0, ov, 0, 1, 0}, {0, ov, 0, 1, 0}, {0, ov, 0, 1, 0}, 0.5, 1.0, mi));
+        // E: F'_bc = F~_bc - sum_kld u_kl^bd (ld|kc);  F'_kj = F~_kj + sum_lcd u_lj^cd (kd|lc)
+        P[G_FVOO].h.push_back(tg(m.u, m.gov, m.Fvv2, 1, v, v, o * ov, v, v, ov, {0, ov, (long long)v * ov, 1, 0}, {0, ov, (long long)v * ov, 1, 0}, {0, v, 0, 1, 0}, -1.0, 1.0, mi));
+        P[G_FVOO].h.push_back(tg(m.gov, m.u, m.Foo2, 1, o, o, v * ov, o, o, ov, {0, (long long)v * ov, ov, 1, 0}, {0, (long long)v * ov, ov, 1, 0}, {0, o, 0, 1, 0}, 1.0, 1.0, mi));
+        //    E_ij^ab = sum_c t_ij^ac F'_bc - sum_k t_ik^ab F'_kj
+        P[G_E1].h.push_back(tg(m.t2, m.Fvv2, m.X2, 1, o * v * o, v, v, o * v * o, v, v, {0, v, 0, 1, 0}, {0, v, 0, 1, 0}, {0, v, 0, 1, 0}, 1.0, 1.0, mi));
+        P[G_E2].h.push_back(tg(m.Foo2, m.t2, m.X2, ov, o, v, o, o, v, o, {0, 1, 0, o, 0}, {0, 1, 0, v, ov}, {0, v, 0, 1, ov}, -1.0, 1.0, mi));
+        // singles: r1 = F~_ai + sum_kc u_ik^ac F~_kc + sum_kcd u_ki^cd (ad|kc)~ - sum_klc u_kl^ac (ki|lc)~
+        P[G_S1].h.push_back(tg(m.u, m.Fd + o, m.r1, 1, ov, 1, ov, ov, 1, v, {0, ov, v, 1, 0}, {0, 0, N, 1, 0}, {0, 1, 0, 0, 0}, 1.0, 1.0, mi));
+        P[G_S1].h.push_back(tg(m.u, m.Bov0, m.U, 1, ov, N, ov, ov, N, ov, {0, ov, 0, 1, 0}, {0, ov, 0, 1, 0}, {0, N, 0, 1, 0}, 1.0, 0.0, mi));
+        P[G_S_UG].h.push_back(tg(m.U, G, m.UG, 1, ov, N, N, ov, N, N, {0, N, 0, 1, 0}, {0, N, 0, 1, 0}, {0, N, 0, 1, 0}, 1.0, 0.0, mi));
+        P[G_S_V].h.push_back(tg(m.UG, m.Y + o, m.Vs, N, o, 1, v, o, 1, v, {0, (long long)v * N, 0, N, 1}, {0, 0, 0, 1, N}, {0, N, 0, 0, 1}, 1.0, 0.0, mi));
+        P[G_S_R1].h.push_back(tg(m.Vs, m.X + o, m.r1, 1, o, v, N, o, v, N, {0, N, 0, 1, 0}, {0, 1, 0, N, 0}, {0, v, 0, 1, 0}, 1.0, 1.0, mi));
+        P[G_S_R1].h.push_back(tg(m.Boo, m.UG, m.r1, 1, o, v, o * N, o, v, N, {0, 1, o, (long long)o * o, 0}, {0, N, (long long)v * N, 1, 0}, {0, v, 0, 1, 0}, -1.0, 1.0, mi));
+    }
+    // Note G_S_R1 holds two GEMMs into r1: they run in one launch on disjoint
+    // tiles of the same output, so they must not overlap -> keep separate groups.
+    Group extra;
+    extra.h.assign(P[G_S_R1].h.begin() + 0, P[G_S_R1].h.end());
+    P[G_S_R1].h.clear();
+    Group g1, g2;
+    for (size_t k = 0; k < extra.h.size(); ++k) (k % 2 == 0 ? g1 : g2).h.push_back(extra.h[k]);
+    P[G_S_R1] = g1;
+    P.push_back(g2);
+}
+
+// ---------------------------------------------------------------- allocation
+static int allocate(hx_ccsd *h)
+{
+    const int nd = h->p.diis_enabled ? h->p.diis_steps : 0;
+    for (int pass = 0; pass < 2; ++pass) {
+        Arena A;
+        A.base = pass ? h->arena : nullptr;
+        h->scf.assign(h->nmol, ScfMol());
+        h->cc.assign(h->nmol, CCMol());
+        h->diis.assign(h->nmol, DiisMol());
+        for (int mi = 0; mi < h->nmol; ++mi) {
+            const int N = h->N[mi], o = h->o[mi], v = h->v[mi];
+            const size_t nn = (size_t)N * N, ov = (size_t)o * v, pr = ov * ov;
+            ScfMol &s = h->scf[mi];
+            s.N = N; s.nocc = o;
+            s.core = A.take<double>(nn); s.G = A.take<double>(nn); s.huckel = A.take<double>(nn);
+            s.D0 = nullptr; s.V0 = nullptr;
+            s.F = A.take<double>(nn); s.D = A.take<double>(nn); s.V = A.take<double>(nn); s.E = A.take<double>(N);
+            s.A = A.take<double>(nn); s.W1 = A.take<double>(nn); s.W2 = A.take<double>(nn); s.Fmo = A.take<double>(nn);
+            s.out = A.take<double>(4); s.status = A.take<int>(2);
+            CCMol &m = h->cc[mi];
+            m.N = N; m.o = o; m.v = v;
+            m.Cmo = s.V; m.G = s.G; m.h = s.core; m.Fmo = s.Fmo;
+            m.Bov0 = A.take<double>(N * ov); m.GBov0 = A.take<double>(N * ov);
+            m.gov = A.take<double>(pr); m.Lov = A.take<double>(pr);
+            m.D1 = A.take<double>(ov); m.D2 = A.take<double>(pr);
+            m.t1 = A.take<double>(ov); m.t2 = A.take<double>(pr);
+            m.r1 = A.take<double>(ov); m.r2 = A.take<double>(pr); m.u = A.take<double>(pr);
+            m.X = A.take<double>(nn); m.Y = A.take<double>(nn); m.Pm = A.take<double>(nn);
+            m.H2 = A.take<double>(nn); m.W1 = A.take<double>(nn); m.Fd = A.take<double>(nn);
+            m.Bia = A.take<double>(N * ov); m.GBia = A.take<double>(N * ov);
+            m.Boo = A.take<double>((size_t)N * o * o); m.GBoo = A.take<double>((size_t)N * o * o);
+            m.Bvv = A.take<double>((size_t)N * v * v); m.GBvv = A.take<double>((size_t)N * v * v);
+            m.T1s = A.take<double>((size_t)o * v * o * N); m.Ts = A.take<double>((size_t)o * N * o * N);
+            m.Z1 = A.take<double>((size_t)o * N * o * v); m.Zo = A.take<double>((size_t)o * N * o * o);
+            m.Woo = A.take<double>((size_t)o * o * o * o);
+            m.Cint = A.take<double>(pr); m.Cp = A.take<double>(pr); m.Dint = A.take<double>(pr); m.X2 = A.take<double>(pr);
+            m.Fvv2 = A.take<double>((size_t)v * v); m.Foo2 = A.take<double>((size_t)o * o);
+            m.U = A.take<double>(ov * N); m.UG = A.take<double>(ov * N); m.Vs = A.take<double>((size_t)o * N);
+            DiisMol &d = h->diis[mi];
+            d.nd = nd > 0 ? nd : 1;
+            d.L = (long long)(ov + pr);
+            d.Ht = nd ? A.take<double>((size_t)nd * d.L) : nullptr;
+            d.He = nd ? A.take<double>((size_t)nd * d.L) : nullptr;
+            d.gram = A.take<double>((size_t)HX_MAX_DIIS * HX_MAX_DIIS);
+            d.coef = A.take<double>(HX_MAX_DIIS + 1);
+            d.count = A.take<int>(1);
+            h->maxw_nn = std::max<long long>(h->maxw_nn, nn);
+            h->maxw_ov = std::max<long long>(h->maxw_ov, ov + v * v + o * o);
+            h->maxw_pair = std::max<long long>(h->maxw_pair, pr + ov);
+            h->maxw_oNoN = std::max<long long>(h->maxw_oNoN, (long long)o * N * o * N);
+            h->maxw_oNoN = std::max<long long>(h->maxw_oNoN, (long long)N * (ov + o * o + v * v));
+            h->maxw_oNoN = std::max<long long>(h->maxw_oNoN, (long long)(ov + pr + N * ov));
+        }
+        double *resblock = A.take<double>((size_t)8 * h->nmol);
+        for (int mi = 0; mi < h->nmol; ++mi) h->cc[mi].res = resblock ? resblock + 8 * mi : nullptr;
+        h->d_res = resblock;
+        if (pass == 0) {
+            h->arena_bytes = A.used;
+            cudaError_t e = cudaMalloc(&h->arena, A.used);
+            if (e != cudaSuccess) {
+                hx_set_error("cudaMalloc(%zu bytes) for the molecule state: %s", A.used, cudaGetErrorString(e));
+                return HX_ERR_NOMEM;
+            }
+            HX_CU(cudaMemsetAsync(h->arena, 0, A.used, h->st));
+        }
+    }
+    HX_CU(cudaMalloc(&h->d_scf, sizeof(ScfMol) * h->nmol));
+    HX_CU(cudaMalloc(&h->d_cc, sizeof(CCMol) * h->nmol));
+    HX_CU(cudaMalloc(&h->d_diis, sizeof(DiisMol) * h->nmol));
+    HX_CU(cudaMalloc(&h->d_active, sizeof(int) * h->nmol));
+    HX_CU(cudaMalloc(&h->d_part, sizeof(double) * (size_t)h->nmol * h->nblk * HX_MAX_DIIS));
+    h->active.assign(h->nmol, 1);
+    h->res.assign((size_t)h->nmol * 8, 0.0);
+    h->status.assign(h->nmol, 0);
+    h->rules.assign(h->nmol, Rules());
+    return HX_OK;
+}
+
+static int upload_views(hx_ccsd *h)
+{
+    HX_CU(cudaMemcpyAsync(h->d_scf, h->scf.data(), sizeof(ScfMol) * h->nmol, cudaMemcpyHostToDevice, h->st));
+    HX_CU(cudaMemcpyAsync(h->d_cc, h->cc.data(), sizeof(CCMol) * h->nmol, cudaMemcpyHostToDevice, h->st));
+    HX_CU(cudaMemcpyAsync(h->d_diis, h->diis.data(), sizeof(DiisMol) * h->nmol, cudaMemcpyHostToDevice, h->st));
+    HX_CU(cudaMemcpyAsync(h->d_active, h->active.data(), sizeof(int) * h->nmol, cudaMemcpyHostToDevice, h->st));
+    return HX_OK;
+}
+
+// ---------------------------------------------------------------- C ABI
+extern "C" {
+
+void hx_cc_params_default(hx_cc_params *p)
+{
+    memset(p, 0, sizeof(*p));
+    p->coulomb = HX_COULOMB_OHNO_KLOPMAN;
+    p->bond_alternation = 0.0;
+    p->scf_maxiter = 400;
+    p->scf_eps = 1e-12;
+    p->scf_step = 0.05;
+    p->projection_type = 2;
+    p->cc_maxiter = 2000;
+    p->cc_eps = 1e-12;
+    p->t1_step = 1.0;
+    p->t2_step = 1.0;
+    p->diis_enabled = 1;
+    p->diis_steps = 20;
+    p->check_divergence = 1;
+    p->divergence_threshold = 1e3;
+    p->check_stagnation = 1;
+    p->stagnation_threshold = 60.0;
+    p->stagnation_after = 200;
+    p->precision = HX_PRECISION_FP64;
+    p->guess = 0;
+}
+
+int hx_ccsd_create_batch(const hx_ppp_model *ms, int32_t n, const hx_cc_params *p, hx_ccsd **out)
+{
+    if (!ms || !p || !out || n <= 0) { hx_set_error("hx_ccsd_create_batch: bad arguments"); return HX_ERR_ARG; }
+    *out = nullptr;
+    if (p->projection_type != 1 && p->projection_type != 2) { hx_set_error("projection-type must be 1 or 2"); return HX_ERR_ARG; }
+    if (p->diis_enabled && (p->diis_steps < 2 || p->diis_steps > HX_MAX_DIIS)) { hx_set_error("diis-steps outside 2..%d", HX_MAX_DIIS); return HX_ERR_ARG; }
+    if (p->precision != HX_PRECISION_FP64 && p->precision != HX_PRECISION_MIXED) { hx_set_error("unknown precision mode"); return HX_ERR_ARG; }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) { hx_set_error("no CUDA device"); return HX_ERR_CUDA; }
+    hx_ccsd *h = new hx_ccsd();
+    h->p = *p;
+    h->nmol = n;
+    h->models.resize(n);
+    for (int i = 0; i < n; ++i) {
+        int rc = build_model(&ms[i], p, h->models[i]);
+        if (rc < 0) { delete h; return rc; }
+        h->N.push_back(h->models[i].N);
+        h->o.push_back(h->models[i].nel / 2);
+        h->v.push_back(h->models[i].N - h->models[i].nel / 2);
+    }
+    if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) {
+        hx_set_error("cudaStreamCreate failed"); delete h; return HX_ERR_CUDA;
+    }
+    int rc = allocate(h);
+    if (rc < 0) { hx_ccsd_destroy(h); return rc; }
+    for (int mi = 0; mi < n; ++mi) {
+        const HostModel &M = h->models[mi];
+        size_t bytes = sizeof(double) * M.N * M.N;
+        if (cudaMemcpyAsync((void *)h->scf[mi].core, M.core.data(), bytes, cudaMemcpyHostToDevice, h->st) != cudaSuccess ||
+            cudaMemcpyAsync((void *)h->scf[mi].G, M.G.data(), bytes, cudaMemcpyHostToDevice, h->st) != cudaSuccess ||
+            cudaMemcpyAsync((void *)h->scf[mi].huckel, M.huckel.data(), bytes, cudaMemcpyHostToDevice, h->st) != cudaSuccess) {
+            hx_set_error("upload of the PPP model failed"); hx_ccsd_destroy(h); return HX_ERR_CUDA;
+        }
+    }
+    rc = upload_views(h);
+    if (rc < 0) { hx_ccsd_destroy(h); return rc; }
+    build_plan(h);
+    for (auto &g : h->plan) {
+        rc = upload_group(g);
+        if (rc < 0) { hx_ccsd_destroy(h); return rc; }
+    }
+    if (p->precision == HX_PRECISION_MIXED) {
+        rc = tc::create(&h->tce, h->plan, h->st);
+        if (rc < 0) { hx_ccsd_destroy(h); return rc; }
+    }
+    if (cudaStreamSynchronize(h->st) != cudaSuccess) { hx_set_error("set-up failed"); hx_ccsd_destroy(h); return HX_ERR_CUDA; }
+    *out = h;
+    return HX_OK;
+}
+
+int hx_ccsd_create(const hx_ppp_model *m, const hx_cc_params *p, hx_ccsd **out)
+{
+    return hx_ccsd_create_batch(m, 1, p, out);
+}
+
+static int cc_setup(hx_ccsd *h, int guess)
+{
+    // Bov0, D1, D2; then G.Bov0, gov = Bov0^T G Bov0; then Lov and the guess
+    HX_CU(hx_ew_setup(h->d_cc, h->d_active, h->nmol, h->maxw_oNoN, guess, h->st));
+    Group g1, g2;
+    for (int mi = 0; mi < h->nmol; ++mi) {
+        const CCMol &m = h->cc[mi];
+        const int N = m.N, ov = m.o * m.v;
+        g1.h.push_back(tg(m.G, m.Bov0, m.GBov0, 1, N, ov, N, N, ov, N, {0, N, 0, 1, 0}, {0, 1, 0, ov, 0}, {0, ov, 0, 1, 0}, 1.0, 0.0, mi));
+        g2.h.push_back(tg(m.Bov0, m.GBov0, m.gov, 1, ov, ov, N, ov, ov, N, {0, 1, 0, ov, 0}, {0, 1, 0, ov, 0}, {0, ov, 0, 1, 0}, 1.0, 0.0, mi));
+    }
+    HX_TRY(upload_group(g1));
+    HX_TRY(upload_group(g2));
+    HX_CU(hx_tgemm_f64_launch(g1.d, (int)g1.h.size(), g1.tiles, h->d_active, h->st));
+    HX_CU(hx_tgemm_f64_launch(g2.d, (int)g2.h.size(), g2.tiles, h->d_active, h->st));
+    HX_CU(hx_ew_setup2(h->d_cc, h->d_active, h->nmol, h->maxw_pair, guess, h->st));
+    HX_CU(cudaStreamSynchronize(h->st));
+    cudaFree(g1.d);
+    cudaFree(g2.d);
+    return HX_OK;
+}
+
+int hx_ccsd_init(hx_ccsd *h)
+{
+    if (!h) { hx_set_error("NULL handle"); return HX_ERR_ARG; }
+    ScfParams sp;
+    sp.maxiter = h->p.scf_maxiter;
+    sp.eps = h->p.scf_eps;
+    sp.step = h->p.scf_step;
+    sp.divergence = h->p.divergence_threshold;
+    sp.stag_pct = h->p.stagnation_threshold;
+    sp.stag_after = h->p.stagnation_after;
+    sp.check_div = h->p.check_divergence;
+    sp.check_stag = h->p.check_stagnation;
+    HX_CU(hx_scf_launch(h->d_scf, h->nmol, sp, h->st));
+    std::vector<double> out(4);
+    std::vector<int> st(2);
+    HX_CU(cudaStreamSynchronize(h->st));
+    for (int mi = 0; mi < h->nmol; ++mi) {
+        HX_CU(cudaMemcpy(out.data(), h->scf[mi].out, sizeof(double) * 4, cudaMemcpyDeviceToHost));
+        HX_CU(cudaMemcpy(st.data(), h->scf[mi].status, sizeof(int) * 2, cudaMemcpyDeviceToHost));
+        if (st[0] != HX_CONVERGED) {
+            hx_set_error("SCF of molecule %d ended with status %d after %d iterations (accuracy %.3e)", mi, st[0], st[1], out[3]);
+            return HX_ERR_SCF;
+        }
+        h->cc[mi].eref = out[0];
+    }
+    HX_TRY(upload_views(h));
+    HX_TRY(cc_setup(h, 1));
+    for (int mi = 0; mi < h->nmol; ++mi) { h->rules[mi] = Rules(); h->status[mi] = 0; h->active[mi] = 1; }
+    for (int mi = 0; mi < h->nmol; ++mi) HX_CU(cudaMemsetAsync(h->diis[mi].count, 0, sizeof(int), h->st));
+    HX_TRY(upload_views(h));
+    HX_CU(cudaStreamSynchronize(h->st));
+    h->initialized = true;
+    return HX_OK;
+}
+
+// One iterationCC for every active molecule (no host synchronisation).
+static int iteration_body(hx_ccsd *h, double eps)
+{
+    const int nm = h->nmol;
+    auto &P = h->plan;
+    int k = 0;
+    HX_CU(hx_ew_dress_init(h->d_cc, h->d_active, nm, h->maxw_nn, h->st));
+    HX_TRY(run_group(h, P[k++]));                                    // dress X, Y
+    HX_TRY(run_group(h, P[k++]));                                    // Pm
+    HX_CU(hx_ew_dress_fock(h->d_cc, h->d_active, nm, h->maxw_nn, h->st));
+    HX_TRY(run_group(h, P[k++]));                                    // W1 = H2 Y
+    HX_TRY(run_group(h, P[k++]));                                    // Fd = X^T W1
+    HX_CU(hx_ew_zdo_products(h->d_cc, h->d_active, nm, h->maxw_oNoN, h->st));
+    HX_TRY(run_group(h, P[k++]));                                    // G B
+    HX_CU(hx_ew_make_u(h->d_cc, h->d_active, nm, h->maxw_pair, h->st));
+    HX_CU(hx_ew_fock_blocks(h->d_cc, h->d_active, nm, h->maxw_ov, h->st));
+    HX_TRY(run_group(h, P[k++]));                                    // lead
+    HX_TRY(run_group(h, P[k++]));                                    // lad_a
+    HX_TRY(run_group(h, P[k++]));                                    // lad_b
+    HX_CU(hx_ew_gamma_scale(h->d_cc, h->d_active, nm, h->maxw_oNoN, h->st));
+    HX_TRY(run_group(h, P[k++]));                                    // lad_d
+    HX_TRY(run_group(h, P[k++]));                                    // lad_e
+    HX_TRY(run_group(h, P[k++]));                                    // w_d
+    HX_TRY(run_group(h, P[k++]));                                    // w_e
+    HX_TRY(run_group(h, P[k++]));                                    // w_int
+    HX_TRY(run_group(h, P[k++]));                                    // hh
+    HX_TRY(run_group(h, P[k++]));                                    // cint1
+    HX_TRY(run_group(h, P[k++]));                                    // cint2
+    HX_TRY(run_group(h, P[k++]));                                    // cterm
+    HX_CU(hx_ew_c_combine(h->d_cc, h->d_active, nm, h->maxw_pair, h->st));
+    HX_TRY(run_group(h, P[k++]));                                    // dint1
+    HX_TRY(run_group(h, P[k++]));                                    // dint2
+    HX_TRY(run_group(h, P[k++]));                                    // dint3
+    HX_TRY(run_group(h, P[k++]));                                    // dterm
+    HX_TRY(run_group(h, P[k++]));                                    // F'vv, F'oo
+    HX_TRY(run_group(h, P[k++]));                                    // e1
+    HX_TRY(run_group(h, P[k++]));                                    // e2
+    HX_CU(hx_ew_assemble(h->d_cc, h->d_active, nm, h->maxw_pair, h->st));
+    HX_TRY(run_group(h, P[k++]));                                    // singles: u F, U
+    HX_TRY(run_group(h, P[k++]));                                    // UG
+    HX_TRY(run_group(h, P[k++]));                                    // Vs
+    HX_TRY(run_group(h, P[k++]));                                    // r1 += Vs Xv
+    HX_TRY(run_group(h, P[k++]));                                    // r1 -= Boo UG
+    const int use_diis = h->p.diis_enabled ? 1 : 0;
+    HX_CU(hx_step(h->d_cc, h->d_diis, h->d_active, nm, h->p.t1_step, h->p.t2_step, use_diis, h->d_part, h->nblk, h->st));
+    if (use_diis) HX_CU(hx_diis(h->d_cc, h->d_diis, h->d_active, nm, eps, h->d_part, h->nblk, h->st));
+    HX_CU(hx_energy(h->d_cc, h->d_active, nm, h->d_part, h->nblk, h->st));
+    return HX_OK;
+}
+
+static int fetch_results(hx_ccsd *h)
+{
+    HX_CU(cudaMemcpyAsync(h->res.data(), h->d_res, sizeof(double) * 8 * h->nmol, cudaMemcpyDeviceToHost, h->st));
+    HX_CU(cudaStreamSynchronize(h->st));
+    return HX_OK;
+}
+
+int hx_ccsd_iterate(hx_ccsd *h, int32_t iteration, double eps, double acc[5])
+{
+    if (!h || !h->initialized) { hx_set_error("hx_ccsd_iterate before hx_ccsd_init"); return HX_ERR_STATE; }
+    if (h->p.projection_type != 2) { hx_set_error("projection-type 1 is not built on the GPU path"); return HX_ERR_UNSUPPORTED; }
+    (void)iteration;
+    HX_TRY(iteration_body(h, eps));
+    HX_TRY(fetch_results(h));
+    if (acc) {
+        acc[0] = h->res[0]; acc[1] = h->res[1];
+        acc[2] = acc[3] = acc[4] = -1.0;
+    }
+    return HX_OK;
+}
+
+int hx_ccsd_energy(hx_ccsd *h, double e[5])
+{
+    if (!h || !h->initialized) { hx_set_error("hx_ccsd_energy before hx_ccsd_init"); return HX_ERR_STATE; }
+    HX_CU(hx_energy(h->d_cc, nullptr, h->nmol, h->d_part, h->nblk, h->st));
+    HX_TRY(fetch_results(h));
+    if (e) { e[0] = h->res[2]; e[1] = h->res[3]; e[2] = h->res[4]; e[3] = h->res[5]; e[4] = 0.0; }
+    return HX_OK;
+}
+
+static int solve_all(hx_ccsd *h, int maxiter, double eps)
+{
+    if (h->p.projection_type != 2) { hx_set_error("projection-type 1 is not built on the GPU path"); return HX_ERR_UNSUPPORTED; }
+    int remaining = 0;
+    for (int mi = 0; mi < h->nmol; ++mi) remaining += h->active[mi];
+    while (remaining > 0) {
+        HX_TRY(iteration_body(h, eps));
+        HX_TRY(fetch_results(h));
+        bool changed = false;
+        const bool cancel = h->cancel.exchange(0) != 0;
+        for (int mi = 0; mi < h->nmol; ++mi) {
+            if (!h->active[mi]) continue;
+            double a = std::max(h->res[(size_t)mi * 8 + 0], h->res[(size_t)mi * 8 + 1]);
+            int s = h->rules[mi].update(a, h->p, maxiter, eps, cancel);
+            if (s != 0) {
+                h->status[mi] = s;
+                h->active[mi] = 0;
+                --remaining;
+                changed = true;
+            }
+        }
+        if (changed) HX_CU(cudaMemcpyAsync(h->d_active, h->active.data(), sizeof(int) * h->nmol, cudaMemcpyHostToDevice, h->st));
+    }
+    // keep every molecule addressable for getters / energy after the solve
+    for (int mi = 0; mi < h->nmol; ++mi) h->active[mi] = 1;
+    HX_CU(cudaMemcpyAsync(h->d_active, h->active.data(), sizeof(int) * h->nmol, cudaMemcpyHostToDevice, h->st));
+    HX_CU(cudaStreamSynchronize(h->st));
+    return HX_OK;
+}
+
+int hx_ccsd_solve(hx_ccsd *h, int32_t maxiter, double eps, int32_t *status, int32_t *iters, double e[5])
+{
+    if (!h || !h->initialized) { hx_set_error("hx_ccsd_solve before hx_ccsd_init"); return HX_ERR_STATE; }
+    HX_TRY(solve_all(h, maxiter, eps));
+    if (status) *status = h->status[0];
+    if (iters) *iters = h->rules[0].iteration;
+    if (e) { e[0] = h->res[2]; e[1] = h->res[3]; e[2] = h->res[4]; e[3] = h->res[5]; e[4] = 0.0; }
+    return HX_OK;
+}
+
+int hx_ccsd_solve_batch(hx_ccsd *h, int32_t *status, int32_t *iters, double *e)
+{
+    if (!h || !h->initialized) { hx_set_error("hx_ccsd_solve_batch before hx_ccsd_init"); return HX_ERR_STATE; }
+    HX_TRY(solve_all(h, h->p.cc_maxiter, h->p.cc_eps));
+    for (int mi = 0; mi < h->nmol; ++mi) {
+        if (status) status[mi] = h->status[mi];
+        if (iters) iters[mi] = h->rules[mi].iteration;
+        if (e) for (int k = 0; k < 4; ++k) e[mi * 5 + k] = h->res[(size_t)mi * 8 + 2 + k];
+        if (e) e[mi * 5 + 4] = 0.0;
+    }
+    return HX_OK;
+}
+
+int hx_ccsd_get_amplitudes(hx_ccsd *h, int32_t mol, double *t1, double *t2)
+{
+    if (!h || mol < 0 || mol >= h->nmol) { hx_set_error("bad handle or molecule index"); return HX_ERR_ARG; }
+    const int o = h->o[mol], v = h->v[mol];
+    const size_t ov = (size_t)o * v;
+    std::vector<double> a(ov), b(ov * ov);
+    HX_CU(cudaMemcpyAsync(a.data(), h->cc[mol].t1, sizeof(double) * ov, cudaMemcpyDeviceToHost, h->st));
+    HX_CU(cudaMemcpyAsync(b.data(), h->cc[mol].t2, sizeof(double) * ov * ov, cudaMemcpyDeviceToHost, h->st));
+    HX_CU(cudaStreamSynchronize(h->st));
+    if (t1)
+        for (int i = 0; i < o; ++i)
+            for (int x = 0; x < v; ++x) t1[i + (size_t)o * x] = a[(size_t)i * v + x];
+    if (t2)
+        for (int i = 0; i < o; ++i)
+            for (int x = 0; x < v; ++x)
+                for (int j = 0; j < o; ++j)
+                    for (int y = 0; y < v; ++y)
+                        t2[i + (size_t)o * (j + (size_t)o * (x + (size_t)v * y))] = b[(((size_t)i * v + x) * o + j) * v + y];
+    return HX_OK;
+}
+
+int hx_ccsd_set_guess(hx_ccsd *h, int32_t mol, const double *t1, const double *t2)
+{
+    if (!h || !h->initialized || mol < 0 || mol >= h->nmol || !t1 || !t2) { hx_set_error("hx_ccsd_set_guess: bad arguments or state"); return HX_ERR_ARG; }
+    const int o = h->o[mol], v = h->v[mol];
+    const size_t ov = (size_t)o * v;
+    std::vector<double> a(ov), b(ov * ov);
+    for (int i = 0; i < o; ++i)
+        for (int x = 0; x < v; ++x) a[(size_t)i * v + x] = t1[i + (size_t)o * x];
+    for (int i = 0; i < o; ++i)
+        for (int x = 0; x < v; ++x)
+            for (int j = 0; j < o; ++j)
+                for (int y = 0; y < v; ++y)
+                    b[(((size_t)i * v + x) * o + j) * v + y] = t2[i + (size_t)o * (j + (size_t)o * (x + (size_t)v * y))];
+    HX_CU(cudaMemcpyAsync(h->cc[mol].t1, a.data(), sizeof(double) * ov, cudaMemcpyHostToDevice, h->st));
+    HX_CU(cudaMemcpyAsync(h->cc[mol].t2, b.data(), sizeof(double) * ov * ov, cudaMemcpyHostToDevice, h->st));
+    HX_CU(cudaMemsetAsync(h->diis[mol].count, 0, sizeof(int), h->st));
+    HX_CU(cudaStreamSynchronize(h->st));
+    h->rules[mol] = Rules();
+    return HX_OK;
+}
+
+int hx_ccsd_get_scf(hx_ccsd *h, int32_t mol, double *C, double *eps, double *fmo, double scf[4], int32_t scf_status[2])
+{
+    if (!h || mol < 0 || mol >= h->nmol) { hx_set_error("bad handle or molecule index"); return HX_ERR_ARG; }
+    const ScfMol &s = h->scf[mol];
+    const size_t nn = (size_t)s.N * s.N;
+    if (C) HX_CU(cudaMemcpyAsync(C, s.V, sizeof(double) * nn, cudaMemcpyDeviceToHost, h->st));
+    if (eps) HX_CU(cudaMemcpyAsync(eps, s.E, sizeof(double) * s.N, cudaMemcpyDeviceToHost, h->st));
+    if (fmo) HX_CU(cudaMemcpyAsync(fmo, s.Fmo, sizeof(double) * nn, cudaMemcpyDeviceToHost, h->st));
+    if (scf) HX_CU(cudaMemcpyAsync(scf, s.out, sizeof(double) * 4, cudaMemcpyDeviceToHost, h->st));
+    if (scf_status) HX_CU(cudaMemcpyAsync(scf_status, s.status, sizeof(int) * 2, cudaMemcpyDeviceToHost, h->st));
+    HX_CU(cudaStreamSynchronize(h->st));
+    return HX_OK;
+}
+
+int hx_ccsd_dims(hx_ccsd *h, int32_t mol, int32_t dims[4])
+{
+    if (!h || mol < 0 || mol >= h->nmol || !dims) { hx_set_error("bad arguments"); return HX_ERR_ARG; }
+    dims[0] = h->N[mol]; dims[1] = h->o[mol]; dims[2] = h->v[mol]; dims[3] = h->models[mol].nel;
+    return HX_OK;
+}
+
+void hx_ccsd_cancel(hx_ccsd *h)
+{
+    if (h) h->cancel.store(1);
+}
+
+void hx_ccsd_destroy(hx_ccsd *h)
+{
+    if (!h) return;
+    if (h->st) cudaStreamSynchronize(h->st);
+    if (h->tce) tc::destroy(h->tce);
+    for (auto &g : h->plan) if (g.d) cudaFree(g.d);
+    cudaFree(h->arena);
+    cudaFree(h->d_scf);
+    cudaFree(h->d_cc);
+    cudaFree(h->d_diis);
+    cudaFree(h->d_active);
+    cudaFree(h->d_part);
+    if (h->st) cudaStreamDestroy(h->st);
+    delete h;
+}
+
+int hx_last_error(char *buf, size_t len)
+{
+    size_t n = strlen(g_err);
+    if (buf && len) {
+        size_t c = n < len - 1 ? n : len - 1;
+        memcpy(buf, g_err, c);
+        buf[c] = 0;
+    }
+    return (int)n;
+}
+
+}  // extern "C"

@@ -1,0 +1,61 @@
+// Per-molecule device views shared by the kernels and the host plan.
+#pragma once
+#include "hx_common.cuh"
+
+#define HX_MAX_DIIS 50         // largest coupled-cluster:diis-steps (definebd.f90: range 2..50)
+
+struct ScfParams {
+    int maxiter;
+    double eps, step, divergence, stag_pct;
+    int stag_after, check_div, check_stag;
+};
+
+// One molecule's SCF state in device memory (row-major N x N matrices).
+struct ScfMol {
+    int N, nocc;
+    const double *core, *G, *huckel;
+    const double *D0, *V0;          // optional warm start (density and basis)
+    double *F, *D, *V, *E, *A, *W1, *W2, *Fmo;
+    double *out;                    // [0] E_total [1] E_el [2] E_nuc [3] last accuracy
+    int *status;                    // [0] status [1] iterations
+};
+
+// One molecule's CCSD state. Pair layout: X[i][a][j][b] for o x v x o x v
+// tensors, i.e. a (o*v) x (o*v) matrix over excitations (ia) with the
+// reference's order (i outer, a inner). Site-basis factors are [site][...].
+struct CCMol {
+    int N, o, v;
+    int pad_;
+    // constants of the molecule (after SCF)
+    const double *Cmo, *G, *h, *Fmo;      // N x N
+    double *Bov0, *GBov0;                 // [N][o*v]  C_mu,k C_mu,c and G . it
+    double *gov, *Lov;                    // pair: (kc|ld), 2(kc|ld)-(kd|lc)
+    double *D1, *D2;                      // denominators F_ii-F_aa, F_ii+F_jj-F_aa-F_bb
+    // amplitudes and residuals
+    double *t1, *t2, *r1, *r2, *u;
+    // T1-dressed factors
+    double *X, *Y, *Pm, *H2, *W1, *Fd;    // N x N
+    double *Bia, *GBia;                   // [N][o*v]  X_mu,a Y_mu,i (index i*v+a)
+    double *Boo, *GBoo;                   // [N][o*o]  X_mu,k Y_mu,i (index k*o+i)
+    double *Bvv, *GBvv;                   // [N][v*v]  X_mu,a Y_mu,c (index a*v+c)
+    // contraction scratch
+    double *T1s, *Ts, *Z1, *Zo, *Woo;     // ladder: o*v*o*N, o*N*o*N, o*N*o*v, o*N*o*o, o^4
+    double *Cint, *Cp, *Dint, *X2;        // o^2 v^2 each
+    double *Fvv2, *Foo2;                  // v*v, o*o
+    double *U, *UG, *Vs;                  // [o*v][N], [o*v][N], [o][N]
+    // results of the iteration (device): [0] max|d1| [1] max|d2| [2] E_total
+    // [3] E_ref [4] 2 sum F t1 [5] doubles part
+    double *res;
+    double eref;
+};
+
+// DIIS history of one molecule: nd slots of the amplitude vector (t1, t2) and
+// of the error vector (d1, 3*Omega2), each of length L = o*v + (o*v)^2, used
+// as a ring (slot = count % nd). gram is nd x nd in slot order; coef holds
+// HX_MAX_DIIS+1 doubles: the mixing coefficients and, last, how many to mix.
+struct DiisMol {
+    double *Ht, *He, *gram, *coef;
+    int *count;
+    int nd;
+    long long L;
+};

@@ -1,0 +1,165 @@
+/*
+ * helios_cc.h -- C ABI of the GB300 closed-shell PPP CCSD engine (helios "r-ccsd").
+ *
+ * Drop-in for the coupled-cluster call of helios. The reference drives CCSD
+ * through module globals from getEnergy (src/modules/mod_property.f90:55-338):
+ *   setCCParameters('r-ccsd')  -> hx_ccsd_create / hx_ccsd_create_batch
+ *   initCC (SCF, MO Fock, integrals, guessCC)        -> hx_ccsd_init
+ *   iterationCC(iteration, epsilon, accuracy)        -> hx_ccsd_iterate
+ *   energyCC(energy)                                 -> hx_ccsd_energy
+ *   iterator(iterationCC, energyCC, ...)             -> hx_ccsd_solve / hx_ccsd_solve_batch
+ *   finalizeCC                                       -> hx_ccsd_destroy
+ * (src/methods/coupledCluster/mod_cc.f90:82-485, 489-603, 634-650, 820-891,
+ *  1916-1952; src/calculation/gIterator.f90:1-210.)
+ *
+ * Conventions
+ *  - Every entry point returns 0 (HX_OK) or a negative code; iteration
+ *    outcomes use the iterator's statuses: 1 converged, -1 failed (max
+ *    iterations), -2 diverged, -3 stagnated, -4 interrupted. Errors are
+ *    <= -100 and hx_last_error() describes the last one. Nothing exits,
+ *    aborts or traps.
+ *  - Caller buffers are host memory, copied in and out; device memory belongs
+ *    to the handle. One handle per host thread; it owns one CUDA stream.
+ *  - Energies are in eV, coordinates in Angstrom, fields in eV/Angstrom.
+ *  - Amplitudes cross the ABI in the reference's Fortran layout: t1(o, v) and
+ *    t2(o, o, v, v), column-major, virtual indices counted from the first
+ *    virtual orbital (t1(i, a) of the reference is t1[i + o*(a-o-1)] with
+ *    1-based i, a).
+ */
+#ifndef HELIOS_CC_H
+#define HELIOS_CC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HX_OK 0
+#define HX_CONVERGED 1
+#define HX_FAILED_MAXITER (-1)
+#define HX_DIVERGED (-2)
+#define HX_STAGNATED (-3)
+#define HX_INTERRUPTED (-4)
+#define HX_ERR_ARG (-100)
+#define HX_ERR_CUDA (-101)
+#define HX_ERR_NOMEM (-102)
+#define HX_ERR_STATE (-103)
+#define HX_ERR_SCF (-104)
+#define HX_ERR_KERNEL (-105)
+#define HX_ERR_UNSUPPORTED (-106)
+
+#define HX_COULOMB_OHNO_KLOPMAN 0
+#define HX_COULOMB_MATAGA_NISHIMOTO 1
+#define HX_COULOMB_HUBBARD 2
+
+#define HX_BOND_SINGLE 0
+#define HX_BOND_DOUBLE 1
+#define HX_BOND_NONSET (-1)
+
+#define HX_PRECISION_FP64 0
+#define HX_PRECISION_MIXED 1
+
+/* One molecule block of a helios input (src/input/readMoleculeInformation.f90:20-117). */
+typedef struct hx_ppp_model {
+    int32_t n_sites;
+    const double *coords;      /* n_sites x 3, Angstrom (re-centred by the engine) */
+    const double *alpha;       /* site energies, eV */
+    const double *gamma;       /* one-centre repulsions, eV */
+    const int32_t *nels;       /* pi electrons donated per site */
+    int32_t n_bonds;
+    const int32_t *bond_i;     /* 0-based site indices */
+    const int32_t *bond_j;
+    const double *beta;        /* resonance integrals, eV */
+    const int32_t *bond_kind;  /* HX_BOND_SINGLE / HX_BOND_DOUBLE / HX_BOND_NONSET */
+} hx_ppp_model;
+
+/* The input keywords of the path (src/input/definebd.f90), with helios's
+ * defaults filled in by hx_cc_params_default. */
+typedef struct hx_cc_params {
+    int32_t coulomb;              /* parametrization:coulomb-integrals (ohno-klopman) */
+    double bond_alternation;      /* parametrization:bond-alternation (0) */
+    double field[3];              /* field:along-x/y/z, or p*polariz:derive-step (0) */
+    int32_t scf_maxiter;          /* scf:max-iterations (400) */
+    double scf_eps;               /* scf:accuracy, as 10^-value (1e-12) */
+    double scf_step;              /* scf:iter-step (0.05) */
+    int32_t projection_type;      /* coupled-cluster:projection-type 1 or 2 (= "2-1", default) */
+    int32_t cc_maxiter;           /* coupled-cluster:max-iterations (2000) */
+    double cc_eps;                /* coupled-cluster:accuracy, as 10^-value (1e-12) */
+    double t1_step, t2_step;      /* coupled-cluster:t1-step, t2-step (1, 1) */
+    int32_t diis_enabled;         /* coupled-cluster:diis-enabled (1) */
+    int32_t diis_steps;           /* coupled-cluster:diis-steps (20, range 2..50) */
+    int32_t check_divergence;     /* iteration:enable-divergence-check (1) */
+    double divergence_threshold;  /* iteration:divergence-threshold, as 10^value (1e3) */
+    int32_t check_stagnation;     /* iteration:enable-stagnation-check (1) */
+    double stagnation_threshold;  /* iteration:stagnation-threshold, percent (60) */
+    int32_t stagnation_after;     /* iteration:stagnation-check-after (200) */
+    int32_t precision;            /* HX_PRECISION_FP64 (default) or HX_PRECISION_MIXED */
+    int32_t guess;                /* 0 reference guess (guessCC), 1 learned guess */
+} hx_cc_params;
+
+typedef struct hx_ccsd hx_ccsd;
+
+/* Fill p with helios's defaults. */
+void hx_cc_params_default(hx_cc_params *p);
+
+/* setCCParameters('r-ccsd') (mod_cc.f90:82-485; r-ccsd branch :415-428): build
+ * the PPP Hamiltonian of one molecule and allocate the device state. */
+int hx_ccsd_create(const hx_ppp_model *m, const hx_cc_params *p, hx_ccsd **out);
+
+/* The same for n molecules solved together (one batched launch per step). */
+int hx_ccsd_create_batch(const hx_ppp_model *ms, int32_t n, const hx_cc_params *p, hx_ccsd **out);
+
+/* initCC r-ccsd (mod_cc.f90:489-603, :538-558, guessCC :634-650): RHF SCF,
+ * MO Fock, reference energy, integrals and the starting amplitudes. */
+int hx_ccsd_init(hx_ccsd *h);
+
+/* Replace molecule mol's amplitudes (reference layout, see above). */
+int hx_ccsd_set_guess(hx_ccsd *h, int32_t mol, const double *t1, const double *t2);
+
+/* iterationCC (mod_cc.f90:820-891) for every active molecule: residuals,
+ * Jacobi step, DIIS. acc[0] = max|d1|, acc[1] = max|d2| of molecule 0
+ * (acc[2..4] = -1, as the reference fills them). */
+int hx_ccsd_iterate(hx_ccsd *h, int32_t iteration, double eps, double acc[5]);
+
+/* energyCC r-ccsd (mod_cc.f90:1916-1952) of molecule 0: e[0] total,
+ * e[1] reference energy, e[2] singles part, e[3] doubles part, e[4] 0. */
+int hx_ccsd_energy(hx_ccsd *h, double e[5]);
+
+/* iterator(iterationCC, energyCC, maxiter, eps) (gIterator.f90:1-210) for
+ * molecule 0; *status gets the iterator status (1, -1, -2, -3, -4). */
+int hx_ccsd_solve(hx_ccsd *h, int32_t maxiter, double eps, int32_t *status, int32_t *iters,
+                  double e[5]);
+
+/* The iterator for every molecule of a batch; arrays have n entries (e: n x 5). */
+int hx_ccsd_solve_batch(hx_ccsd *h, int32_t *status, int32_t *iters, double *e);
+
+/* Amplitudes of molecule mol in the reference layout (t1: o*v, t2: o*o*v*v). */
+int hx_ccsd_get_amplitudes(hx_ccsd *h, int32_t mol, double *t1, double *t2);
+
+/* SCF results of molecule mol: C (N x N, column p = MO p, row-major [site][MO]),
+ * orbital energies (N), MO Fock (N x N row-major); scf[0..3] = E_total, E_el,
+ * E_nuc, last accuracy; scf_status[0..1] = status, iterations. Any pointer may
+ * be NULL. */
+int hx_ccsd_get_scf(hx_ccsd *h, int32_t mol, double *C, double *eps, double *fmo, double scf[4],
+                    int32_t scf_status[2]);
+
+/* Sizes of molecule mol: dims[0..3] = N, o, v, electrons. */
+int hx_ccsd_dims(hx_ccsd *h, int32_t mol, int32_t dims[4]);
+
+/* Request a cooperative stop (the reference's stop-iteration / SIGUSR1); safe
+ * from any thread. The running solve ends with status -4 after the current
+ * iteration. */
+void hx_ccsd_cancel(hx_ccsd *h);
+
+/* finalizeCC: free the device state. */
+void hx_ccsd_destroy(hx_ccsd *h);
+
+/* Copy the message of the last error (thread-local) into buf; returns its length. */
+int hx_last_error(char *buf, size_t len);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HELIOS_CC_H */
