@@ -1,0 +1,419 @@
+"""Benchmark of the GB300 closed-shell PPP CCSD engine (helios r-ccsd).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Workload (N = 1 per GPU): the 160-site polyene (o = v = 80), the single-GPU
+configuration the headline metric is quoted on. One step = one full solve
+through the engine: RHF SCF, integrals, guess and the CCSD iteration to
+|dE_corr| <= 1e-6 eV, in mixed precision (exact-slice BF16 tcgen05
+contractions, FP64 finishing iterations; stop rule: FP64 residual < 1e-7).
+value = polyene solves per second over all ranks (replicas: every rank solves
+its own polyene, no device collective). The same line carries the plain FP64
+GPU path's time to 1e-6 eV on the same molecule, the 512-molecule ensemble
+throughput, the roofline of the dominant kernel (the tcgen05 GEMM, timed live
+with CUDA events during the timed steps), the end-to-end number through the
+C ABI with host buffers, the SM clocks seen during the timed region and a CPU
+baseline (the factorised FP64 oracle, one sampled residual on the host cores).
+
+--impl reference times the reference's own algorithm on the host cores: the
+literal C restatement of its o^4 v^4 r-ccsd (oracle/cc_literal.c) on a bounded
+sample of the doubles residual of the same molecule, scaled to one solve.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "CCSD time-to-1e-6 eV & molecules/s: mixed+learned vs plain FP64, 1 GB300"
+N_SITES = 160
+EPS_TIMED = 1e-7          # FP64 residual that ends a timed solve (|dE| well below 1e-6 eV)
+
+
+def env_rank():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("bf16_tflops"), d.get("bf16_tflops_sustained"), d.get("hbm_gbs"), "measured"
+    return 1900.0, 1700.0, 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    def __init__(self, gpu):
+        self.gpu, self.proc, self.path = gpu, None, None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        mhz, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    mhz.append(float(f[1]))
+                    mx = float(f[2])
+                except ValueError:
+                    continue
+                for k, nm in enumerate(names):
+                    if f[5 + k].lower() == "active":
+                        reasons.add(nm)
+        finally:
+            os.unlink(self.path)
+        return {"sm_mhz": statistics.median(mhz) if mhz else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(mhz)}
+
+
+def time_to_tolerance(trace, e_ref, tol=1e-6):
+    """Seconds into the solve after which |E - e_ref| <= tol holds for every later iteration."""
+    t = None
+    for row in trace:
+        if abs(row[2] - e_ref) <= tol:
+            if t is None:
+                t = row[3]
+        else:
+            t = None
+    return t
+
+
+def golden_polyene():
+    p = os.path.join(ROOT, "tests", "golden", f"polyene{N_SITES}.json")
+    return json.load(open(p)) if os.path.exists(p) else None
+
+
+# ----------------------------------------------------------------------- GB300 arm
+def run_gb300(args):
+    rank, world, local = env_rank()
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        torch.cuda.set_device(0)
+    import __graft_entry__ as g
+    if rank == 0 or world == 1:
+        g.build()
+    if world > 1:
+        dist.barrier()
+    from helios_gb300 import api, molecules
+
+    def barrier_sync():
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    mol = molecules.polyene(N_SITES)
+    kw = api.Keywords(bond_alternation=0.1, accuracy=-__import__("math").log10(EPS_TIMED), precision="mixed",
+                      mixed_switch=1e-6)
+    cc = api.CoupledCluster(mol, kw)
+
+    def step():
+        cc.initCC()
+        r = cc.iterate()
+        tm = cc.timing()
+        return r, tm
+
+    for _ in range(args.warmup):
+        step()
+    peaks = measured_peaks()
+    cc.timing(profile=1)
+    barrier_sync()
+    t0 = time.perf_counter()
+    dev_ms, results, traces = [], [], []
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            r, tm = step()
+            dev_ms.append(tm["init_ms"] + tm["solve_ms"])
+            results.append(r)
+            traces.append(cc.trace(0))
+    barrier_sync()
+    wall = time.perf_counter() - t0
+    prof = cc.timing(profile=0)
+    clocks = clk.summary()
+    step_ms = max(dev_ms) if dev_ms else float("nan")
+    if world > 1:
+        t = torch.tensor([wall, step_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        wall, step_ms = float(t[0]), float(t[1])
+    ms_per_step = 1e3 * wall / args.steps
+    value = world * args.steps / wall
+    last = results[-1]
+    cc.finalizeCC()
+
+    if rank != 0:
+        if world > 1:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    gold = golden_polyene()
+    e_final = float(last["energy"][0])
+    extra = {}
+    # --- plain FP64 GPU path on the same molecule (one solve, rank 0)
+    e_ref = gold["energy"][0] if gold else None
+    if args.fp64_compare:
+        c64 = api.CoupledCluster(mol, api.Keywords(bond_alternation=0.1, accuracy=10, precision="fp64"))
+        c64.initCC()
+        r64 = c64.iterate()
+        tr64 = c64.trace(0)
+        t64 = c64.timing()
+        c64.finalizeCC()
+        if e_ref is None:
+            e_ref = float(r64["energy"][0])
+        t_fp64 = time_to_tolerance(tr64, e_ref)
+        extra["fp64_plain"] = {"status": int(r64["status"]), "iterations": int(r64["iterations"]),
+                               "scf_s": t64["init_ms"] / 1e3,
+                               "time_to_1e-6_eV_s": None if t_fp64 is None else t64["init_ms"] / 1e3 + t_fp64,
+                               "s_per_iteration": float(tr64[-1, 3] / len(tr64)), "E_total": float(r64["energy"][0])}
+    # --- the mixed path's own accuracy and time to 1e-6 eV
+    tr = traces[-1]
+    t_mixed = time_to_tolerance(tr, e_ref) if e_ref is not None else None
+    mixed = {"status": int(last["status"]), "iterations": int(last["iterations"]),
+             "tensor_core_iterations": int(tr[:, 4].sum()), "E_total": e_final,
+             "dE_vs_fp64_oracle_eV": None if e_ref is None else abs(e_final - e_ref),
+             "reference_energy": "FP64 oracle (tests/golden)" if gold else "FP64 GPU path",
+             "time_to_1e-6_eV_s": None if t_mixed is None else tm["init_ms"] / 1e3 + t_mixed,
+             "solve_s": step_ms / 1e3}
+    extra["mixed"] = mixed
+    if args.fp64_compare and mixed["time_to_1e-6_eV_s"] and extra["fp64_plain"]["time_to_1e-6_eV_s"]:
+        extra["speedup_mixed_vs_fp64"] = extra["fp64_plain"]["time_to_1e-6_eV_s"] / mixed["time_to_1e-6_eV_s"]
+    # --- ensemble of 512 random molecules (8..64 sites) in one batched handle
+    if args.batch > 0:
+        mols = molecules.ensemble(20261203, args.batch)
+        cb = api.CoupledCluster(mols, api.Keywords(bond_alternation=0.1, accuracy=8, precision="mixed"))
+        cb.initCC()
+        cb.solve_batch()
+        cb.initCC()
+        out = cb.solve_batch()
+        tb = cb.timing()
+        cb.finalizeCC()
+        secs = (tb["init_ms"] + tb["solve_ms"]) / 1e3
+        extra["batch"] = {"molecules": args.batch, "seconds": secs, "molecules_per_s": args.batch / secs,
+                          "converged": int((out["status"] == 1).sum()),
+                          "mean_iterations": float(out["iterations"].mean())}
+    # --- end to end through the C ABI with host buffers
+    e2e = run_e2e(api, mol, kw, max(1, min(args.steps, 3)))
+    # --- roofline of the tcgen05 GEMM, live over the timed steps
+    peak = peaks[1] if peaks[1] else peaks[0]
+    achieved = prof["gemm_flops"] / (prof["gemm_ms"] * 1e-3) / 1e12 if prof["gemm_ms"] > 0 else None
+    hw = prof["gemm_hw_flops"] / (prof["gemm_ms"] * 1e-3) / 1e12 if prof["gemm_ms"] > 0 else None
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "tc_gemm_traffic.json")
+    if os.path.exists(tpath):
+        traffic = json.load(open(tpath)).get("bytes_per_launch_full_size")
+    roof = {"kernel": "tc::tc_gemm (exact-slice BF16, tcgen05)", "bound": "tensor",
+            "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": None if achieved is None else achieved / peak, "traffic": traffic,
+            "peak_kind": f"bf16 sustained ({peaks[3]})",
+            "achieved_tensor_flops_issued": hw, "frac_tensor_issued": None if hw is None else hw / peak,
+            "launches": prof["gemm_launches"], "gemm_ms_total": prof["gemm_ms"],
+            "share_of_step": prof["gemm_ms"] / sum(dev_ms) if dev_ms else None}
+    cpu = cpu_baseline_factorised(args)
+    line = {
+        "metric": METRIC, "value": value, "unit": "molecules/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16 exact integer slices (tcgen05) + f64",
+        "data": "synthetic (generated PPP polyene, no dataset)",
+        "config": {"workload": f"polyene-{N_SITES} r-ccsd (o=v=80), bond-alternation 0.1, Ohno-Klopman, "
+                               "mixed precision + FP64 finish, stop at FP64 residual 1e-7",
+                   "step": "RHF SCF + integrals + guess + CCSD to convergence (device time)",
+                   "l2": "inputs larger than L2 (t2 alone is 328 MB)", "parallelism": f"replicas x{world}"},
+        "roofline": roof, "cpu_baseline": cpu,
+        "e2e": e2e, "gpu_launches": prof["kernel_launches"], "clocks": clocks,
+        "device_ms_per_step": statistics.mean(dev_ms), **extra,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def run_e2e(api, mol, kw, steps):
+    """Solves through the C ABI from host arrays: create (H2D model) .. energy (D2H) .. destroy."""
+    import numpy as np
+    n = mol.n_sites
+    h2d = 3 * n * n * 8 + n * (3 * 8 + 8 + 8 + 4) + len(mol.bonds) * (4 + 4 + 8 + 4)
+    ts = []
+    value = None
+    for _ in range(steps + 1):
+        t0 = time.perf_counter()
+        cc = api.CoupledCluster(mol, kw)
+        cc.initCC()
+        r = cc.iterate()
+        e = np.array(r["energy"])
+        cc.finalizeCC()
+        ts.append(time.perf_counter() - t0)
+        value = e
+    t = statistics.mean(ts[1:])
+    return {"value": 1.0 / t, "unit": "molecules/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 5 * 8,
+            "seconds_per_step": t, "note": "hx_ccsd_create + init + solve + energy + destroy, host wall clock"}
+
+
+# ----------------------------------------------------------------------- CPU baselines
+def _fact_sample(nthreads):
+    """One factorised FP64 oracle residual on the polyene: seconds."""
+    import numpy as np
+    from helios_gb300 import molecules
+    from oracle import ccsd_fact
+    from oracle.ppp import build_model
+    from oracle.rhf import mo_fock, rhf
+    mol = molecules.polyene(N_SITES)
+    model = build_model(mol, alternation=0.1)
+    scf = rhf(model)
+    F, eref = mo_fock(model, scf["V"], scf["D"])
+    o = model["nel"] // 2
+    I = ccsd_fact.Integrals(scf["V"], model["G"], o)
+    t1, t2 = ccsd_fact.guess(F, I, o)
+    t0 = time.perf_counter()
+    ccsd_fact.residuals(F, I, t1, t2)
+    return time.perf_counter() - t0
+
+
+def iterations_to_tolerance(tol=1e-6):
+    gold = golden_polyene()
+    if not gold:
+        return 40, "assumed 40 (no oracle trace committed)"
+    e = gold["energy"][0]
+    tr = gold["trace"]
+    n = None
+    for k, row in enumerate(tr):
+        if abs(row[2] - e) <= tol:
+            if n is None:
+                n = k + 1
+        else:
+            n = None
+    return n or gold["iterations"], "from the committed FP64 oracle trace (tests/golden)"
+
+
+def cpu_baseline_factorised(args):
+    if args.no_cpu:
+        return None
+    cores = os.cpu_count() or 1
+    secs = _fact_sample(cores)
+    nit, how = iterations_to_tolerance()
+    per_solve = secs * nit
+    return {"value": 1.0 / per_solve, "unit": "molecules/s", "cores": cores, "kind": "port",
+            "sample": f"one residual evaluation of the factorised FP64 oracle (numpy/OpenBLAS, {cores} threads) "
+                      f"on polyene-{N_SITES}: {secs:.1f} s, times {nit} iterations to 1e-6 eV ({how}); "
+                      "RHF and integrals not counted"}
+
+
+def run_reference(args):
+    rank, world, local = env_rank()
+    if rank != 0:
+        return
+    import numpy as np
+    from helios_gb300 import molecules
+    from oracle import literal
+    from oracle import build as ob
+    from oracle.ppp import build_model
+    from oracle.rhf import mo_fock, rhf
+    ob.build()
+    mol = molecules.polyene(N_SITES)
+    model = build_model(mol, alternation=0.1)
+    scf = rhf(model)
+    F, eref = mo_fock(model, scf["V"], scf["D"])
+    o = model["nel"] // 2
+    v = N_SITES - o
+    ne = o * v
+    # full R(p,q,r,s) = 2(pq|rs) - (ps|rq) as the reference stores it (5.2 GB), built by GEMMs
+    C, G = scf["V"], model["G"]
+    B = np.einsum("mp,mq->mpq", C, C).reshape(N_SITES, -1)
+    J = (B.T @ (G @ B)).reshape(N_SITES, N_SITES, N_SITES, N_SITES)
+    R = 2.0 * J - J.transpose(0, 3, 2, 1)
+    del J, B
+    from oracle import ccsd_fact
+    I = ccsd_fact.Integrals(C, G, o)
+    t1, t2 = ccsd_fact.guess(F, I, o)
+    rng = np.random.default_rng(0)
+    npairs = args.ref_pairs
+    mm = rng.integers(0, ne, size=npairs)
+    nn = rng.integers(0, ne, size=npairs)
+    lo, hi = np.minimum(mm, nn), np.maximum(mm, nn)
+    nit, how = iterations_to_tolerance()
+    times = []
+    for s in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        literal.doubles_sample(F, R, t1, t2, lo, hi)
+        dt = time.perf_counter() - t0
+        if s >= args.warmup:
+            times.append(dt)
+    per_pair = statistics.mean(times) / npairs
+    per_iter = per_pair * ne * (ne + 1) / 2
+    per_solve = per_iter * nit
+    value = 1.0 / per_solve
+    cores = literal.lib().orc_num_threads()
+    sample = (f"literal reference r-ccsd doubles residual (oracle/cc_literal.c, OpenMP {cores} threads) on "
+              f"{npairs} random excitation pairs of polyene-{N_SITES} per step: {statistics.mean(times):.2f} s; "
+              f"scaled to all {ne*(ne+1)//2} pairs = {per_iter:.3g} s per iteration, times {nit} iterations "
+              f"({how}); singles, step, DIIS and SCF not counted")
+    line = {"metric": METRIC, "value": value, "unit": "molecules/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (generated PPP polyene)",
+            "config": {"workload": f"polyene-{N_SITES} r-ccsd (o=v=80), bond-alternation 0.1, Ohno-Klopman"},
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "molecules/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "molecules/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--batch", type=int, default=512, help="molecules of the ensemble leg (0 = skip)")
+    ap.add_argument("--no-fp64-compare", dest="fp64_compare", action="store_false")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--ref-pairs", type=int, default=48, help="doubles pairs per reference-arm step")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        print("bench.py: at least 3 warm-up steps are required", file=sys.stderr)
+        sys.exit(2)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

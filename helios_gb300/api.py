@@ -46,7 +46,8 @@ class CCParams(ctypes.Structure):
                 ("t2_step", ctypes.c_double), ("diis_enabled", ctypes.c_int32), ("diis_steps", ctypes.c_int32),
                 ("check_divergence", ctypes.c_int32), ("divergence_threshold", ctypes.c_double),
                 ("check_stagnation", ctypes.c_int32), ("stagnation_threshold", ctypes.c_double),
-                ("stagnation_after", ctypes.c_int32), ("precision", ctypes.c_int32), ("guess", ctypes.c_int32)]
+                ("stagnation_after", ctypes.c_int32), ("precision", ctypes.c_int32), ("guess", ctypes.c_int32),
+                ("mixed_switch", ctypes.c_double), ("mixed_patience", ctypes.c_int32)]
 
 
 class HxError(RuntimeError):
@@ -71,10 +72,24 @@ def library():
         lib.hx_ccsd_destroy.restype = None
         for name in ("hx_ccsd_create", "hx_ccsd_create_batch", "hx_ccsd_init", "hx_ccsd_set_guess",
                      "hx_ccsd_iterate", "hx_ccsd_energy", "hx_ccsd_solve", "hx_ccsd_solve_batch",
-                     "hx_ccsd_get_amplitudes", "hx_ccsd_get_scf", "hx_ccsd_dims", "hx_last_error"):
+                     "hx_ccsd_get_amplitudes", "hx_ccsd_get_scf", "hx_ccsd_dims", "hx_ccsd_trace",
+                     "hx_gemm", "hx_ccsd_timing", "hx_last_error"):
             getattr(lib, name).restype = ctypes.c_int
         _lib = lib
     return _lib
+
+
+def gemm(A, B, precision="fp64", reps=1):
+    """C = A @ B.T on the engine's FP64 or tensor-core GEMM; returns (C, ms per launch)."""
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    B = np.ascontiguousarray(B, dtype=np.float64)
+    M, K = A.shape
+    N = B.shape[0]
+    C = np.zeros((M, N))
+    ms = ctypes.c_double()
+    _check(library().hx_gemm(A.ctypes.data_as(_c_d), B.ctypes.data_as(_c_d), C.ctypes.data_as(_c_d), M, N, K,
+                             {"fp64": 0, "mixed": 1}[precision], reps, ctypes.byref(ms)))
+    return C, ms.value
 
 
 def last_error() -> str:
@@ -112,6 +127,8 @@ class Keywords:
     stagnation_check_after: int = 200            # iteration:stagnation-check-after
     precision: str = "fp64"                      # engine: "fp64" or "mixed"
     guess: str = "reference"                     # engine: "reference" (guessCC) or "learned"
+    mixed_switch: float = 1e-6                   # engine: residual where mixed hands over to FP64
+    mixed_patience: int = 3                      # engine: non-improving mixed iterations before FP64
 
     def to_c(self) -> CCParams:
         p = CCParams()
@@ -136,6 +153,8 @@ class Keywords:
         p.stagnation_after = self.stagnation_check_after
         p.precision = {"fp64": 0, "mixed": 1}[self.precision]
         p.guess = {"reference": 0, "learned": 1}[self.guess]
+        p.mixed_switch = self.mixed_switch
+        p.mixed_patience = self.mixed_patience
         return p
 
 
@@ -231,6 +250,21 @@ class CoupledCluster:
                                          fmo.ctypes.data_as(_c_d), out.ctypes.data_as(_c_d), st.ctypes.data_as(_c_i)))
         return {"C": C, "eps": eps, "F": fmo, "energy": out[0], "eel": out[1], "enuc": out[2],
                 "accuracy": out[3], "status": int(st[0]), "iterations": int(st[1])}
+
+    def trace(self, mol: int = 0) -> np.ndarray:
+        """Per-iteration (max|d1|, max|d2|, E_total, seconds, mixed?) of the last solve."""
+        n = _check(library().hx_ccsd_trace(self._h, mol, None, 0))
+        out = np.zeros((max(n, 1), 5))
+        library().hx_ccsd_trace(self._h, mol, out.ctypes.data_as(_c_d), n)
+        return out[:n]
+
+    def timing(self, profile: int = -1) -> dict:
+        """Device timing of the last init/solve and the tcgen05 GEMM totals (see hx_ccsd_timing)."""
+        out = np.zeros(8)
+        _check(library().hx_ccsd_timing(self._h, out.ctypes.data_as(_c_d), profile))
+        return {"init_ms": out[0], "solve_ms": out[1], "gemm_launches": int(out[2]), "gemm_ms": out[3],
+                "gemm_flops": out[4], "gemm_hw_flops": out[5], "device_bytes": int(out[6]),
+                "kernel_launches": int(out[7])}
 
     def cancel(self):
         library().hx_ccsd_cancel(self._h)

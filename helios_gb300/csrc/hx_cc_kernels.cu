@@ -198,8 +198,12 @@ __global__ void k_step(const CCMol *mols, const DiisMol *diis, const int *active
             int j = (int)(r % o); r /= o;
             int a = (int)(r % v);
             int i = (int)(r / v);
-            double w = m.r2[f];
-            double d2 = 2.0 * w - m.r2[(((long long)i * v + b) * o + j) * v + a];
+            // as the reference, each pair (ia),(jb) takes the value computed for
+            // (ia) <= (jb), so the amplitudes stay exactly pair-symmetric
+            const long long p1 = (long long)i * v + a, q1 = (long long)j * v + b;
+            const long long p2 = (long long)i * v + b, q2 = (long long)j * v + a;
+            double w = m.r2[min(p1, q1) * ov + max(p1, q1)];
+            double d2 = 2.0 * w - m.r2[min(p2, q2) * ov + max(p2, q2)];
             mx2 = fmax(mx2, fabs(d2));
             double t = m.t2[f] + 3.0 * s2 * w / m.D2[f];
             m.t2[f] = t;
@@ -240,23 +244,22 @@ __global__ void k_diis_dots(const CCMol *mols, const DiisMol *diis, const int *a
     if (!(fmax(m.res[0], m.res[1]) >= eps)) return;      // converged: the reference skips DIIS
     const long long ov = (long long)m.o * m.v;
     const int cnt = h.count[0] + 1, n = cnt < h.nd ? cnt : h.nd;
+    const int k = blockIdx.z;                             // stored vector of this block
+    if (k >= n) return;
     const int slot = h.count[0] % h.nd;
     const double *en = h.He + (long long)slot * h.L;
-    double acc[HX_MAX_DIIS];
-    for (int k = 0; k < n; ++k) acc[k] = 0.0;
+    const double *ek = h.He + (long long)k * h.L;
+    double acc = 0.0;
     GRID_LOOP(e, h.L) {
         double w = 1.0;
         if (e >= ov) {
             long long f = e - ov, p = f / ov, q = f % ov;
             w = (p == q) ? 1.0 : 0.5;
         }
-        double x = w * en[e];
-        for (int k = 0; k < n; ++k) acc[k] += x * h.He[(long long)k * h.L + e];
+        acc += w * en[e] * ek[e];
     }
-    for (int k = 0; k < n; ++k) {
-        double r = block_red(acc[k], false);
-        if (threadIdx.x == 0) part[((long long)blockIdx.y * nblk + blockIdx.x) * HX_MAX_DIIS + k] = r;
-    }
+    double r = block_red(acc, false);
+    if (threadIdx.x == 0) part[((long long)blockIdx.y * nblk + blockIdx.x) * HX_MAX_DIIS + k] = r;
 }
 
 // Ordered sum of the partial dots into the Gram matrix (slot indexing), then
@@ -317,7 +320,10 @@ __global__ void k_diis_solve(const CCMol *mols, const DiisMol *diis, const int *
         for (int c = k + 1; c < nb; ++c) s -= A[k * nb + c] * x[c];
         x[k] = s / A[k * nb + k];
     }
-    for (int k = 0; k < n; ++k) h.coef[k] = x[k];
+    for (int k = 0; k < n; ++k) {
+        if (!isfinite(x[k])) { h.coef[HX_MAX_DIIS] = 0.0; return; }   // singular subspace: no mixing
+        h.coef[k] = x[k];
+    }
     h.coef[HX_MAX_DIIS] = (double)n;     // number of vectors to mix
 }
 
@@ -448,6 +454,7 @@ static inline dim3 grid_for(long long work, int nmol, int cap = 4096)
 #define LAUNCH_EW(kern, work, ...)                                                   \
     do {                                                                             \
         kern<<<grid_for(work, nmol), NT, 0, s>>>(__VA_ARGS__);                       \
+        hx_count_launches(1);                                                        \
         cudaError_t e_ = cudaGetLastError();                                         \
         if (e_ != cudaSuccess) return e_;                                            \
     } while (0)
@@ -483,6 +490,7 @@ cudaError_t hx_step(const CCMol *m, const DiisMol *h, const int *act, int nmol, 
                     int use_diis, double *part, int nblk, cudaStream_t s)
 {
     k_step<<<dim3(nblk, nmol), NT, 0, s>>>(m, h, act, s1, s2, use_diis, part, nblk);
+    hx_count_launches(2);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_step_finish<<<nmol, 32, 0, s>>>(m, act, part, nblk);
@@ -490,9 +498,10 @@ cudaError_t hx_step(const CCMol *m, const DiisMol *h, const int *act, int nmol, 
 }
 
 cudaError_t hx_diis(const CCMol *m, const DiisMol *h, const int *act, int nmol, double eps, double *part,
-                    int nblk, cudaStream_t s)
+                    int nblk, int nd_max, cudaStream_t s)
 {
-    k_diis_dots<<<dim3(nblk, nmol), NT, 0, s>>>(m, h, act, eps, part, nblk);
+    k_diis_dots<<<dim3(nblk, nmol, nd_max), NT, 0, s>>>(m, h, act, eps, part, nblk);
+    hx_count_launches(3);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_diis_solve<<<nmol, 32, 0, s>>>(m, h, act, eps, part, nblk);
@@ -505,6 +514,7 @@ cudaError_t hx_diis(const CCMol *m, const DiisMol *h, const int *act, int nmol, 
 cudaError_t hx_energy(const CCMol *m, const int *act, int nmol, double *part, int nblk, cudaStream_t s)
 {
     k_energy<<<dim3(nblk, nmol), NT, 0, s>>>(m, act, part, nblk);
+    hx_count_launches(2);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_energy_finish<<<nmol, 32, 0, s>>>(m, act, part, nblk);

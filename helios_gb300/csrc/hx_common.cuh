@@ -24,6 +24,8 @@ struct TgemmDesc {
     long long a[5], b[5], c[5];
     double alpha, beta;
     int mol;            // molecule index (skipped when that molecule is inactive)
+    int ksplit;         // K is cut into ksplit slices accumulated atomically (needs beta == 1)
+    int a_const, b_const;   // operand unchanged between hx_ccsd_init calls (prepared once)
     int tiles_m, tiles_n;
     long long tile_start;   // prefix sum of batch*tiles_m*tiles_n over the group
 };
@@ -39,3 +41,5 @@ struct TgemmDesc {
     } while (0)
 
 void hx_set_error(const char *fmt, ...);
+// Count kernel launches of the engine (read back through hx_ccsd_timing).
+void hx_count_launches(int n);

@@ -1,7 +1,9 @@
 // Host side of the engine: PPP model, device state, the contraction plan of one
 // CCSD iteration, the iterator, and the C ABI of include/helios_cc.h.
 #include <algorithm>
+#include <array>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstring>
@@ -14,6 +16,9 @@
 
 // ---------------------------------------------------------------- errors
 static thread_local char g_err[1024];
+static std::atomic<long long> g_launches{0};
+
+void hx_count_launches(int n) { g_launches.fetch_add(n); }
 
 void hx_set_error(const char *fmt, ...)
 {
@@ -158,12 +163,6 @@ struct Rules {   // gIterator.f90:88-210
     }
 };
 
-struct Group {   // one grouped tgemm launch
-    std::vector<TgemmDesc> h;
-    TgemmDesc *d = nullptr;
-    long long tiles = 0;
-};
-
 struct hx_ccsd {
     hx_cc_params p{};
     int nmol = 0;
@@ -183,7 +182,7 @@ struct hx_ccsd {
     std::vector<int> active;
     double *d_part = nullptr;
     double *d_res = nullptr;             // nmol x 8 iteration results (inside the arena)
-    int nblk = 64;
+    int nblk = 64;                       // blocks per molecule of the reductions (set at allocation)
     std::vector<Group> plan;             // GEMM groups of one iteration (in order)
     std::vector<Group> setup_groups;
     long long maxw_nn = 0, maxw_ov = 0, maxw_pair = 0, maxw_oNoN = 0;
@@ -194,6 +193,15 @@ struct hx_ccsd {
     std::vector<Rules> rules;
     std::vector<int> status;
     tc::Engine *tce = nullptr;           // tensor-core backend (mixed precision)
+    // mixed precision: per-molecule phase (1 = tensor-core iterations) and masks
+    std::vector<int> phase_tc, stall;
+    std::vector<double> best;
+    int *d_act_tc = nullptr, *d_act_fp = nullptr;
+    std::vector<std::vector<std::array<double, 5>>> trace;
+    // device time of the last hx_ccsd_init and solve (events on st)
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    float init_ms = 0.f, solve_ms = 0.f;
+    double prof[4] = {0, 0, 0, 0};
 };
 
 // ---------------------------------------------------------------- plan helpers
@@ -212,6 +220,26 @@ static TgemmDesc tg(const double *A, const double *B, double *C, int batch, int 
     return d;
 }
 
+// Operands that stay fixed between hx_ccsd_init calls: the tensor-core
+// backend slices them once per initialisation.
+static void mark_constants(hx_ccsd *h)
+{
+    for (auto &g : h->plan)
+        for (auto &d : g.h) {
+            const CCMol &m = h->cc[d.mol];
+            auto fixed = [&](const double *p) {
+                const double *lo[] = {m.Cmo, m.G, m.gov, m.Lov, m.Bov0, m.GBov0};
+                const size_t n[] = {(size_t)m.N * m.N, (size_t)m.N * m.N, (size_t)m.o * m.v * m.o * m.v,
+                                    (size_t)m.o * m.v * m.o * m.v, (size_t)m.N * m.o * m.v, (size_t)m.N * m.o * m.v};
+                for (int k = 0; k < 6; ++k)
+                    if (p >= lo[k] && p < lo[k] + n[k]) return 1;
+                return 0;
+            };
+            d.a_const = fixed(d.A);
+            d.b_const = fixed(d.B);
+        }
+}
+
 static int upload_group(Group &g)
 {
     g.tiles = hx_tgemm_f64_prepare(g.h.data(), (int)g.h.size());
@@ -221,15 +249,42 @@ static int upload_group(Group &g)
     return HX_OK;
 }
 
+// Molecules in their tensor-core phase run the group on tcgen05 (d_act_tc),
+// the others on the FP64 kernel (d_act_fp); each kernel skips the rest.
 static int run_group(hx_ccsd *h, Group &g)
 {
     if (g.tiles == 0) return HX_OK;
-    if (h->p.precision == HX_PRECISION_MIXED && h->tce) {
-        cudaError_t e = tc::run_group(h->tce, g.h.data(), (int)g.h.size(), h->active.data(), h->st);
-        if (e != cudaSuccess) { hx_set_error("tensor-core group: %s", cudaGetErrorString(e)); return HX_ERR_CUDA; }
+    if (h->tce) {
+        int n_tc = 0, n_fp = 0;
+        for (int mi = 0; mi < h->nmol; ++mi) {
+            if (!h->active[mi]) continue;
+            if (h->phase_tc[mi]) ++n_tc; else ++n_fp;
+        }
+        if (n_tc) {
+            cudaError_t e = tc::run_group(h->tce, g.h.data(), (int)g.h.size(), h->d_act_tc, h->st);
+            if (e != cudaSuccess) { hx_set_error("tensor-core group: %s", cudaGetErrorString(e)); return HX_ERR_CUDA; }
+        }
+        if (n_fp) HX_CU(hx_tgemm_f64_launch(g.d, (int)g.h.size(), g.tiles, h->d_act_fp, h->st));
         return HX_OK;
     }
     HX_CU(hx_tgemm_f64_launch(g.d, (int)g.h.size(), g.tiles, h->d_active, h->st));
+    return HX_OK;
+}
+
+static int upload_masks(hx_ccsd *h)
+{
+    std::vector<int> a(h->nmol), b(h->nmol);
+    for (int mi = 0; mi < h->nmol; ++mi) {
+        a[mi] = h->active[mi] && h->phase_tc[mi];
+        b[mi] = h->active[mi] && !h->phase_tc[mi];
+    }
+    HX_CU(cudaMemcpyAsync(h->d_active, h->active.data(), sizeof(int) * h->nmol, cudaMemcpyHostToDevice, h->st));
+    if (h->d_act_tc) {
+        HX_CU(cudaMemcpyAsync(h->d_act_tc, a.data(), sizeof(int) * h->nmol, cudaMemcpyHostToDevice, h->st));
+        HX_CU(cudaMemcpyAsync(h->d_act_fp, b.data(), sizeof(int) * h->nmol, cudaMemcpyHostToDevice, h->st));
+    }
+    // the masks are pageable host vectors: wait so they may go out of scope
+    HX_CU(cudaStreamSynchronize(h->st));
     return HX_OK;
 }
 
@@ -377,8 +432,18 @@ static int allocate(hx_ccsd *h)
     HX_CU(cudaMalloc(&h->d_cc, sizeof(CCMol) * h->nmol));
     HX_CU(cudaMalloc(&h->d_diis, sizeof(DiisMol) * h->nmol));
     HX_CU(cudaMalloc(&h->d_active, sizeof(int) * h->nmol));
-    HX_CU(cudaMalloc(&h->d_part, sizeof(double) * (size_t)h->nmol * h->nblk * HX_MAX_DIIS));
+    // reductions: enough blocks per molecule to fill the GPU, capped by the work
+    long long maxpair = 0;
+    for (int mi = 0; mi < h->nmol; ++mi) maxpair = std::max<long long>(maxpair, (long long)h->o[mi] * h->v[mi] * h->o[mi] * h->v[mi]);
+    h->nblk = (int)std::max<long long>(1, std::min<long long>(std::max(1, 1216 / h->nmol), (maxpair + 4095) / 4096));
+    HX_CU(cudaMalloc(&h->d_part, sizeof(double) * std::max<size_t>((size_t)h->nmol * h->nblk * HX_MAX_DIIS, 2 * HX_SCF_GRID_MAX)));
+    HX_CU(cudaMalloc(&h->d_act_tc, sizeof(int) * h->nmol));
+    HX_CU(cudaMalloc(&h->d_act_fp, sizeof(int) * h->nmol));
     h->active.assign(h->nmol, 1);
+    h->phase_tc.assign(h->nmol, 0);
+    h->stall.assign(h->nmol, 0);
+    h->best.assign(h->nmol, 1e300);
+    h->trace.assign(h->nmol, {});
     h->res.assign((size_t)h->nmol * 8, 0.0);
     h->status.assign(h->nmol, 0);
     h->rules.assign(h->nmol, Rules());
@@ -419,6 +484,8 @@ void hx_cc_params_default(hx_cc_params *p)
     p->stagnation_after = 200;
     p->precision = HX_PRECISION_FP64;
     p->guess = 0;
+    p->mixed_switch = 1e-6;
+    p->mixed_patience = 3;
 }
 
 int hx_ccsd_create_batch(const hx_ppp_model *ms, int32_t n, const hx_cc_params *p, hx_ccsd **out)
@@ -458,6 +525,7 @@ int hx_ccsd_create_batch(const hx_ppp_model *ms, int32_t n, const hx_cc_params *
     rc = upload_views(h);
     if (rc < 0) { hx_ccsd_destroy(h); return rc; }
     build_plan(h);
+    mark_constants(h);
     for (auto &g : h->plan) {
         rc = upload_group(g);
         if (rc < 0) { hx_ccsd_destroy(h); return rc; }
@@ -510,7 +578,11 @@ int hx_ccsd_init(hx_ccsd *h)
     sp.stag_after = h->p.stagnation_after;
     sp.check_div = h->p.check_divergence;
     sp.check_stag = h->p.check_stagnation;
-    HX_CU(hx_scf_launch(h->d_scf, h->nmol, sp, h->st));
+    int nmax = 0;
+    for (int mi = 0; mi < h->nmol; ++mi) nmax = std::max(nmax, h->N[mi]);
+    if (!h->ev[0]) for (int k = 0; k < 4; ++k) HX_CU(cudaEventCreate(&h->ev[k]));
+    HX_CU(cudaEventRecord(h->ev[0], h->st));
+    HX_CU(hx_scf_launch(h->d_scf, h->nmol, nmax, sp, h->d_part, h->st));
     std::vector<double> out(4);
     std::vector<int> st(2);
     HX_CU(cudaStreamSynchronize(h->st));
@@ -525,10 +597,13 @@ int hx_ccsd_init(hx_ccsd *h)
     }
     HX_TRY(upload_views(h));
     HX_TRY(cc_setup(h, 1));
+    if (h->tce) tc::invalidate(h->tce);          // new orbitals: re-slice the constant operands
     for (int mi = 0; mi < h->nmol; ++mi) { h->rules[mi] = Rules(); h->status[mi] = 0; h->active[mi] = 1; }
     for (int mi = 0; mi < h->nmol; ++mi) HX_CU(cudaMemsetAsync(h->diis[mi].count, 0, sizeof(int), h->st));
     HX_TRY(upload_views(h));
-    HX_CU(cudaStreamSynchronize(h->st));
+    HX_CU(cudaEventRecord(h->ev[1], h->st));
+    HX_TRY(upload_masks(h));
+    cudaEventElapsedTime(&h->init_ms, h->ev[0], h->ev[1]);
     h->initialized = true;
     return HX_OK;
 }
@@ -578,7 +653,7 @@ static int iteration_body(hx_ccsd *h, double eps)
     HX_TRY(run_group(h, P[k++]));                                    // r1 -= Boo UG
     const int use_diis = h->p.diis_enabled ? 1 : 0;
     HX_CU(hx_step(h->d_cc, h->d_diis, h->d_active, nm, h->p.t1_step, h->p.t2_step, use_diis, h->d_part, h->nblk, h->st));
-    if (use_diis) HX_CU(hx_diis(h->d_cc, h->d_diis, h->d_active, nm, eps, h->d_part, h->nblk, h->st));
+    if (use_diis) HX_CU(hx_diis(h->d_cc, h->d_diis, h->d_active, nm, eps, h->d_part, h->nblk, h->p.diis_steps, h->st));
     HX_CU(hx_energy(h->d_cc, h->d_active, nm, h->d_part, h->nblk, h->st));
     return HX_OK;
 }
@@ -613,19 +688,58 @@ int hx_ccsd_energy(hx_ccsd *h, double e[5])
     return HX_OK;
 }
 
+// The iterator (gIterator.f90:88-210) over every active molecule. In mixed
+// precision a molecule starts on the tensor cores and moves on to FP64
+// iterations (keeping its DIIS history) once its residual falls below
+// mixed_switch or stops improving; convergence is only declared on an FP64
+// residual, so the final answer is FP64-verified.
 static int solve_all(hx_ccsd *h, int maxiter, double eps)
 {
     if (h->p.projection_type != 2) { hx_set_error("projection-type 1 is not built on the GPU path"); return HX_ERR_UNSUPPORTED; }
+    const bool mixed = h->tce != nullptr;
     int remaining = 0;
-    for (int mi = 0; mi < h->nmol; ++mi) remaining += h->active[mi];
+    for (int mi = 0; mi < h->nmol; ++mi) {
+        remaining += h->active[mi];
+        h->phase_tc[mi] = mixed ? 1 : 0;
+        h->stall[mi] = 0;
+        h->best[mi] = 1e300;
+        h->trace[mi].clear();
+    }
+    HX_TRY(upload_masks(h));
+    const auto t0 = std::chrono::steady_clock::now();
+    HX_CU(cudaEventRecord(h->ev[2], h->st));
     while (remaining > 0) {
         HX_TRY(iteration_body(h, eps));
         HX_TRY(fetch_results(h));
+        if (h->tce) tc::collect(h->tce, h->prof);
+        const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (h->tce && tc::error_word(h->tce) != 0) {
+            hx_set_error("a tensor-core kernel timed out waiting (code %d)", tc::error_word(h->tce));
+            return HX_ERR_KERNEL;
+        }
         bool changed = false;
         const bool cancel = h->cancel.exchange(0) != 0;
         for (int mi = 0; mi < h->nmol; ++mi) {
             if (!h->active[mi]) continue;
-            double a = std::max(h->res[(size_t)mi * 8 + 0], h->res[(size_t)mi * 8 + 1]);
+            const double *r = &h->res[(size_t)mi * 8];
+            const double a = std::max(r[0], r[1]);
+            h->trace[mi].push_back({r[0], r[1], r[2], secs, (double)h->phase_tc[mi]});
+            if (h->phase_tc[mi] && !cancel) {
+                // tensor-core phase: no convergence claim, hand over to FP64 instead
+                if (a < h->best[mi]) { h->best[mi] = a; h->stall[mi] = 0; } else ++h->stall[mi];
+                const bool handover = a < h->p.mixed_switch || a < eps || h->stall[mi] >= h->p.mixed_patience;
+                Rules &R = h->rules[mi];
+                int s = R.update(handover ? std::max(a, eps * 2) : a, h->p, maxiter, eps, false);
+                if (s == HX_DIVERGED || s == HX_STAGNATED || s == HX_FAILED_MAXITER) {
+                    h->status[mi] = s; h->active[mi] = 0; --remaining; changed = true;
+                } else if (handover) {
+                    // FP64 iterations restart DIIS: error vectors of the tensor-core
+                    // phase are not comparable with FP64 residuals
+                    h->phase_tc[mi] = 0; changed = true;
+                    HX_CU(cudaMemsetAsync(h->diis[mi].count, 0, sizeof(int), h->st));
+                }
+                continue;
+            }
             int s = h->rules[mi].update(a, h->p, maxiter, eps, cancel);
             if (s != 0) {
                 h->status[mi] = s;
@@ -634,13 +748,25 @@ static int solve_all(hx_ccsd *h, int maxiter, double eps)
                 changed = true;
             }
         }
-        if (changed) HX_CU(cudaMemcpyAsync(h->d_active, h->active.data(), sizeof(int) * h->nmol, cudaMemcpyHostToDevice, h->st));
+        if (changed) HX_TRY(upload_masks(h));
     }
+    HX_CU(cudaEventRecord(h->ev[3], h->st));
+    HX_CU(cudaEventSynchronize(h->ev[3]));
+    cudaEventElapsedTime(&h->solve_ms, h->ev[2], h->ev[3]);
     // keep every molecule addressable for getters / energy after the solve
-    for (int mi = 0; mi < h->nmol; ++mi) h->active[mi] = 1;
-    HX_CU(cudaMemcpyAsync(h->d_active, h->active.data(), sizeof(int) * h->nmol, cudaMemcpyHostToDevice, h->st));
-    HX_CU(cudaStreamSynchronize(h->st));
+    for (int mi = 0; mi < h->nmol; ++mi) { h->active[mi] = 1; h->phase_tc[mi] = 0; }
+    HX_TRY(upload_masks(h));
     return HX_OK;
+}
+
+int hx_ccsd_trace(hx_ccsd *h, int32_t mol, double *out, int32_t cap)
+{
+    if (!h || mol < 0 || mol >= h->nmol) { hx_set_error("bad handle or molecule index"); return HX_ERR_ARG; }
+    const auto &t = h->trace[mol];
+    int n = (int)t.size();
+    for (int k = 0; k < n && k < cap && out; ++k)
+        for (int c = 0; c < 5; ++c) out[5 * k + c] = t[k][c];
+    return n;
 }
 
 int hx_ccsd_solve(hx_ccsd *h, int32_t maxiter, double eps, int32_t *status, int32_t *iters, double e[5])
@@ -729,6 +855,24 @@ int hx_ccsd_dims(hx_ccsd *h, int32_t mol, int32_t dims[4])
     return HX_OK;
 }
 
+int hx_ccsd_timing(hx_ccsd *h, double out[8], int32_t profile)
+{
+    if (!h) { hx_set_error("NULL handle"); return HX_ERR_ARG; }
+    if (profile >= 0) {
+        if (h->tce) tc::set_profile(h->tce, profile != 0);
+        if (profile) { for (int k = 0; k < 4; ++k) h->prof[k] = 0.0; g_launches.store(0); }
+    }
+    if (out) {
+        out[0] = h->init_ms;
+        out[1] = h->solve_ms;
+        if (h->tce) tc::collect(h->tce, h->prof);
+        for (int k = 0; k < 4; ++k) out[2 + k] = h->prof[k];
+        out[6] = (double)h->arena_bytes;
+        out[7] = (double)g_launches.load();
+    }
+    return HX_OK;
+}
+
 void hx_ccsd_cancel(hx_ccsd *h)
 {
     if (h) h->cancel.store(1);
@@ -739,15 +883,82 @@ void hx_ccsd_destroy(hx_ccsd *h)
     if (!h) return;
     if (h->st) cudaStreamSynchronize(h->st);
     if (h->tce) tc::destroy(h->tce);
+    for (int k = 0; k < 4; ++k) if (h->ev[k]) cudaEventDestroy(h->ev[k]);
     for (auto &g : h->plan) if (g.d) cudaFree(g.d);
     cudaFree(h->arena);
     cudaFree(h->d_scf);
     cudaFree(h->d_cc);
     cudaFree(h->d_diis);
     cudaFree(h->d_active);
+    cudaFree(h->d_act_tc);
+    cudaFree(h->d_act_fp);
     cudaFree(h->d_part);
     if (h->st) cudaStreamDestroy(h->st);
     delete h;
+}
+
+// C = A B^T for row-major FP64 host matrices, on the engine's FP64 or
+// tensor-core GEMM; reps > 1 repeats the launch and reports the mean time.
+int hx_gemm(const double *A, const double *B, double *C, int32_t M, int32_t N, int32_t K, int32_t precision,
+            int32_t reps, double *ms)
+{
+    if (!A || !B || !C || M <= 0 || N <= 0 || K <= 0 || reps < 1) { hx_set_error("hx_gemm: bad arguments"); return HX_ERR_ARG; }
+    cudaStream_t st;
+    HX_CU(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    double *dA = nullptr, *dB = nullptr, *dC = nullptr;
+    int *dact = nullptr;
+    int rc = HX_OK;
+    tc::Engine *te = nullptr;
+    std::vector<Group> plan(1);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    auto fail = [&](int code) { rc = code; };
+    if (cudaMalloc(&dA, sizeof(double) * (size_t)M * K) != cudaSuccess ||
+        cudaMalloc(&dB, sizeof(double) * (size_t)N * K) != cudaSuccess ||
+        cudaMalloc(&dC, sizeof(double) * (size_t)M * N) != cudaSuccess || cudaMalloc(&dact, sizeof(int)) != cudaSuccess) {
+        hx_set_error("hx_gemm: device allocation failed");
+        fail(HX_ERR_NOMEM);
+    }
+    if (rc == HX_OK) {
+        int one = 1;
+        cudaMemcpy(dA, A, sizeof(double) * (size_t)M * K, cudaMemcpyHostToDevice);
+        cudaMemcpy(dB, B, sizeof(double) * (size_t)N * K, cudaMemcpyHostToDevice);
+        cudaMemcpy(dact, &one, sizeof(int), cudaMemcpyHostToDevice);
+        // accumulate into a zeroed C (beta = 1) so that long-K problems use split-K as in the plan
+        cudaMemset(dC, 0, sizeof(double) * (size_t)M * N);
+        plan[0].h.push_back(tg(dA, dB, dC, 1, M, N, K, M, N, K, {0, K, 0, 1, 0}, {0, K, 0, 1, 0}, {0, N, 0, 1, 0}, 1.0, 1.0, 0));
+        rc = upload_group(plan[0]);
+    }
+    if (rc == HX_OK && precision == HX_PRECISION_MIXED) rc = tc::create(&te, plan, st);
+    if (rc == HX_OK) {
+        auto launch = [&]() -> cudaError_t {
+            if (te) return tc::run_group(te, plan[0].h.data(), 1, dact, st);
+            return hx_tgemm_f64_launch(plan[0].d, 1, plan[0].tiles, dact, st);
+        };
+        cudaError_t ce = launch();               // warm-up
+        cudaEventRecord(e0, st);
+        for (int r = 0; r < reps && ce == cudaSuccess; ++r) ce = launch();
+        cudaEventRecord(e1, st);
+        // C now holds (reps + 1) A B^T: one clean product for the caller
+        if (ce == cudaSuccess) ce = cudaMemsetAsync(dC, 0, sizeof(double) * (size_t)M * N, st);
+        if (ce == cudaSuccess) ce = launch();
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+        if (ce != cudaSuccess) { hx_set_error("hx_gemm: %s", cudaGetErrorString(ce)); rc = HX_ERR_CUDA; }
+        if (rc == HX_OK && te && tc::error_word(te)) { hx_set_error("hx_gemm: tensor-core wait timed out"); rc = HX_ERR_KERNEL; }
+        if (rc == HX_OK) {
+            float t = 0;
+            cudaEventElapsedTime(&t, e0, e1);
+            if (ms) *ms = t / reps;
+            cudaMemcpy(C, dC, sizeof(double) * (size_t)M * N, cudaMemcpyDeviceToHost);
+        }
+    }
+    if (te) tc::destroy(te);
+    if (plan[0].d) cudaFree(plan[0].d);
+    cudaFree(dA); cudaFree(dB); cudaFree(dC); cudaFree(dact);
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    cudaStreamDestroy(st);
+    return rc;
 }
 
 int hx_last_error(char *buf, size_t len)

@@ -6,7 +6,8 @@ long long hx_tgemm_f64_prepare(TgemmDesc *descs, int n);
 cudaError_t hx_tgemm_f64_launch(const TgemmDesc *d_descs, int n, long long total_tiles,
                                 const int *d_active, cudaStream_t s);
 
-cudaError_t hx_scf_launch(const ScfMol *d_mols, int nmol, const ScfParams &p, cudaStream_t s);
+cudaError_t hx_scf_launch(const ScfMol *d_mols, int nmol, int nmax, const ScfParams &p, double *d_gpart,
+                          cudaStream_t s);
 
 cudaError_t hx_ew_dress_init(const CCMol *m, const int *act, int nmol, long long maxw, cudaStream_t s);
 cudaError_t hx_ew_dress_fock(const CCMol *m, const int *act, int nmol, long long maxw, cudaStream_t s);
@@ -21,5 +22,5 @@ cudaError_t hx_ew_setup2(const CCMol *m, const int *act, int nmol, long long max
 cudaError_t hx_step(const CCMol *m, const DiisMol *h, const int *act, int nmol, double s1, double s2,
                     int use_diis, double *part, int nblk, cudaStream_t s);
 cudaError_t hx_diis(const CCMol *m, const DiisMol *h, const int *act, int nmol, double eps, double *part,
-                    int nblk, cudaStream_t s);
+                    int nblk, int nd_max, cudaStream_t s);
 cudaError_t hx_energy(const CCMol *m, const int *act, int nmol, double *part, int nblk, cudaStream_t s);

@@ -1,7 +1,9 @@
 // Per-molecule device views shared by the kernels and the host plan.
 #pragma once
+#include <vector>
 #include "hx_common.cuh"
 
+#define HX_SCF_GRID_MAX 152    // CTAs of the cooperative SCF (global partials are sized for it)
 #define HX_MAX_DIIS 50         // largest coupled-cluster:diis-steps (definebd.f90: range 2..50)
 
 struct ScfParams {
@@ -58,4 +60,11 @@ struct DiisMol {
     int *count;
     int nd;
     long long L;
+};
+
+// One grouped tensor-GEMM launch of the plan (descriptors on host and device).
+struct Group {
+    std::vector<TgemmDesc> h;
+    TgemmDesc *d = nullptr;
+    long long tiles = 0;
 };

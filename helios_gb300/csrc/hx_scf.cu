@@ -14,40 +14,78 @@
 // the basis of the previous iteration already nearly diagonalises F) and
 // accumulates the rotations into V. Eigenpairs are then sorted ascending, as
 // the reference's tred4 returns them (src/modules/mod_math.f90:31-230).
+//
+// The SCF body is written once over an execution context: a batch runs one
+// CTA per molecule (BlockCtx, barriers are __syncthreads); a single large
+// molecule runs on a cooperative grid (GridCtx, barriers are grid syncs) so
+// that every Jacobi round and every N^3 product is spread over many SMs.
+#include <algorithm>
+#include <cooperative_groups.h>
 #include "hx_common.cuh"
 #include "hx_plan.h"
 
 namespace {
+namespace cg = cooperative_groups;
 constexpr int NT = 512;
 
-__device__ double block_reduce(double v, double *sh, bool is_max)
-{
-    for (int o = 16; o > 0; o >>= 1) {
-        double w = __shfl_xor_sync(0xffffffffu, v, o);
-        v = is_max ? fmax(v, w) : v + w;
-    }
-    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) sh[wid] = v;
-    __syncthreads();
-    if (wid == 0) {
-        v = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : (is_max ? 0.0 : 0.0);
+// ---- execution contexts -------------------------------------------------
+struct BlockCtx {
+    int tid, nt;
+    double *sh;          // >= 33 doubles of shared scratch
+    __device__ BlockCtx(double *s) : tid(threadIdx.x), nt(blockDim.x), sh(s) {}
+    __device__ void sync() { __syncthreads(); }
+    __device__ double reduce(double v, bool mx)
+    {
         for (int o = 16; o > 0; o >>= 1) {
             double w = __shfl_xor_sync(0xffffffffu, v, o);
-            v = is_max ? fmax(v, w) : v + w;
+            v = mx ? fmax(v, w) : v + w;
         }
-        if (lane == 0) sh[32] = v;
+        int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        __syncthreads();
+        if (lane == 0) sh[wid] = v;
+        __syncthreads();
+        if (wid == 0) {
+            v = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) {
+                double w = __shfl_xor_sync(0xffffffffu, v, o);
+                v = mx ? fmax(v, w) : v + w;
+            }
+            if (lane == 0) sh[32] = v;
+        }
+        __syncthreads();
+        double r = sh[32];
+        __syncthreads();
+        return r;
     }
-    __syncthreads();
-    double r = sh[32];
-    __syncthreads();
-    return r;
-}
+};
+
+struct GridCtx {
+    int tid, nt;
+    double *sh;          // shared scratch of this CTA
+    double *gpart;       // 2 x gridDim.x global partials
+    int parity;
+    __device__ GridCtx(double *s, double *gp)
+        : tid(blockIdx.x * blockDim.x + threadIdx.x), nt(gridDim.x * blockDim.x), sh(s), gpart(gp), parity(0) {}
+    __device__ void sync() { cg::this_grid().sync(); }
+    __device__ double reduce(double v, bool mx)
+    {
+        BlockCtx b(sh);
+        v = b.reduce(v, mx);
+        double *p = gpart + parity * gridDim.x;
+        parity ^= 1;
+        if (threadIdx.x == 0) p[blockIdx.x] = v;
+        sync();
+        double r = mx ? 0.0 : 0.0;
+        for (unsigned k = 0; k < gridDim.x; ++k) r = mx ? fmax(r, p[k]) : r + p[k];
+        return r;   // the same ordered sum in every thread
+    }
+};
 
 // C = op(A) op(B) for N x N row-major matrices (ta/tb: use the transpose).
-__device__ void mm(double *C, const double *A, const double *B, int n, bool ta, bool tb, int kmax)
+template <class Ctx>
+__device__ void mm(Ctx &c, double *C, const double *A, const double *B, int n, bool ta, bool tb, int kmax)
 {
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    for (int e = c.tid; e < n * n; e += c.nt) {
         int i = e / n, j = e % n;
         double s = 0.0;
         for (int k = 0; k < kmax; ++k) {
@@ -57,13 +95,14 @@ __device__ void mm(double *C, const double *A, const double *B, int n, bool ta, 
         }
         C[e] = s;
     }
-    __syncthreads();
+    c.sync();
 }
 
 // F = core - G o D + 2 diag(G diag D)
-__device__ void fock(double *F, const double *core, const double *G, const double *D, int n)
+template <class Ctx>
+__device__ void fock(Ctx &c, double *F, const double *core, const double *G, const double *D, int n)
 {
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    for (int e = c.tid; e < n * n; e += c.nt) {
         int i = e / n, j = e % n;
         double f = core[e] - G[e] * D[e];
         if (i == j) {
@@ -73,38 +112,42 @@ __device__ void fock(double *F, const double *core, const double *G, const doubl
         }
         F[e] = f;
     }
-    __syncthreads();
+    c.sync();
 }
 
 // D = sum_{i<nocc} V[:,i] V[:,i]^T
-__device__ void density(double *D, const double *V, int n, int nocc)
+template <class Ctx>
+__device__ void density(Ctx &c, double *D, const double *V, int n, int nocc)
 {
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    for (int e = c.tid; e < n * n; e += c.nt) {
         int mu = e / n, nu = e % n;
         double s = 0.0;
         for (int i = 0; i < nocc; ++i) s = fma(V[mu * n + i], V[nu * n + i], s);
         D[e] = s;
     }
-    __syncthreads();
+    c.sync();
 }
 
 // Jacobi eigen-decomposition of symmetric A (n x n, destroyed: its diagonal
 // ends as the eigenvalues); rotations accumulate into V. W is n x n scratch.
-// Afterwards V's columns and E are sorted ascending.
-__device__ int jacobi(double *A, double *V, double *E, double *W, int n, double *sh,
-                      int *pp, int *pq, double *pc, double *ps)
+// pp/pq/pc/ps are shared arrays of the CTA: every CTA derives the rotations
+// of a round itself from the same matrix entries, so a round needs only the
+// two barriers between its column and row passes.
+template <class Ctx>
+__device__ int jacobi(Ctx &c, double *A, double *V, double *E, double *W, int n, int *pp, int *pq, double *pc,
+                      double *ps)
 {
     const int np = n + (n & 1);
     int sweeps = 0;
     for (; sweeps < 40; ++sweeps) {
         double off = 0.0, tot = 0.0;
-        for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        for (int e = c.tid; e < n * n; e += c.nt) {
             double a = A[e] * A[e];
             tot += a;
             if (e / n != e % n) off += a;
         }
-        off = block_reduce(off, sh, false);
-        tot = block_reduce(tot, sh, false);
+        off = c.reduce(off, false);
+        tot = c.reduce(tot, false);
         if (off <= 1e-30 * tot || off < 1e-300) break;
         for (int r = 0; r < np - 1; ++r) {
             for (int k = threadIdx.x; k < np / 2; k += blockDim.x) {
@@ -112,7 +155,7 @@ __device__ int jacobi(double *A, double *V, double *E, double *W, int n, double 
                 int p = (x == 0) ? 0 : 1 + (x - 1 + r) % (np - 1);
                 int q = 1 + (y - 1 + r) % (np - 1);
                 if (p > q) { int t = p; p = q; q = t; }
-                double c = 1.0, s = 0.0;
+                double cc = 1.0, s = 0.0;
                 if (q < n) {
                     double apq = A[p * n + q];
                     if (fabs(apq) > 1e-300) {
@@ -120,42 +163,43 @@ __device__ int jacobi(double *A, double *V, double *E, double *W, int n, double 
                         double t;
                         if (fabs(theta) > 1e150) t = 0.5 / theta;
                         else t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-                        c = 1.0 / sqrt(t * t + 1.0);
-                        s = t * c;
+                        cc = 1.0 / sqrt(t * t + 1.0);
+                        s = t * cc;
                     }
                 } else {
                     p = -1;   // bye for odd n
                 }
-                pp[k] = p; pq[k] = q; pc[k] = c; ps[k] = s;
+                pp[k] = p; pq[k] = q; pc[k] = cc; ps[k] = s;
             }
-            __syncthreads();
+            // every CTA has read the pair entries before any column is rotated
+            c.sync();
             // columns of A and V: X <- X J
-            for (int e = threadIdx.x; e < (np / 2) * n; e += blockDim.x) {
+            for (int e = c.tid; e < (np / 2) * n; e += c.nt) {
                 int k = e / n, row = e % n, p = pp[k], q = pq[k];
                 if (p < 0 || ps[k] == 0.0) continue;
-                double c = pc[k], s = ps[k];
+                double cs = pc[k], s = ps[k];
                 double akp = A[row * n + p], akq = A[row * n + q];
-                A[row * n + p] = c * akp - s * akq;
-                A[row * n + q] = s * akp + c * akq;
+                A[row * n + p] = cs * akp - s * akq;
+                A[row * n + q] = s * akp + cs * akq;
                 double vkp = V[row * n + p], vkq = V[row * n + q];
-                V[row * n + p] = c * vkp - s * vkq;
-                V[row * n + q] = s * vkp + c * vkq;
+                V[row * n + p] = cs * vkp - s * vkq;
+                V[row * n + q] = s * vkp + cs * vkq;
             }
-            __syncthreads();
+            c.sync();
             // rows of A: A <- J^T A
-            for (int e = threadIdx.x; e < (np / 2) * n; e += blockDim.x) {
+            for (int e = c.tid; e < (np / 2) * n; e += c.nt) {
                 int k = e / n, col = e % n, p = pp[k], q = pq[k];
                 if (p < 0 || ps[k] == 0.0) continue;
-                double c = pc[k], s = ps[k];
+                double cs = pc[k], s = ps[k];
                 double apk = A[p * n + col], aqk = A[q * n + col];
-                A[p * n + col] = c * apk - s * aqk;
-                A[q * n + col] = s * apk + c * aqk;
+                A[p * n + col] = cs * apk - s * aqk;
+                A[q * n + col] = s * apk + cs * aqk;
             }
-            __syncthreads();
+            c.sync();
         }
     }
     // sort ascending: rank each eigenvalue, permute V's columns through W
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    for (int e = c.tid; e < n * n; e += c.nt) {
         int row = e / n, p = e % n;
         double ep = A[p * n + p];
         int rank = 0;
@@ -166,61 +210,58 @@ __device__ int jacobi(double *A, double *V, double *E, double *W, int n, double 
         W[row * n + rank] = V[row * n + p];
         if (row == 0) E[rank] = ep;
     }
-    __syncthreads();
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) V[e] = W[e];
-    __syncthreads();
+    c.sync();
+    for (int e = c.tid; e < n * n; e += c.nt) V[e] = W[e];
+    c.sync();
     return sweeps;
 }
 
-__global__ void __launch_bounds__(NT) scf_kernel(const ScfMol *__restrict__ mols, ScfParams prm)
+template <class Ctx>
+__device__ void scf_body(Ctx &c, const ScfMol &m, const ScfParams &prm, int *pp, int *pq, double *pc, double *ps)
 {
-    __shared__ double sh[40];
-    __shared__ int pp[HX_MAX_MOL_N / 2], pq[HX_MAX_MOL_N / 2];
-    __shared__ double pc[HX_MAX_MOL_N / 2], ps[HX_MAX_MOL_N / 2];
-    const ScfMol m = mols[blockIdx.x];
     const int n = m.N, no = m.nocc, nn = n * n;
     double *F = m.F, *D = m.D, *V = m.V, *A = m.A, *W1 = m.W1, *W2 = m.W2;
 
     // guess
     if (m.D0) {
-        for (int e = threadIdx.x; e < nn; e += blockDim.x) D[e] = m.D0[e];
-        for (int e = threadIdx.x; e < nn; e += blockDim.x) V[e] = m.V0 ? m.V0[e] : (e / n == e % n);
-        __syncthreads();
+        for (int e = c.tid; e < nn; e += c.nt) D[e] = m.D0[e];
+        for (int e = c.tid; e < nn; e += c.nt) V[e] = m.V0 ? m.V0[e] : (e / n == e % n);
+        c.sync();
     } else {
-        for (int e = threadIdx.x; e < nn; e += blockDim.x) {
+        for (int e = c.tid; e < nn; e += c.nt) {
             A[e] = m.huckel[e];
             V[e] = (e / n == e % n) ? 1.0 : 0.0;
         }
-        __syncthreads();
-        jacobi(A, V, m.E, W1, n, sh, pp, pq, pc, ps);
-        density(D, V, n, no);
+        c.sync();
+        jacobi(c, A, V, m.E, W1, n, pp, pq, pc, ps);
+        density(c, D, V, n, no);
     }
-    fock(F, m.core, m.G, D, n);
+    fock(c, F, m.core, m.G, D, n);
 
     int iteration = 0, successful = 1, status = 0;
     double current = 0.0;
     for (;;) {
         ++iteration;
         // W1 = F R, R = 2D - 1
-        for (int e = threadIdx.x; e < nn; e += blockDim.x) W2[e] = 2.0 * D[e] - (e / n == e % n);
-        __syncthreads();
-        mm(W1, F, W2, n, false, false, n);
+        for (int e = c.tid; e < nn; e += c.nt) W2[e] = 2.0 * D[e] - (e / n == e % n);
+        c.sync();
+        mm(c, W1, F, W2, n, false, false, n);
         // A = W1 - W1^T  (F R - R F, both symmetric)
-        for (int e = threadIdx.x; e < nn; e += blockDim.x) A[e] = W1[e] - W1[(e % n) * n + e / n];
-        __syncthreads();
-        mm(W1, A, W2, n, false, false, n);           // Fmin
+        for (int e = c.tid; e < nn; e += c.nt) A[e] = W1[e] - W1[(e % n) * n + e / n];
+        c.sync();
+        mm(c, W1, A, W2, n, false, false, n);           // Fmin
         double acc = 0.0;
-        for (int e = threadIdx.x; e < nn; e += blockDim.x) acc = fmax(acc, fabs(W1[e]));
-        acc = block_reduce(acc, sh, true);
-        for (int e = threadIdx.x; e < nn; e += blockDim.x) D[e] -= prm.step * W1[e];
-        __syncthreads();
-        fock(F, m.core, m.G, D, n);
+        for (int e = c.tid; e < nn; e += c.nt) acc = fmax(acc, fabs(W1[e]));
+        acc = c.reduce(acc, true);
+        for (int e = c.tid; e < nn; e += c.nt) D[e] -= prm.step * W1[e];
+        c.sync();
+        fock(c, F, m.core, m.G, D, n);
         // diagonalise F in the current basis: A = V^T F V
-        mm(W1, F, V, n, false, false, n);
-        mm(A, V, W1, n, true, false, n);
-        jacobi(A, V, m.E, W1, n, sh, pp, pq, pc, ps);
-        density(D, V, n, no);
-        fock(F, m.core, m.G, D, n);
+        mm(c, W1, F, V, n, false, false, n);
+        mm(c, A, V, W1, n, true, false, n);
+        jacobi(c, A, V, m.E, W1, n, pp, pq, pc, ps);
+        density(c, D, V, n, no);
+        fock(c, F, m.core, m.G, D, n);
 
         double previous = current;
         current = acc;
@@ -234,13 +275,13 @@ __global__ void __launch_bounds__(NT) scf_kernel(const ScfMol *__restrict__ mols
     }
     // energy: Eel = sum D (core + F), Enuc = sum_{mu<nu} G   (energySCF :166-200)
     double eel = 0.0, enuc = 0.0;
-    for (int e = threadIdx.x; e < nn; e += blockDim.x) {
+    for (int e = c.tid; e < nn; e += c.nt) {
         eel += D[e] * (m.core[e] + F[e]);
         if (e / n < e % n) enuc += m.G[e];
     }
-    eel = block_reduce(eel, sh, false);
-    enuc = block_reduce(enuc, sh, false);
-    if (threadIdx.x == 0) {
+    eel = c.reduce(eel, false);
+    enuc = c.reduce(enuc, false);
+    if (c.tid == 0) {
         m.out[0] = eel + enuc;
         m.out[1] = eel;
         m.out[2] = enuc;
@@ -248,22 +289,55 @@ __global__ void __launch_bounds__(NT) scf_kernel(const ScfMol *__restrict__ mols
         m.status[0] = status;
         m.status[1] = iteration;
     }
+    // MO Fock (prepareFock('spatial'), mod_cc.f90:2336-2396): Fmo = V^T F V
+    mm(c, W1, F, V, n, false, false, n);
+    mm(c, m.Fmo, V, W1, n, true, false, n);
 }
 
-// MO Fock (prepareFock('spatial'), mod_cc.f90:2336-2396): Fmo = V^T F V.
-__global__ void __launch_bounds__(NT) mo_fock_kernel(const ScfMol *__restrict__ mols)
+__global__ void __launch_bounds__(NT) scf_kernel(const ScfMol *__restrict__ mols, ScfParams prm)
 {
+    __shared__ double sh[40];
+    __shared__ int pp[HX_MAX_MOL_N / 2], pq[HX_MAX_MOL_N / 2];
+    __shared__ double pc[HX_MAX_MOL_N / 2], ps[HX_MAX_MOL_N / 2];
     const ScfMol m = mols[blockIdx.x];
-    mm(m.W1, m.F, m.V, m.N, false, false, m.N);
-    mm(m.Fmo, m.V, m.W1, m.N, true, false, m.N);
+    BlockCtx c(sh);
+    scf_body(c, m, prm, pp, pq, pc, ps);
+}
+
+__global__ void __launch_bounds__(256) scf_grid_kernel(const ScfMol *__restrict__ mols, ScfParams prm, double *gpart)
+{
+    __shared__ double sh[40];
+    __shared__ int pp[HX_MAX_MOL_N / 2], pq[HX_MAX_MOL_N / 2];
+    __shared__ double pc[HX_MAX_MOL_N / 2], ps[HX_MAX_MOL_N / 2];
+    const ScfMol m = mols[0];
+    GridCtx c(sh, gpart);
+    scf_body(c, m, prm, pp, pq, pc, ps);
 }
 }  // namespace
 
-cudaError_t hx_scf_launch(const ScfMol *d_mols, int nmol, const ScfParams &p, cudaStream_t s)
+// One molecule of more than 64 sites runs on a cooperative grid (one CTA per
+// Jacobi pair, at most one per SM); batches run one CTA per molecule.
+cudaError_t hx_scf_launch(const ScfMol *d_mols, int nmol, int nmax, const ScfParams &p, double *d_gpart,
+                          cudaStream_t s)
 {
+    if (nmol == 1 && nmax > 64 && d_gpart) {
+        int dev = 0, nsm = 0, per_sm = 0, coop = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, scf_grid_kernel, 256, 0);
+        int grid = std::min(nmax / 2, nsm * std::max(per_sm, 1));
+        grid = std::min(grid, HX_SCF_GRID_MAX);
+        if (coop && per_sm > 0 && grid >= 2) {
+            ScfParams pc = p;
+            const ScfMol *pm = d_mols;
+            double *gp = d_gpart;
+            void *args[] = {(void *)&pm, (void *)&pc, (void *)&gp};
+            hx_count_launches(1);
+            return cudaLaunchCooperativeKernel((void *)scf_grid_kernel, dim3(grid), dim3(256), args, 0, s);
+        }
+    }
     scf_kernel<<<nmol, NT, 0, s>>>(d_mols, p);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    mo_fock_kernel<<<nmol, NT, 0, s>>>(d_mols);
+    hx_count_launches(1);
     return cudaGetLastError();
 }

@@ -1,15 +1,735 @@
-// Tensor-core backend placeholder: the BF16x3 tcgen05 GEMM lands in this file.
+// Tensor-core backend of the grouped tensor-GEMM: exact-slice BF16 products on tcgen05.
+//
+// FP64 operands are turned into integer slices (an error-free splitting in
+// the spirit of the Ozaki scheme): row r of A is scaled by 2^-e_r so that its
+// largest entry is below 1, then a = 2^-7 (s0 + 2^-8 s1 + 2^-16 s2 + ...)
+// with S = 3 integer slices |s_k| <= 128, each exactly representable in bf16
+// (the representation error is below 2^-24 of the row maximum). The product
+// keeps every slice pair (i, j) with i + j <= 3 (eight of the nine; the one
+// dropped weighs 2^-32). Products of such slices are integers below 2^14, so a
+// tensor-core accumulation of a few hundred of them is exact in FP32 (checked
+// on the hardware: integer inputs give bit-exact sums, while general bf16
+// inputs lose low bits as K grows). Pairs of equal weight 2^-8q (q = i + j)
+// share one TMEM accumulator; every 256-deep K chunk the four accumulators
+// are combined and added into an FP32 (hi, lo) pair per output by TwoSum, so
+// the result carries about FP32 accuracy relative to the operands' row maxima
+// without the tensor core's accumulation error. (A drain in FP64 would be
+// exact too, but at GB300's FP64 rate it costs more than the MMAs.)
+//
+// Per group of TgemmDesc problems:
+//   1. row_scale: per row of A and B (through the descriptor's strides) the
+//      binary exponent of the largest |entry|.
+//   2. split_gather: scaled integer slices, K-major, zero-padded:
+//      [slice][batch][rows][Kp] (rows to 128 for A, 64 for B; Kp to 64).
+//   3. tc_gemm: one CTA per 128x64 output tile (or per K slice of it).
+//      Warp 8 streams 64-deep k-blocks of all slices with TMA
+//      (cp.async.bulk.tensor, 128-byte swizzle) through a 3-stage ring; one
+//      thread of warp 9 issues tcgen05.mma (kind::f16, BF16 x BF16 -> FP32,
+//      M=128, N=64, K=16) into four class accumulators of 64 columns,
+//      alternating between two TMEM buffers per chunk; warps 0-7 drain a
+//      finished buffer with tcgen05.ld (a TMEM lane is an output row; two
+//      warps share a lane quarter and split its columns) while the next chunk
+//      runs, then write C = alpha*2^(e_m+f_n-14)*(hi+lo) + beta*C in FP64.
+//   Every mbarrier wait is bounded by wall time; a wait that runs out records
+//   a code in a device error word and the CTA still frees its TMEM.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
 #include "hx_common.cuh"
+#include "hx_kernels.h"
 #include "hx_tc.h"
 
 namespace tc {
-struct Engine { int unused; };
-int create(Engine **out, const std::vector<Group> &, cudaStream_t)
+
+constexpr int S = 3;                 // integer slices per FP64 operand
+constexpr int QMAX = 3;              // slice pairs with i + j <= QMAX are multiplied
+constexpr int NQ = QMAX + 1;         // accumulator classes q = i + j
+constexpr int BM = 128, BN = 64, BK = 64;
+constexpr int KC = 4;                // k-blocks per exact chunk: 3 pairs * 256 * 2^14 < 2^24
+constexpr int STAGES = 3;
+constexpr int ATILE = BM * BK * 2;                   // 16 KB per A slice
+constexpr int BTILE = BN * BK * 2;                   // 8 KB per B slice
+constexpr int STAGE_BYTES = S * (ATILE + BTILE);
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+constexpr int NTHREADS = 320;                       // 8 epilogue warps, producer, MMA issuer
+constexpr int EPI_THREADS = 256;
+constexpr int EPI_COLS = BN / 2;                     // columns drained per epilogue thread
+constexpr int TMEM_COLS = 512;                       // 2 buffers x NQ classes x 64 columns
+constexpr unsigned long long WAIT_NS = 4000000000ull; // a wait longer than 4 s is declared failed
+
+struct TcDesc {
+    long long a_base, b_base;        // element offsets into the A / B scratch
+    int batch, M, N, K, Mp, Np, Kp;
+    int Mi, Ni;
+    long long c[5];
+    double alpha, beta;
+    double *C;
+    int tiles_m, tiles_n;
+    long long tile_start;
+    int mol;
+    int ksplit;                      // K slices accumulated with FP64 atomics (beta == 1 only)
+    int kb_per;                      // k-blocks per slice
+    const int *expA, *expB;          // per-row binary exponents ([batch][Mp], [batch][Np])
+    CUtensorMap mapA, mapB;          // 2D maps over this desc's scratch
+};
+
+// ------------------------------------------------------------------ PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: false (and an error record) if the phase never completes.
+__device__ __forceinline__ unsigned long long globaltimer()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err, int code)
+{
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = globaltimer();
+    for (;;) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (globaltimer() - t0 > WAIT_NS) break;
+    }
+    if (err) atomicCAS(err, 0, code);
+    return false;
+}
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+            smem_u32(dst)),
+        "l"(map), "r"(smem_u32(bar)), "r"(x), "r"(y)
+        : "memory");
+}
+// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row
+// groups 1024 bytes apart (SBO), tcgen05 descriptor version 1.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((addr & 0x3FFFF) >> 4);
+    d |= (uint64_t)1 << 16;                    // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;          // stride byte offset
+    d |= (uint64_t)1 << 46;                    // descriptor version
+    d |= (uint64_t)2 << 61;                    // SWIZZLE_128B
+    return d;
+}
+// Instruction descriptor: kind::f16, D=F32, A=B=BF16, both K-major, M x N.
+__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void mma_commit(uint64_t *bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v)
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ long long split_off(int x, int xi, long long s0, long long s1)
+{
+    return (long long)(x / xi) * s0 + (long long)(x % xi) * s1;
+}
+
+// ------------------------------------------------------------------ split + gather
+struct PrepDesc {
+    const double *src;
+    __nv_bfloat16 *dst;              // [S][batch][Rp][Kp]
+    int *rexp;                       // [batch][Rp] binary exponent of each row's largest entry
+    int batch, R, K, Rp, Kp, Ri, Ki;
+    long long s[5];                  // r0, r1, k0, k1, batch strides of the FP64 source
+    long long work_start;            // prefix of batch*Rp*(Kp/8) over the launch
+    long long row_start;             // prefix of batch*Rp over the launch
+    int mol;
+};
+
+__device__ __forceinline__ int find_desc(const PrepDesc *pd, int n, long long w, bool rows)
+{
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if ((rows ? pd[mid].row_start : pd[mid].work_start) <= w) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// One warp per row: e with max|x| < 2^e (0 for an all-zero row).
+__global__ void __launch_bounds__(256) row_scale(const PrepDesc *__restrict__ pd, int n, long long rows,
+                                                 const int *__restrict__ active)
+{
+    const int lane = threadIdx.x & 31;
+    for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < rows;
+         w += ((long long)gridDim.x * blockDim.x) >> 5) {
+        const PrepDesc &d = pd[find_desc(pd, n, w, true)];
+        if (active && !active[d.mol]) continue;
+        const long long local = w - d.row_start;
+        const int r = (int)(local % d.Rp), b = (int)(local / d.Rp);
+        double mx = 0.0;
+        if (r < d.R) {
+            const long long base = split_off(r, d.Ri, d.s[0], d.s[1]) + (long long)b * d.s[4];
+            for (int k = lane; k < d.K; k += 32) mx = fmax(mx, fabs(d.src[base + split_off(k, d.Ki, d.s[2], d.s[3])]));
+        }
+        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (lane == 0) {
+            int e = 0;
+            if (mx > 0.0) frexp(mx, &e);      // mx = f 2^e with f in [0.5, 1)
+            d.rexp[local] = e;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) split_gather(const PrepDesc *__restrict__ pd, int n, long long total,
+                                                    const int *__restrict__ active)
+{
+    for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < total;
+         w += (long long)gridDim.x * blockDim.x) {
+        const PrepDesc &d = pd[find_desc(pd, n, w, false)];
+        if (active && !active[d.mol]) continue;
+        long long local = w - d.work_start;
+        const int kc = d.Kp / 8;
+        const int k8 = (int)(local % kc) * 8;
+        long long rr = local / kc;
+        const int r = (int)(rr % d.Rp);
+        const int b = (int)(rr / d.Rp);
+        const int e = d.rexp[(long long)b * d.Rp + r];
+        __align__(16) __nv_bfloat16 out[S][8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            int k = k8 + q;
+            double x = 0.0;
+            if (r < d.R && k < d.K)
+                x = d.src[split_off(r, d.Ri, d.s[0], d.s[1]) + split_off(k, d.Ki, d.s[2], d.s[3]) + (long long)b * d.s[4]];
+            double a = ldexp(x, 7 - e);       // |a| < 128
+#pragma unroll
+            for (int p = 0; p < S; ++p) {
+                double sl = rint(a);          // integer slice, |sl| <= 128
+                out[p][q] = __float2bfloat16_rn((float)sl);
+                a = (a - sl) * 256.0;
+            }
+        }
+        const long long plane = (long long)d.batch * d.Rp * d.Kp;
+        const long long off = ((long long)b * d.Rp + r) * d.Kp + k8;
+#pragma unroll
+        for (int p = 0; p < S; ++p)
+            *reinterpret_cast<uint4 *>(d.dst + p * plane + off) = *reinterpret_cast<const uint4 *>(out[p]);
+    }
+}
+
+// ------------------------------------------------------------------ the GEMM
+__global__ void __launch_bounds__(NTHREADS, 1) tc_gemm(const TcDesc *__restrict__ descs, int ndesc,
+                                                        const int *__restrict__ active, int *err)
+{
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t *full = (uint64_t *)(smem + STAGES * STAGE_BYTES);
+    uint64_t *empty = full + STAGES;
+    uint64_t *acc_full = empty + STAGES;      // [2] MMA -> epilogue: chunk done in buffer b
+    uint64_t *acc_empty = acc_full + 2;       // [2] epilogue -> MMA: buffer b drained
+    uint32_t *tmem_slot = (uint32_t *)(acc_empty + 2);
+    __shared__ int s_d;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long tile = blockIdx.x;
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = ndesc - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (descs[mid].tile_start <= tile) lo = mid; else hi = mid - 1;
+        }
+        s_d = lo;
+    }
+    __syncthreads();
+    const TcDesc &d = descs[s_d];
+    if (active && !active[d.mol]) return;
+    long long local = tile - d.tile_start;
+    const int ks = (int)(local % d.ksplit);
+    local /= d.ksplit;
+    const long long per_batch = (long long)d.tiles_m * d.tiles_n;
+    const int bt = (int)(local / per_batch);
+    local -= bt * per_batch;
+    // grouped rasterisation: 16 tile-rows per group keep A and B blocks L2-resident
+    const int GM = 16;
+    const int group = (int)(local / (GM * d.tiles_n));
+    const int first_m = group * GM;
+    const int gsz = min(d.tiles_m - first_m, GM);
+    const int in_g = (int)(local % (GM * d.tiles_n));
+    const int tm = first_m + in_g % gsz, tn = in_g / gsz;
+    const int kb0 = ks * d.kb_per;
+    const int nkb = min(d.Kp / BK - kb0, d.kb_per);     // >= 1 by construction
+    const int nchunk = (nkb + KC - 1) / KC;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
+        for (int b = 0; b < 2; ++b) { mbar_init(&acc_full[b], 1); mbar_init(&acc_empty[b], EPI_THREADS); }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 9) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+    bool ok = true;
+
+    if (warp == 8) {
+        if (lane == 0) {
+            const int arow0 = bt * d.Mp + tm * BM, brow0 = bt * d.Np + tn * BN;
+            const int aplane = d.batch * d.Mp, bplane = d.batch * d.Np;
+            for (int kb = 0; kb < nkb && ok; ++kb) {
+                const int st = kb % STAGES;
+                const uint32_t ph = (kb / STAGES) & 1;
+                ok = mbar_wait(&empty[st], ph ^ 1, err, 1);
+                if (!ok) break;
+                uint8_t *sa = smem + st * STAGE_BYTES;
+                uint8_t *sb = sa + S * ATILE;
+                mbar_expect_tx(&full[st], STAGE_BYTES);
+                for (int p = 0; p < S; ++p) {
+                    tma_load_2d(sa + p * ATILE, &d.mapA, &full[st], (kb0 + kb) * BK, p * aplane + arow0);
+                    tma_load_2d(sb + p * BTILE, &d.mapB, &full[st], (kb0 + kb) * BK, p * bplane + brow0);
+                }
+            }
+        }
+    } else if (warp == 9) {
+        if (lane == 0) {
+            const uint32_t idesc = idesc_bf16(BM, BN);
+            for (int c = 0; c < nchunk && ok; ++c) {
+                const int buf = c & 1;
+                const uint32_t use = (uint32_t)(c >> 1);
+                ok = mbar_wait(&acc_empty[buf], (use & 1) ^ 1, err, 4);
+                if (!ok) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t dbase = tmem + (uint32_t)(buf * NQ * BN);
+                const int kend = min(nkb, (c + 1) * KC);
+                for (int kb = c * KC; kb < kend && ok; ++kb) {
+                    const int st = kb % STAGES;
+                    const uint32_t ph = (kb / STAGES) & 1;
+                    ok = mbar_wait(&full[st], ph, err, 2);
+                    if (!ok) break;
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t sa = smem_u32(smem + st * STAGE_BYTES);
+                    const uint32_t sb = sa + S * ATILE;
+#pragma unroll
+                    for (int kk = 0; kk < BK / 16; ++kk) {
+#pragma unroll
+                        for (int i = 0; i < S; ++i) {
+#pragma unroll
+                            for (int j = 0; j < S; ++j) {
+                                const int q = i + j;
+                                if (q > QMAX) continue;
+                                const uint64_t ad = sw128_desc(sa + i * ATILE + kk * 32);
+                                const uint64_t bd = sw128_desc(sb + j * BTILE + kk * 32);
+                                // the first product of a class in the chunk overwrites its accumulator
+                                const bool first = (kb == c * KC) && kk == 0 && i == (q < S ? 0 : q - (S - 1));
+                                mma_bf16(dbase + q * BN, ad, bd, idesc, first ? 0u : 1u);
+                            }
+                        }
+                    }
+                    mma_commit(&empty[st]);
+                }
+                mma_commit(&acc_full[buf]);
+            }
+        }
+    } else {
+        // epilogue: warps 0-7; warp w drains TMEM lanes 32*(w%4).. (output rows) and
+        // the column half w/4 of the tile
+        const int row = (warp & 3) * 32 + lane;
+        const int col0 = (warp >> 2) * EPI_COLS;
+        const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+        float hi[EPI_COLS], lo[EPI_COLS];
+#pragma unroll
+        for (int e = 0; e < EPI_COLS; ++e) { hi[e] = 0.f; lo[e] = 0.f; }
+        for (int c = 0; c < nchunk; ++c) {
+            const int buf = c & 1;
+            const uint32_t use = (uint32_t)(c >> 1);
+            if (ok) ok = mbar_wait(&acc_full[buf], use & 1, err, 3);
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+            for (int c0 = 0; c0 < EPI_COLS; c0 += 16) {
+                // chunk value: exact integer classes combined with weights 2^-8q
+                float x[16], t[16];
+                tmem_ld16(tmem + lane_base + (uint32_t)(buf * NQ * BN + (NQ - 1) * BN + col0 + c0), x);
+#pragma unroll
+                for (int q = NQ - 2; q >= 0; --q) {
+                    tmem_ld16(tmem + lane_base + (uint32_t)(buf * NQ * BN + q * BN + col0 + c0), t);
+#pragma unroll
+                    for (int e = 0; e < 16; ++e) x[e] = fmaf(x[e], 0.00390625f, t[e]);
+                }
+#pragma unroll
+                for (int e = 0; e < 16; ++e) {
+                    // TwoSum of the chunk value into (hi, lo)
+                    const float s = hi[c0 + e] + x[e];
+                    const float bb = s - hi[c0 + e];
+                    lo[c0 + e] += (hi[c0 + e] - (s - bb)) + (x[e] - bb);
+                    hi[c0 + e] = s;
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            mbar_arrive(&acc_empty[buf]);
+        }
+        const int m = tm * BM + row;
+        if (ok && m < d.M) {
+            double *C = d.C + (long long)bt * d.c[4];
+            const long long offm = split_off(m, d.Mi, d.c[0], d.c[1]);
+            const int ea = d.expA[(long long)bt * d.Mp + m];
+#pragma unroll
+            for (int e = 0; e < EPI_COLS; ++e) {
+                const int n = tn * BN + col0 + e;
+                if (n >= d.N) continue;
+                const int eb = d.expB[(long long)bt * d.Np + n];
+                double *p = C + offm + split_off(n, d.Ni, d.c[2], d.c[3]);
+                double r = d.alpha * ldexp((double)hi[e] + (double)lo[e], ea + eb - 14);
+                if (d.ksplit > 1) { atomicAdd(p, r); continue; }
+                if (d.beta != 0.0) r += d.beta * *p;
+                *p = r;
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 9) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+    }
+}
+
+// ------------------------------------------------------------------ host side
+struct PrepList {                    // operands sliced by one pair of launches
+    std::vector<PrepDesc> h;
+    PrepDesc *d = nullptr;
+    long long work = 0, rows = 0;
+};
+
+struct SubGroup {
+    std::vector<TcDesc> tcd;         // tensor-core problems
+    TcDesc *d_tcd = nullptr;
+    PrepList var, fixed;             // operands sliced every run / once per initialisation
+    int fixed_gen = -1;              // generation the fixed slices were made for
+    long long tiles = 0;
+    Group fp64;                       // problems too small for the tensor cores
+};
+
+struct Engine {
+    __nv_bfloat16 *scratch = nullptr;
+    size_t scratch_elems = 0;
+    int *rexp = nullptr;              // per-row exponents of every operand of the largest group
+    size_t rexp_elems = 0;
+    int *d_err = nullptr;
+    std::vector<SubGroup> groups;     // one per plan group, same order
+    std::vector<const Group *> keys;
+    bool profile = false;
+    int generation = 0;
+    struct Pending { cudaEvent_t a, b; double flops, hwflops; };
+    std::vector<Pending> pending;
+    std::vector<cudaEvent_t> pool;
+    double tot[4] = {0, 0, 0, 0};
+};
+
+static cudaEvent_t take_event(Engine *e)
+{
+    if (!e->pool.empty()) { cudaEvent_t x = e->pool.back(); e->pool.pop_back(); return x; }
+    cudaEvent_t x;
+    cudaEventCreate(&x);
+    return x;
+}
+
+void set_profile(Engine *e, bool on) { if (e) e->profile = on; }
+
+void invalidate(Engine *e) { if (e) ++e->generation; }
+
+void collect(Engine *e, double out[4])
+{
+    if (!e) return;
+    for (auto &p : e->pending) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+            e->tot[0] += 1; e->tot[1] += ms; e->tot[2] += p.flops; e->tot[3] += p.hwflops;
+        }
+        e->pool.push_back(p.a);
+        e->pool.push_back(p.b);
+    }
+    e->pending.clear();
+    if (out) for (int k = 0; k < 4; ++k) out[k] = e->tot[k];
+}
+
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+static int make_map(CUtensorMap *map, void *base, long long rows, int kp, int box_rows)
+{
+    auto fn = encode_fn();
+    if (!fn) { hx_set_error("cuTensorMapEncodeTiled is unavailable"); return HX_ERR_CUDA; }
+    cuuint64_t dims[2] = {(cuuint64_t)kp, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)kp * 2};
+    cuuint32_t box[2] = {BK, (cuuint32_t)box_rows};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) { hx_set_error("cuTensorMapEncodeTiled failed (%d)", (int)r); return HX_ERR_CUDA; }
+    return HX_OK;
+}
+
+static inline long long rup(long long x, long long m) { return (x + m - 1) / m * m; }
+
+// Problems below this many multiply-adds stay on the FP64 CUDA-core kernel.
+static const double kMinTcWork = 4.0e6;
+
+int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s)
 {
     *out = nullptr;
-    hx_set_error("mixed precision is not available in this build");
-    return HX_ERR_UNSUPPORTED;
+    Engine *e = new Engine();
+    // pass 1: sizes
+    size_t need = 0, need_rows = 0;
+    for (const Group &g : plan) {
+        size_t gneed = 0, grows = 0;
+        for (const TgemmDesc &t : g.h) {
+            double work = (double)t.batch * t.M * t.N * t.K;
+            if (work < kMinTcWork) continue;
+            gneed += (size_t)S * t.batch * (rup(t.M, BM) + rup(t.N, BN)) * rup(t.K, BK);
+            grows += (size_t)t.batch * (rup(t.M, BM) + rup(t.N, BN));
+        }
+        need = std::max(need, gneed);
+        need_rows = std::max(need_rows, grows);
+    }
+    e->scratch_elems = need;
+    e->rexp_elems = need_rows;
+    if ((need && cudaMalloc(&e->scratch, need * sizeof(__nv_bfloat16)) != cudaSuccess) ||
+        (need_rows && cudaMalloc(&e->rexp, need_rows * sizeof(int)) != cudaSuccess)) {
+        hx_set_error("cudaMalloc of %zu bytes of tensor-core scratch failed", need * 2 + need_rows * 4);
+        destroy(e);
+        return HX_ERR_NOMEM;
+    }
+    if (cudaMalloc(&e->d_err, sizeof(int)) != cudaSuccess) { delete e; return HX_ERR_NOMEM; }
+    cudaMemsetAsync(e->d_err, 0, sizeof(int), s);
+    // pass 2: descriptors and tensor maps
+    for (const Group &g : plan) {
+        SubGroup sg;
+        size_t off = 0, roff = 0;
+        long long tiles = 0;
+        for (const TgemmDesc &t : g.h) {
+            double w = (double)t.batch * t.M * t.N * t.K;
+            if (w < kMinTcWork) { sg.fp64.h.push_back(t); continue; }
+            TcDesc d;
+            memset(&d, 0, sizeof(d));
+            d.batch = t.batch; d.M = t.M; d.N = t.N; d.K = t.K;
+            d.Mp = (int)rup(t.M, BM); d.Np = (int)rup(t.N, BN); d.Kp = (int)rup(t.K, BK);
+            d.Mi = t.Mi; d.Ni = t.Ni;
+            for (int k = 0; k < 5; ++k) d.c[k] = t.c[k];
+            d.alpha = t.alpha; d.beta = t.beta; d.C = t.C; d.mol = t.mol;
+            d.tiles_m = d.Mp / BM; d.tiles_n = d.Np / BN;
+            // long K over few output tiles: cut K into slices that fill the GPU
+            const int nkb = d.Kp / BK;
+            const long long out_tiles = (long long)d.batch * d.tiles_m * d.tiles_n;
+            int ks = 1;
+            if (t.beta == 1.0 && out_tiles < 152 && nkb >= 16) ks = (int)std::min<long long>((152 + out_tiles - 1) / out_tiles, nkb / 8);
+            d.kb_per = (nkb + ks - 1) / ks;
+            d.ksplit = (nkb + d.kb_per - 1) / d.kb_per;
+            d.tile_start = tiles;
+            tiles += out_tiles * d.ksplit;
+            d.a_base = (long long)off;
+            size_t asz = (size_t)S * d.batch * d.Mp * d.Kp;
+            d.b_base = (long long)(off + asz);
+            size_t bsz = (size_t)S * d.batch * d.Np * d.Kp;
+            int rc = make_map(&d.mapA, e->scratch + d.a_base, (long long)S * d.batch * d.Mp, d.Kp, BM);
+            if (rc == HX_OK) rc = make_map(&d.mapB, e->scratch + d.b_base, (long long)S * d.batch * d.Np, d.Kp, BN);
+            if (rc < 0) { destroy(e); return rc; }
+            PrepDesc pa, pb;
+            memset(&pa, 0, sizeof(pa));
+            pa.src = t.A; pa.dst = e->scratch + d.a_base; pa.batch = t.batch; pa.R = t.M; pa.K = t.K;
+            pa.Rp = d.Mp; pa.Kp = d.Kp; pa.Ri = t.Mi; pa.Ki = t.Ki; pa.mol = t.mol;
+            pa.s[0] = t.a[0]; pa.s[1] = t.a[1]; pa.s[2] = t.a[2]; pa.s[3] = t.a[3]; pa.s[4] = t.a[4];
+            pa.rexp = e->rexp + roff;
+            d.expA = pa.rexp;
+            roff += (size_t)t.batch * d.Mp;
+            pb = pa;
+            pb.src = t.B; pb.dst = e->scratch + d.b_base; pb.R = t.N; pb.Rp = d.Np; pb.Ri = t.Ni;
+            pb.s[0] = t.b[0]; pb.s[1] = t.b[1]; pb.s[2] = t.b[2]; pb.s[3] = t.b[3]; pb.s[4] = t.b[4];
+            pb.rexp = e->rexp + roff;
+            d.expB = pb.rexp;
+            roff += (size_t)t.batch * d.Np;
+            auto add = [&](PrepList &L, PrepDesc p) {
+                p.work_start = L.work;
+                p.row_start = L.rows;
+                L.work += (long long)p.batch * p.Rp * (p.Kp / 8);
+                L.rows += (long long)p.batch * p.Rp;
+                L.h.push_back(p);
+            };
+            add(t.a_const ? sg.fixed : sg.var, pa);
+            add(t.b_const ? sg.fixed : sg.var, pb);
+            sg.tcd.push_back(d);
+            off += asz + bsz;
+        }
+        sg.tiles = tiles;
+        if (!sg.tcd.empty()) {
+            if (cudaMalloc(&sg.d_tcd, sizeof(TcDesc) * sg.tcd.size()) != cudaSuccess) {
+                destroy(e);
+                hx_set_error("descriptor allocation failed");
+                return HX_ERR_NOMEM;
+            }
+            cudaMemcpy(sg.d_tcd, sg.tcd.data(), sizeof(TcDesc) * sg.tcd.size(), cudaMemcpyHostToDevice);
+            for (PrepList *L : {&sg.var, &sg.fixed}) {
+                if (L->h.empty()) continue;
+                if (cudaMalloc(&L->d, sizeof(PrepDesc) * L->h.size()) != cudaSuccess) {
+                    destroy(e);
+                    hx_set_error("descriptor allocation failed");
+                    return HX_ERR_NOMEM;
+                }
+                cudaMemcpy(L->d, L->h.data(), sizeof(PrepDesc) * L->h.size(), cudaMemcpyHostToDevice);
+            }
+        }
+        if (!sg.fp64.h.empty()) {
+            sg.fp64.tiles = hx_tgemm_f64_prepare(sg.fp64.h.data(), (int)sg.fp64.h.size());
+            cudaMalloc(&sg.fp64.d, sizeof(TgemmDesc) * sg.fp64.h.size());
+            cudaMemcpy(sg.fp64.d, sg.fp64.h.data(), sizeof(TgemmDesc) * sg.fp64.h.size(), cudaMemcpyHostToDevice);
+        } else {
+            sg.fp64.d = nullptr;
+            sg.fp64.tiles = 0;
+        }
+        e->groups.push_back(sg);
+        e->keys.push_back(&g);
+    }
+    if (cudaFuncSetAttribute(tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) != cudaSuccess) {
+        destroy(e);
+        hx_set_error("cannot reserve %d bytes of shared memory for tc_gemm", SMEM_BYTES);
+        return HX_ERR_CUDA;
+    }
+    *out = e;
+    return HX_OK;
 }
-cudaError_t run_group(Engine *, const TgemmDesc *, int, const int *, cudaStream_t) { return cudaErrorNotSupported; }
-void destroy(Engine *) {}
+
+cudaError_t run_group(Engine *e, const TgemmDesc *descs, int n, const int *d_active, cudaStream_t s)
+{
+    // find the sub-group built for this plan group (same descriptor array)
+    int gi = -1;
+    for (size_t k = 0; k < e->keys.size(); ++k)
+        if (e->keys[k]->h.data() == descs) { gi = (int)k; break; }
+    if (gi < 0) return cudaErrorInvalidValue;
+    SubGroup &sg = e->groups[gi];
+    if (sg.fp64.tiles > 0) {
+        cudaError_t r = hx_tgemm_f64_launch(sg.fp64.d, (int)sg.fp64.h.size(), sg.fp64.tiles, d_active, s);
+        if (r != cudaSuccess) return r;
+    }
+    if (sg.tiles == 0) return cudaSuccess;
+    cudaError_t r = cudaSuccess;
+    auto prep = [&](PrepList &L) -> cudaError_t {
+        if (L.h.empty()) return cudaSuccess;
+        long long rblocks = std::min<long long>((L.rows * 32 + 255) / 256, 1 << 16);
+        row_scale<<<(unsigned)rblocks, 256, 0, s>>>(L.d, (int)L.h.size(), L.rows, d_active);
+        cudaError_t x = cudaGetLastError();
+        if (x != cudaSuccess) return x;
+        long long blocks = std::min<long long>((L.work + 255) / 256, 1 << 16);
+        split_gather<<<(unsigned)blocks, 256, 0, s>>>(L.d, (int)L.h.size(), L.work, d_active);
+        hx_count_launches(2);
+        return cudaGetLastError();
+    };
+    if (sg.fixed_gen != e->generation) {
+        if ((r = prep(sg.fixed)) != cudaSuccess) return r;
+        sg.fixed_gen = e->generation;
+    }
+    if ((r = prep(sg.var)) != cudaSuccess) return r;
+    hx_count_launches(1);
+    Engine::Pending pend{};
+    if (e->profile) {
+        pend.a = take_event(e);
+        pend.b = take_event(e);
+        for (const TcDesc &d : sg.tcd) {
+            double f = 2.0 * d.batch * (double)d.M * d.N * d.K;
+            pend.flops += f;
+            pend.hwflops += 2.0 * d.batch * (double)d.Mp * d.Np * d.Kp * 8;   // 8 slice products
+        }
+        cudaEventRecord(pend.a, s);
+    }
+    tc_gemm<<<(unsigned)sg.tiles, NTHREADS, SMEM_BYTES, s>>>(sg.d_tcd, (int)sg.tcd.size(), d_active, e->d_err);
+    r = cudaGetLastError();
+    if (e->profile) {
+        cudaEventRecord(pend.b, s);
+        e->pending.push_back(pend);
+    }
+    return r;
+}
+
+int error_word(Engine *e)
+{
+    int v = 0;
+    if (e && e->d_err) cudaMemcpy(&v, e->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+    return v;
+}
+
+void destroy(Engine *e)
+{
+    if (!e) return;
+    for (auto &g : e->groups) {
+        cudaFree(g.d_tcd);
+        cudaFree(g.var.d);
+        cudaFree(g.fixed.d);
+        if (g.fp64.d) cudaFree(g.fp64.d);
+    }
+    for (auto &p : e->pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
+    for (auto x : e->pool) cudaEventDestroy(x);
+    cudaFree(e->scratch);
+    cudaFree(e->rexp);
+    cudaFree(e->d_err);
+    delete e;
+}
+
 }  // namespace tc

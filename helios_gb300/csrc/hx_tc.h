@@ -3,7 +3,6 @@
 #include <vector>
 #include "hx_plan.h"
 
-struct Group;
 namespace tc {
 struct Engine;
 // Build the backend for the GEMM groups of a plan (scratch sized to the largest operand).
@@ -11,4 +10,14 @@ int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s);
 // Run one group: gather + split the operands to BF16 hi/lo, tcgen05 GEMM, FP64 epilogue.
 cudaError_t run_group(Engine *e, const TgemmDesc *descs, int n, const int *active_host, cudaStream_t s);
 void destroy(Engine *e);
+// Device error word of the tensor-core kernels (0 = no wait timed out).
+int error_word(Engine *e);
+// Live timing of the tcgen05 GEMM launches (CUDA events on the launching
+// stream): enable/disable, then collect after the stream has synchronised.
+void set_profile(Engine *e, bool on);
+// The constant operands changed (new orbitals): slice them again on next use.
+void invalidate(Engine *e);
+// Adds the finished launches to totals: out[0] launches, [1] ms, [2]
+// algorithmic flops (2*M*N*K per problem), [3] tensor-core flops issued.
+void collect(Engine *e, double out[4]);
 }  // namespace tc

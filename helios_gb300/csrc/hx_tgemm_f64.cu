@@ -9,6 +9,7 @@
 // gathered through the descriptor's split strides, so any index permutation
 // of a 4-index tensor is read in place; the loader walks the operand's
 // contiguous dimension first so the warp's loads coalesce.
+#include <algorithm>
 #include "hx_common.cuh"
 
 namespace {
@@ -38,10 +39,15 @@ __global__ void __launch_bounds__(NT) tgemm_f64_kernel(const TgemmDesc *__restri
     const TgemmDesc &d = descs[s_d];
     if (active && !active[d.mol]) return;
     long long local = tile - d.tile_start;
+    const int ks = (int)(local % d.ksplit);
+    local /= d.ksplit;
     const int per_batch = d.tiles_m * d.tiles_n;
     const int bt = (int)(local / per_batch);
     local -= (long long)bt * per_batch;
     const int tm = (int)(local / d.tiles_n), tn = (int)(local % d.tiles_n);
+    // K slice of this CTA (multiples of BK)
+    const int kslice = ((d.K + d.ksplit - 1) / d.ksplit + BK - 1) / BK * BK;
+    const int kbeg = ks * kslice, kend = min(d.K, kbeg + kslice);
     const int m0 = tm * BM, n0 = tn * BN;
     const double *A = d.A + (long long)bt * d.a[4];
     const double *B = d.B + (long long)bt * d.b[4];
@@ -57,7 +63,7 @@ __global__ void __launch_bounds__(NT) tgemm_f64_kernel(const TgemmDesc *__restri
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
 
-    for (int k0 = 0; k0 < d.K; k0 += BK) {
+    for (int k0 = kbeg; k0 < kend; k0 += BK) {
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
             int e = threadIdx.x + NT * r;
@@ -65,7 +71,7 @@ __global__ void __launch_bounds__(NT) tgemm_f64_kernel(const TgemmDesc *__restri
             if (a_kfast) { kk = e % BK; mm = e / BK; } else { mm = e % BM; kk = e / BM; }
             int m = m0 + mm, k = k0 + kk;
             double val = 0.0;
-            if (m < d.M && k < d.K)
+            if (m < d.M && k < kend)
                 val = A[split_off(m, d.Mi, d.a[0], d.a[1]) + split_off(k, d.Ki, d.a[2], d.a[3])];
             As[kk][mm] = val;
             int nn;
@@ -73,7 +79,7 @@ __global__ void __launch_bounds__(NT) tgemm_f64_kernel(const TgemmDesc *__restri
             int n = n0 + nn;
             k = k0 + kk;
             val = 0.0;
-            if (n < d.N && k < d.K)
+            if (n < d.N && k < kend)
                 val = B[split_off(n, d.Ni, d.b[0], d.b[1]) + split_off(k, d.Ki, d.b[2], d.b[3])];
             Bs[kk][nn] = val;
         }
@@ -103,6 +109,7 @@ __global__ void __launch_bounds__(NT) tgemm_f64_kernel(const TgemmDesc *__restri
             if (n >= d.N) continue;
             double *p = C + offm + split_off(n, d.Ni, d.c[2], d.c[3]);
             double r = d.alpha * acc[i][j];
+            if (d.ksplit > 1) { atomicAdd(p, r); continue; }
             if (d.beta != 0.0) r += d.beta * *p;
             *p = r;
         }
@@ -118,8 +125,16 @@ long long hx_tgemm_f64_prepare(TgemmDesc *descs, int n)
         TgemmDesc &d = descs[i];
         d.tiles_m = (d.M + BM - 1) / BM;
         d.tiles_n = (d.N + BN - 1) / BN;
+        // split K when the output has few tiles but K is long (accumulating problems only)
+        d.ksplit = 1;
+        const long long out_tiles = (long long)d.batch * d.tiles_m * d.tiles_n;
+        if (d.beta == 1.0 && d.K >= 4 * BK * 8 && out_tiles < 304) {
+            long long want = (304 + out_tiles - 1) / out_tiles;
+            long long maxk = d.K / (BK * 8);
+            d.ksplit = (int)std::max(1LL, std::min(want, maxk));
+        }
         d.tile_start = start;
-        if (d.M > 0 && d.N > 0 && d.batch > 0) start += (long long)d.batch * d.tiles_m * d.tiles_n;
+        if (d.M > 0 && d.N > 0 && d.batch > 0) start += out_tiles * d.ksplit;
     }
     return start;
 }
@@ -129,5 +144,6 @@ cudaError_t hx_tgemm_f64_launch(const TgemmDesc *d_descs, int n, long long total
 {
     if (total_tiles <= 0) return cudaSuccess;
     tgemm_f64_kernel<<<(unsigned)total_tiles, NT, 0, s>>>(d_descs, n, d_active);
+    hx_count_launches(1);
     return cudaGetLastError();
 }

@@ -97,6 +97,10 @@ typedef struct hx_cc_params {
     int32_t stagnation_after;     /* iteration:stagnation-check-after (200) */
     int32_t precision;            /* HX_PRECISION_FP64 (default) or HX_PRECISION_MIXED */
     int32_t guess;                /* 0 reference guess (guessCC), 1 learned guess */
+    double mixed_switch;          /* mixed precision: residual at which a molecule moves on to
+                                     FP64 iterations (1e-6) */
+    int32_t mixed_patience;       /* mixed precision: iterations without a new lowest residual
+                                     after which it moves on to FP64 anyway (3) */
 } hx_cc_params;
 
 typedef struct hx_ccsd hx_ccsd;
@@ -145,6 +149,22 @@ int hx_ccsd_get_amplitudes(hx_ccsd *h, int32_t mol, double *t1, double *t2);
 int hx_ccsd_get_scf(hx_ccsd *h, int32_t mol, double *C, double *eps, double *fmo, double scf[4],
                     int32_t scf_status[2]);
 
+/* Per-iteration record of molecule mol's last solve: for each iteration
+ * k < cap, out[5k..5k+4] = max|d1|, max|d2|, E_total, seconds since the start
+ * of the solve, precision of the iteration (0 FP64, 1 mixed). Returns the
+ * number of iterations recorded. */
+int hx_ccsd_trace(hx_ccsd *h, int32_t mol, double *out, int32_t cap);
+
+/* Engine utility with no counterpart in the reference: device timing.
+ * out[0] = ms of the last hx_ccsd_init (SCF, integrals, guess), out[1] = ms
+ * of the last solve, both from CUDA events on the handle's stream;
+ * out[2..5] = launches, ms, algorithmic flops (2*M*N*K) and tensor-core
+ * flops issued by the tcgen05 GEMM since profiling was switched on;
+ * out[6] = device bytes held by the handle; out[7] = kernels the library
+ * launched (all handles) since profiling was last switched on. profile = 1 switches per-launch
+ * GEMM timing on (and clears the totals), 0 off, -1 leaves it. */
+int hx_ccsd_timing(hx_ccsd *h, double out[8], int32_t profile);
+
 /* Sizes of molecule mol: dims[0..3] = N, o, v, electrons. */
 int hx_ccsd_dims(hx_ccsd *h, int32_t mol, int32_t dims[4]);
 
@@ -155,6 +175,14 @@ void hx_ccsd_cancel(hx_ccsd *h);
 
 /* finalizeCC: free the device state. */
 void hx_ccsd_destroy(hx_ccsd *h);
+
+/* Engine utility with no counterpart in the reference: C = A B^T for
+ * row-major FP64 host matrices (A: M x K, B: N x K, C: M x N) on the engine's
+ * FP64 CUDA-core GEMM (precision 0) or its split-BF16 tcgen05 GEMM
+ * (precision 1); the launch is repeated reps times after one warm-up and
+ * *ms (if not NULL) receives the mean device time per launch. */
+int hx_gemm(const double *A, const double *B, double *C, int32_t M, int32_t N, int32_t K, int32_t precision,
+            int32_t reps, double *ms);
 
 /* Copy the message of the last error (thread-local) into buf; returns its length. */
 int hx_last_error(char *buf, size_t len);

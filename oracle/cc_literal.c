@@ -124,15 +124,13 @@ void orc_singles(int N, int o, const double *F, const double *R,
     }
 }
 
-void orc_doubles(int N, int o, const double *F, const double *R,
-                 const double *t1, const double *t2, double *d2)
+/* The doubles formula for one pair of excitations (i,a), (j,b). */
+static double doubles_pair(int N, int o, const double *F, const double *R, const double *t1, const double *t2,
+                           int i, int a, int j, int b)
 {
-    int v = N - o, ne = o * v;
-    #pragma omp parallel for schedule(dynamic)
-    for (int mm = 0; mm < ne; ++mm) {
-        int i = mm / v, a = o + mm % v;
-        for (int nn = mm; nn < ne; ++nn) {
-            int j = nn / v, b = o + nn % v;
+    int v = N - o;
+    {
+        {
             double rez = RR(a, i, b, j), sum;               /* 14 */
 
             sum = 0;                                        /* 25 */
@@ -260,9 +258,37 @@ void orc_doubles(int N, int o, const double *F, const double *R,
                                        + T2(j, i, a, c) * T1(k, b) + T2(i, j, b, c) * T1(k, a));
             rez += sum;
 
+            return rez;
+        }
+    }
+}
+
+void orc_doubles(int N, int o, const double *F, const double *R,
+                 const double *t1, const double *t2, double *d2)
+{
+    int v = N - o, ne = o * v;
+    #pragma omp parallel for schedule(dynamic)
+    for (int mm = 0; mm < ne; ++mm) {
+        int i = mm / v, a = o + mm % v;
+        for (int nn = mm; nn < ne; ++nn) {
+            int j = nn / v, b = o + nn % v;
+            double rez = doubles_pair(N, o, F, R, t1, t2, i, a, j, b);
             D2(i, j, a, b) = rez;
             D2(j, i, b, a) = rez;
         }
+    }
+}
+
+/* The doubles formula on a list of pairs (mm[k], nn[k]) only: a bounded
+ * sample of one reference iteration, for timing on large systems. */
+void orc_doubles_sample(int N, int o, const double *F, const double *R, const double *t1, const double *t2,
+                        const int *mm, const int *nn, int npairs, double *out)
+{
+    int v = N - o;
+    #pragma omp parallel for schedule(dynamic)
+    for (int k = 0; k < npairs; ++k) {
+        int i = mm[k] / v, a = o + mm[k] % v, j = nn[k] / v, b = o + nn[k] % v;
+        out[k] = doubles_pair(N, o, F, R, t1, t2, i, a, j, b);
     }
 }
 
@@ -450,6 +476,10 @@ static void diis_new(diis_t *h, int N, int o, int iteration, double *t1, double 
         for (int k = 0; k < n; ++k) c[k] = (k == ub);
         gauss_solve(n, A, c);
     }
+    /* a singular subspace (more vectors than the amplitude space has
+     * dimensions) gives no usable mixing: keep the stepped amplitudes */
+    for (int k = 0; k < iteration; ++k)
+        if (!isfinite(c[k])) { free(A); free(V); free(w); free(c); return; }
     for (int x = 0; x < ne; ++x) {
         double s = 0;
         for (int p = 0; p < iteration; ++p) s += c[p] * h->st1[(size_t)p * ne + x];

@@ -239,7 +239,13 @@ class DIIS:
             return None
         A = np.ones((n + 1, n + 1)); A[:n, :n] = B[:n, :n]; A[n, n] = 0.0
         rhs = np.zeros(n + 1); rhs[n] = 1.0
-        c = np.linalg.solve(A, rhs)[:n]
+        with np.errstate(all="ignore"):
+            try:
+                c = np.linalg.solve(A, rhs)[:n]
+            except np.linalg.LinAlgError:
+                return None
+        if not np.all(np.isfinite(c)):
+            return None          # singular subspace: keep the stepped amplitudes
         x = sum(c[k] * self.st[k] for k in range(n))
         o, v = self.o, self.v
         t1 = x[:o * v].reshape(o, v)

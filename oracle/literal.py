@@ -26,7 +26,7 @@ def lib():
     if _lib is None:
         _lib = ctypes.CDLL(_build.build())
         for name in ("orc_integrals", "orc_guess", "orc_singles", "orc_doubles", "orc_step",
-                     "orc_energy"):
+                     "orc_energy", "orc_doubles_sample"):
             getattr(_lib, name).restype = None
         _lib.orc_ccsd_solve.restype = ctypes.c_int
         _lib.orc_num_threads.restype = ctypes.c_int
@@ -66,6 +66,19 @@ def residuals(F, R, t1, t2):
     lib().orc_singles(N, o, _p(F), _p(R), _p(t1), _p(t2), _p(d1))
     lib().orc_doubles(N, o, _p(F), _p(R), _p(t1), _p(t2), _p(d2))
     return d1, d2
+
+
+def doubles_sample(F, R, t1, t2, mm, nn):
+    """Reference doubles residual on the excitation pairs (mm[k], nn[k]) only."""
+    N = F.shape[0]
+    o = t1.shape[0]
+    mm = np.ascontiguousarray(mm, dtype=np.int32)
+    nn = np.ascontiguousarray(nn, dtype=np.int32)
+    out = np.zeros(len(mm))
+    F, R, t1, t2 = c64(F), c64(R), c64(t1), c64(t2)
+    lib().orc_doubles_sample(N, o, _p(F), _p(R), _p(t1), _p(t2), mm.ctypes.data_as(_ip), nn.ctypes.data_as(_ip),
+                             len(mm), _p(out))
+    return out
 
 
 def energy(F, R, t1, t2, eref):

@@ -1,0 +1,164 @@
+"""CPU tests of the host side: the C-ABI library, keywords, generators, replicas, stencils."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from helios_gb300 import molecules, polariz, replicas
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="session")
+def lib():
+    import shutil
+    if not (shutil.which("nvcc") or os.path.exists("/usr/local/cuda/bin/nvcc")):
+        pytest.skip("nvcc is not installed")
+    from helios_gb300 import build as b
+    b.build()
+    from helios_gb300 import api
+    return api.library()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    header = open(os.path.join(ROOT, "include", "helios_cc.h")).read()
+    declared = set(re.findall(r"\b(hx_[a-z_0-9]+)\s*\(", header))
+    assert {"hx_ccsd_create", "hx_ccsd_init", "hx_ccsd_iterate", "hx_ccsd_energy", "hx_ccsd_solve",
+            "hx_ccsd_destroy", "hx_last_error"} <= declared
+    for name in declared:
+        assert hasattr(lib, name), name
+
+
+def test_default_parameters_are_helios_defaults(lib):
+    from helios_gb300 import api
+    p = api.CCParams()
+    lib.hx_cc_params_default(ctypes.byref(p))
+    assert p.cc_maxiter == 2000 and p.cc_eps == 1e-12 and p.diis_steps == 20 and p.diis_enabled == 1
+    assert p.scf_maxiter == 400 and p.scf_eps == 1e-12 and p.scf_step == 0.05
+    assert p.projection_type == 2 and p.divergence_threshold == 1e3 and p.stagnation_after == 200
+    assert p.stagnation_threshold == 60.0
+
+
+def test_keywords_potentiate_like_the_reference(lib):
+    from helios_gb300 import api
+    p = api.Keywords(accuracy=10, scf_accuracy=11, divergence_threshold=4, projection_type="2-1").to_c()
+    assert p.cc_eps == pytest.approx(1e-10) and p.scf_eps == pytest.approx(1e-11)
+    assert p.divergence_threshold == pytest.approx(1e4) and p.projection_type == 2
+
+
+def test_create_rejects_bad_input_without_a_gpu_call(lib):
+    from helios_gb300 import api
+    p = api.Keywords().to_c()
+    h = ctypes.c_void_p()
+    assert lib.hx_ccsd_create_batch(None, 0, ctypes.byref(p), ctypes.byref(h)) == -100
+    buf = ctypes.create_string_buffer(256)
+    assert lib.hx_last_error(buf, 256) > 0
+
+
+def _is_perfect_matching(mol):
+    seen = set()
+    for (i, j, beta, kind) in mol.bonds:
+        if kind == "double":
+            if i in seen or j in seen:
+                return False
+            seen.update((i, j))
+    return len(seen) == mol.n_sites
+
+
+@pytest.mark.parametrize("n", [4, 6, 8, 10, 12, 30, 64])
+def test_ladder_geometry_and_kekule(n):
+    m = molecules.ladder(n)
+    assert m.n_sites == n and m.n_electrons == n
+    assert _is_perfect_matching(m)
+    assert np.allclose(m.coords[:, 2], 0.0)
+    for (i, j, _, _) in m.bonds:
+        assert np.linalg.norm(m.coords[i] - m.coords[j]) == pytest.approx(1.40)
+
+
+@pytest.mark.parametrize("n", [2, 12, 160])
+def test_polyene_geometry(n):
+    m = molecules.polyene(n)
+    assert _is_perfect_matching(m)
+    for k, (i, j, _, kind) in enumerate(m.bonds):
+        d = np.linalg.norm(m.coords[i] - m.coords[j])
+        assert d == pytest.approx(1.35 if kind == "double" else 1.46)
+    if n >= 3:
+        a, b, c = m.coords[0], m.coords[1], m.coords[2]
+        cosang = np.dot(a - b, c - b) / np.linalg.norm(a - b) / np.linalg.norm(c - b)
+        assert cosang == pytest.approx(-0.5)
+
+
+def test_random_ensemble_is_seeded_and_in_range():
+    a = molecules.ensemble(100, 64)
+    b = molecules.ensemble(100, 64)
+    assert [m.name for m in a] == [m.name for m in b]
+    assert all(8 <= m.n_sites <= 64 and m.n_sites % 2 == 0 for m in a)
+    kinds = {m.name.split("-")[1] for m in a}
+    assert kinds == {"polyene", "ladder"}
+    assert all(_is_perfect_matching(m) for m in a)
+
+
+def test_stencil_weights_match_oracle():
+    from oracle.polariz import lagrange_derivative_weights
+    for n in (3, 5, 7, 9):
+        assert np.allclose(polariz.lagrange_weights(n, 2), lagrange_derivative_weights(n, 2), atol=1e-12)
+    assert np.allclose(polariz.lagrange_weights(5, 2) * 12, [-1, 16, -30, 16, -1])
+
+
+def test_alpha_of_a_quadratic_energy():
+    # E(F) = E0 - alpha_ev F^2 / 2 in eV with F in V/Angstrom -> alpha in a.u.
+    h = 0.0514221
+    F = np.arange(-2, 3) * h
+    a_au = 123.0
+    alpha_ev = a_au / (polariz.HARTREE_ENERGY / polariz.BOHR_RADIUS ** 2)
+    E = -5.0 - 0.5 * alpha_ev * F ** 2
+    assert polariz.alpha_from_energies(E, h) == pytest.approx(a_au, rel=1e-12)
+
+
+def test_field_molecule_equals_oracle_field_model():
+    from oracle.ppp import build_model
+    m = molecules.polyene(10)
+    a = build_model(polariz.field_molecule(m, 0.03), alternation=0.1)
+    b = build_model(m, alternation=0.1, field=(0.03, 0, 0))
+    assert np.allclose(a["core"], b["core"], atol=1e-13)
+    assert np.allclose(a["huckelCore"], b["huckelCore"], atol=1e-13)
+
+
+def test_shards_cover_every_molecule_once():
+    mols = molecules.ensemble(7, 50)
+    for world in (1, 2, 3, 8):
+        got = sorted(i for r in range(world) for i in replicas.shard(mols, r, world))
+        assert got == list(range(len(mols)))
+
+
+def _replica_worker(rank, world, port, q):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from oracle.literal import solve_literal
+    mols = [molecules.polyene(n) for n in (4, 6, 8, 4, 6)]
+    mine = replicas.shard(mols, rank, world)
+    local = {i: solve_literal(mols[i], eps=1e-10)["ecorr"] for i in mine}
+    out = replicas.gather(local, rank, world)
+    if rank == 0:
+        q.put(out)
+    dist.destroy_process_group()
+
+
+def test_replicas_gather_over_gloo():
+    import multiprocessing as mp
+    import random
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = 29500 + random.randint(0, 2000)
+    ps = [ctx.Process(target=_replica_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in ps:
+        p.start()
+    out = q.get(timeout=120)
+    for p in ps:
+        p.join(timeout=60)
+    assert sorted(out) == [0, 1, 2, 3, 4]
+    assert out[0] == pytest.approx(out[3]) and out[1] == pytest.approx(out[4])
