@@ -407,7 +407,8 @@ __global__ void k_setup(const CCMol *mols, const int *active)
             int j = (int)(r % o); r /= o;
             int a = (int)(r % v);
             int i = (int)(r / v);
-            m.D2[f] = m.Fmo[i * n + i] + m.Fmo[j * n + j] - m.Fmo[(o + a) * n + o + a] - m.Fmo[(o + b) * n + o + b];
+            // grouped so that (ia),(jb) and (jb),(ia) round identically
+            m.D2[f] = (m.Fmo[i * n + i] + m.Fmo[j * n + j]) - (m.Fmo[(o + a) * n + o + a] + m.Fmo[(o + b) * n + o + b]);
         } else {
             long long f = e - ov - ov * ov;
             int mu = (int)(f / ov), r = (int)(f % ov), k = r / v, c = r % v;
@@ -429,8 +430,11 @@ __global__ void k_setup2(const CCMol *mols, const int *active, int guess)
         int j = (int)(r % o); r /= o;
         int a = (int)(r % v);
         int i = (int)(r / v);
-        double g = m.gov[e];
-        double gx = m.gov[(((long long)i * v + b) * o + j) * v + a];
+        // canonical (upper-triangle) values: the guess and L are exactly pair-symmetric
+        const long long p1 = (long long)i * v + a, q1 = (long long)j * v + b;
+        const long long p2 = (long long)i * v + b, q2 = (long long)j * v + a;
+        double g = m.gov[min(p1, q1) * ov + max(p1, q1)];
+        double gx = m.gov[min(p2, q2) * ov + max(p2, q2)];
         double L = 2.0 * g - gx;
         m.Lov[e] = L;
         if (guess) m.t2[e] = L / m.D2[e];     // R(i,a,j,b) / (F_ii+F_jj-F_aa-F_bb)

@@ -63,7 +63,6 @@ constexpr int TMEM_COLS = 512;                       // 2 buffers x NQ classes x
 constexpr unsigned long long WAIT_NS = 4000000000ull; // a wait longer than 4 s is declared failed
 
 struct TcDesc {
-    long long a_base, b_base;        // element offsets into the A / B scratch
     int batch, M, N, K, Mp, Np, Kp;
     int Mi, Ni;
     long long c[5];
@@ -463,6 +462,8 @@ struct Engine {
     size_t scratch_elems = 0;
     int *rexp = nullptr;              // per-row exponents of every operand of the largest group
     size_t rexp_elems = 0;
+    __nv_bfloat16 *fixed = nullptr;   // slices of the constant operands of every group (persistent)
+    int *fixed_rexp = nullptr;
     int *d_err = nullptr;
     std::vector<SubGroup> groups;     // one per plan group, same order
     std::vector<const Group *> keys;
@@ -539,14 +540,19 @@ int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s)
     *out = nullptr;
     Engine *e = new Engine();
     // pass 1: sizes
-    size_t need = 0, need_rows = 0;
+    // variable operands share one scratch (groups run one after another);
+    // constant operands keep their slices for the life of the engine
+    size_t need = 0, need_rows = 0, fneed = 0, frows = 0;
     for (const Group &g : plan) {
         size_t gneed = 0, grows = 0;
         for (const TgemmDesc &t : g.h) {
             double work = (double)t.batch * t.M * t.N * t.K;
             if (work < kMinTcWork) continue;
-            gneed += (size_t)S * t.batch * (rup(t.M, BM) + rup(t.N, BN)) * rup(t.K, BK);
-            grows += (size_t)t.batch * (rup(t.M, BM) + rup(t.N, BN));
+            const size_t Kp = rup(t.K, BK), Ma = rup(t.M, BM), Nb = rup(t.N, BN);
+            (t.a_const ? fneed : gneed) += (size_t)S * t.batch * Ma * Kp;
+            (t.b_const ? fneed : gneed) += (size_t)S * t.batch * Nb * Kp;
+            (t.a_const ? frows : grows) += (size_t)t.batch * Ma;
+            (t.b_const ? frows : grows) += (size_t)t.batch * Nb;
         }
         need = std::max(need, gneed);
         need_rows = std::max(need_rows, grows);
@@ -554,11 +560,15 @@ int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s)
     e->scratch_elems = need;
     e->rexp_elems = need_rows;
     if ((need && cudaMalloc(&e->scratch, need * sizeof(__nv_bfloat16)) != cudaSuccess) ||
-        (need_rows && cudaMalloc(&e->rexp, need_rows * sizeof(int)) != cudaSuccess)) {
-        hx_set_error("cudaMalloc of %zu bytes of tensor-core scratch failed", need * 2 + need_rows * 4);
+        (need_rows && cudaMalloc(&e->rexp, need_rows * sizeof(int)) != cudaSuccess) ||
+        (fneed && cudaMalloc(&e->fixed, fneed * sizeof(__nv_bfloat16)) != cudaSuccess) ||
+        (frows && cudaMalloc(&e->fixed_rexp, frows * sizeof(int)) != cudaSuccess)) {
+        hx_set_error("cudaMalloc of %zu bytes of tensor-core scratch failed",
+                     (need + fneed) * 2 + (need_rows + frows) * 4);
         destroy(e);
         return HX_ERR_NOMEM;
     }
+    size_t foff = 0, froff = 0;
     if (cudaMalloc(&e->d_err, sizeof(int)) != cudaSuccess) { delete e; return HX_ERR_NOMEM; }
     cudaMemsetAsync(e->d_err, 0, sizeof(int), s);
     // pass 2: descriptors and tensor maps
@@ -586,27 +596,29 @@ int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s)
             d.ksplit = (nkb + d.kb_per - 1) / d.kb_per;
             d.tile_start = tiles;
             tiles += out_tiles * d.ksplit;
-            d.a_base = (long long)off;
-            size_t asz = (size_t)S * d.batch * d.Mp * d.Kp;
-            d.b_base = (long long)(off + asz);
-            size_t bsz = (size_t)S * d.batch * d.Np * d.Kp;
-            int rc = make_map(&d.mapA, e->scratch + d.a_base, (long long)S * d.batch * d.Mp, d.Kp, BM);
-            if (rc == HX_OK) rc = make_map(&d.mapB, e->scratch + d.b_base, (long long)S * d.batch * d.Np, d.Kp, BN);
+            const size_t asz = (size_t)S * d.batch * d.Mp * d.Kp;
+            const size_t bsz = (size_t)S * d.batch * d.Np * d.Kp;
+            __nv_bfloat16 *abuf, *bbuf;
+            int *aexp, *bexp;
+            if (t.a_const) { abuf = e->fixed + foff; foff += asz; aexp = e->fixed_rexp + froff; froff += (size_t)t.batch * d.Mp; }
+            else { abuf = e->scratch + off; off += asz; aexp = e->rexp + roff; roff += (size_t)t.batch * d.Mp; }
+            if (t.b_const) { bbuf = e->fixed + foff; foff += bsz; bexp = e->fixed_rexp + froff; froff += (size_t)t.batch * d.Np; }
+            else { bbuf = e->scratch + off; off += bsz; bexp = e->rexp + roff; roff += (size_t)t.batch * d.Np; }
+            int rc = make_map(&d.mapA, abuf, (long long)S * d.batch * d.Mp, d.Kp, BM);
+            if (rc == HX_OK) rc = make_map(&d.mapB, bbuf, (long long)S * d.batch * d.Np, d.Kp, BN);
             if (rc < 0) { destroy(e); return rc; }
             PrepDesc pa, pb;
             memset(&pa, 0, sizeof(pa));
-            pa.src = t.A; pa.dst = e->scratch + d.a_base; pa.batch = t.batch; pa.R = t.M; pa.K = t.K;
+            pa.src = t.A; pa.dst = abuf; pa.batch = t.batch; pa.R = t.M; pa.K = t.K;
             pa.Rp = d.Mp; pa.Kp = d.Kp; pa.Ri = t.Mi; pa.Ki = t.Ki; pa.mol = t.mol;
             pa.s[0] = t.a[0]; pa.s[1] = t.a[1]; pa.s[2] = t.a[2]; pa.s[3] = t.a[3]; pa.s[4] = t.a[4];
-            pa.rexp = e->rexp + roff;
-            d.expA = pa.rexp;
-            roff += (size_t)t.batch * d.Mp;
+            pa.rexp = aexp;
+            d.expA = aexp;
             pb = pa;
-            pb.src = t.B; pb.dst = e->scratch + d.b_base; pb.R = t.N; pb.Rp = d.Np; pb.Ri = t.Ni;
+            pb.src = t.B; pb.dst = bbuf; pb.R = t.N; pb.Rp = d.Np; pb.Ri = t.Ni;
             pb.s[0] = t.b[0]; pb.s[1] = t.b[1]; pb.s[2] = t.b[2]; pb.s[3] = t.b[3]; pb.s[4] = t.b[4];
-            pb.rexp = e->rexp + roff;
-            d.expB = pb.rexp;
-            roff += (size_t)t.batch * d.Np;
+            pb.rexp = bexp;
+            d.expB = bexp;
             auto add = [&](PrepList &L, PrepDesc p) {
                 p.work_start = L.work;
                 p.row_start = L.rows;
@@ -617,7 +629,6 @@ int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s)
             add(t.a_const ? sg.fixed : sg.var, pa);
             add(t.b_const ? sg.fixed : sg.var, pb);
             sg.tcd.push_back(d);
-            off += asz + bsz;
         }
         sg.tiles = tiles;
         if (!sg.tcd.empty()) {
@@ -728,6 +739,8 @@ void destroy(Engine *e)
     for (auto x : e->pool) cudaEventDestroy(x);
     cudaFree(e->scratch);
     cudaFree(e->rexp);
+    cudaFree(e->fixed);
+    cudaFree(e->fixed_rexp);
     cudaFree(e->d_err);
     delete e;
 }
