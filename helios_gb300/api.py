@@ -80,7 +80,8 @@ def library():
 
 
 def gemm(A, B, precision="fp64", reps=1):
-    """C = A @ B.T on the engine's FP64 or tensor-core GEMM; returns (C, ms per launch)."""
+    """C = A @ B.T on the engine's FP64 ("fp64") or tensor-core GEMM ("mixed": 3 slices,
+    "high": 5 slices); returns (C, ms per launch)."""
     A = np.ascontiguousarray(A, dtype=np.float64)
     B = np.ascontiguousarray(B, dtype=np.float64)
     M, K = A.shape
@@ -88,7 +89,7 @@ def gemm(A, B, precision="fp64", reps=1):
     C = np.zeros((M, N))
     ms = ctypes.c_double()
     _check(library().hx_gemm(A.ctypes.data_as(_c_d), B.ctypes.data_as(_c_d), C.ctypes.data_as(_c_d), M, N, K,
-                             {"fp64": 0, "mixed": 1}[precision], reps, ctypes.byref(ms)))
+                             {"fp64": 0, "mixed": 1, "high": 2}[precision], reps, ctypes.byref(ms)))
     return C, ms.value
 
 
@@ -127,8 +128,8 @@ class Keywords:
     stagnation_check_after: int = 200            # iteration:stagnation-check-after
     precision: str = "fp64"                      # engine: "fp64" or "mixed"
     guess: str = "reference"                     # engine: "reference" (guessCC) or "learned"
-    mixed_switch: float = 1e-6                   # engine: residual where mixed hands over to FP64
-    mixed_patience: int = 3                      # engine: non-improving mixed iterations before FP64
+    mixed_switch: float = 1e-6                   # engine: residual where 3-slice hands over to 5-slice
+    mixed_patience: int = 3                      # engine: non-improving iterations before the next phase
 
     def to_c(self) -> CCParams:
         p = CCParams()
@@ -252,7 +253,8 @@ class CoupledCluster:
                 "accuracy": out[3], "status": int(st[0]), "iterations": int(st[1])}
 
     def trace(self, mol: int = 0) -> np.ndarray:
-        """Per-iteration (max|d1|, max|d2|, E_total, seconds, mixed?) of the last solve."""
+        """Per-iteration (max|d1|, max|d2|, E_total, seconds, phase) of the last solve;
+        phase 2 = 3-slice tensor cores, 1 = 5-slice tensor cores, 0 = FP64."""
         n = _check(library().hx_ccsd_trace(self._h, mol, None, 0))
         out = np.zeros((max(n, 1), 5))
         library().hx_ccsd_trace(self._h, mol, out.ctypes.data_as(_c_d), n)

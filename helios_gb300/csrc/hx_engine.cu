@@ -163,6 +163,8 @@ struct Rules {   // gIterator.f90:88-210
     }
 };
 
+enum { PH_FP64 = 0, PH_HIGH = 1, PH_LOW = 2 };
+
 struct hx_ccsd {
     hx_cc_params p{};
     int nmol = 0;
@@ -193,10 +195,11 @@ struct hx_ccsd {
     std::vector<Rules> rules;
     std::vector<int> status;
     tc::Engine *tce = nullptr;           // tensor-core backend (mixed precision)
-    // mixed precision: per-molecule phase (1 = tensor-core iterations) and masks
-    std::vector<int> phase_tc, stall;
+    // mixed precision: per-molecule phase (PH_LOW / PH_HIGH tensor-core
+    // iterations, PH_FP64 CUDA-core FP64) and the matching launch masks
+    std::vector<int> phase, stall;
     std::vector<double> best;
-    int *d_act_tc = nullptr, *d_act_fp = nullptr;
+    int *d_act_lo = nullptr, *d_act_hi = nullptr, *d_act_fp = nullptr;
     std::vector<std::vector<std::array<double, 5>>> trace;
     // device time of the last hx_ccsd_init and solve (events on st)
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -249,22 +252,25 @@ static int upload_group(Group &g)
     return HX_OK;
 }
 
-// Molecules in their tensor-core phase run the group on tcgen05 (d_act_tc),
-// the others on the FP64 kernel (d_act_fp); each kernel skips the rest.
+// Each molecule runs the group in its current phase: the tensor-core modes
+// on tcgen05 (d_act_lo / d_act_hi), the others on the FP64 kernel (d_act_fp);
+// every launch skips the molecules that are not its own.
 static int run_group(hx_ccsd *h, Group &g)
 {
     if (g.tiles == 0) return HX_OK;
     if (h->tce) {
-        int n_tc = 0, n_fp = 0;
-        for (int mi = 0; mi < h->nmol; ++mi) {
-            if (!h->active[mi]) continue;
-            if (h->phase_tc[mi]) ++n_tc; else ++n_fp;
-        }
-        if (n_tc) {
-            cudaError_t e = tc::run_group(h->tce, g.h.data(), (int)g.h.size(), h->d_act_tc, h->st);
+        int n[3] = {0, 0, 0};
+        for (int mi = 0; mi < h->nmol; ++mi)
+            if (h->active[mi]) ++n[h->phase[mi]];
+        if (n[PH_LOW]) {
+            cudaError_t e = tc::run_group(h->tce, g.h.data(), (int)g.h.size(), h->d_act_lo, h->st, 0);
             if (e != cudaSuccess) { hx_set_error("tensor-core group: %s", cudaGetErrorString(e)); return HX_ERR_CUDA; }
         }
-        if (n_fp) HX_CU(hx_tgemm_f64_launch(g.d, (int)g.h.size(), g.tiles, h->d_act_fp, h->st));
+        if (n[PH_HIGH]) {
+            cudaError_t e = tc::run_group(h->tce, g.h.data(), (int)g.h.size(), h->d_act_hi, h->st, 1);
+            if (e != cudaSuccess) { hx_set_error("tensor-core group: %s", cudaGetErrorString(e)); return HX_ERR_CUDA; }
+        }
+        if (n[PH_FP64]) HX_CU(hx_tgemm_f64_launch(g.d, (int)g.h.size(), g.tiles, h->d_act_fp, h->st));
         return HX_OK;
     }
     HX_CU(hx_tgemm_f64_launch(g.d, (int)g.h.size(), g.tiles, h->d_active, h->st));
@@ -273,15 +279,17 @@ static int run_group(hx_ccsd *h, Group &g)
 
 static int upload_masks(hx_ccsd *h)
 {
-    std::vector<int> a(h->nmol), b(h->nmol);
+    std::vector<int> lo(h->nmol), hi(h->nmol), fp(h->nmol);
     for (int mi = 0; mi < h->nmol; ++mi) {
-        a[mi] = h->active[mi] && h->phase_tc[mi];
-        b[mi] = h->active[mi] && !h->phase_tc[mi];
+        lo[mi] = h->active[mi] && h->phase[mi] == PH_LOW;
+        hi[mi] = h->active[mi] && h->phase[mi] == PH_HIGH;
+        fp[mi] = h->active[mi] && h->phase[mi] == PH_FP64;
     }
     HX_CU(cudaMemcpyAsync(h->d_active, h->active.data(), sizeof(int) * h->nmol, cudaMemcpyHostToDevice, h->st));
-    if (h->d_act_tc) {
-        HX_CU(cudaMemcpyAsync(h->d_act_tc, a.data(), sizeof(int) * h->nmol, cudaMemcpyHostToDevice, h->st));
-        HX_CU(cudaMemcpyAsync(h->d_act_fp, b.data(), sizeof(int) * h->nmol, cudaMemcpyHostToDevice, h->st));
+    if (h->d_act_lo) {
+        HX_CU(cudaMemcpyAsync(h->d_act_lo, lo.data(), sizeof(int) * h->nmol, cudaMemcpyHostToDevice, h->st));
+        HX_CU(cudaMemcpyAsync(h->d_act_hi, hi.data(), sizeof(int) * h->nmol, cudaMemcpyHostToDevice, h->st));
+        HX_CU(cudaMemcpyAsync(h->d_act_fp, fp.data(), sizeof(int) * h->nmol, cudaMemcpyHostToDevice, h->st));
     }
     // the masks are pageable host vectors: wait so they may go out of scope
     HX_CU(cudaStreamSynchronize(h->st));
@@ -437,10 +445,11 @@ static int allocate(hx_ccsd *h)
     for (int mi = 0; mi < h->nmol; ++mi) maxpair = std::max<long long>(maxpair, (long long)h->o[mi] * h->v[mi] * h->o[mi] * h->v[mi]);
     h->nblk = (int)std::max<long long>(1, std::min<long long>(std::max(1, 1216 / h->nmol), (maxpair + 4095) / 4096));
     HX_CU(cudaMalloc(&h->d_part, sizeof(double) * std::max<size_t>((size_t)h->nmol * h->nblk * HX_MAX_DIIS, 2 * HX_SCF_GRID_MAX)));
-    HX_CU(cudaMalloc(&h->d_act_tc, sizeof(int) * h->nmol));
+    HX_CU(cudaMalloc(&h->d_act_lo, sizeof(int) * h->nmol));
+    HX_CU(cudaMalloc(&h->d_act_hi, sizeof(int) * h->nmol));
     HX_CU(cudaMalloc(&h->d_act_fp, sizeof(int) * h->nmol));
     h->active.assign(h->nmol, 1);
-    h->phase_tc.assign(h->nmol, 0);
+    h->phase.assign(h->nmol, PH_FP64);
     h->stall.assign(h->nmol, 0);
     h->best.assign(h->nmol, 1e300);
     h->trace.assign(h->nmol, {});
@@ -689,10 +698,20 @@ int hx_ccsd_energy(hx_ccsd *h, double e[5])
 }
 
 // The iterator (gIterator.f90:88-210) over every active molecule. In mixed
-// precision a molecule starts on the tensor cores and moves on to FP64
-// iterations (keeping its DIIS history) once its residual falls below
-// mixed_switch or stops improving; convergence is only declared on an FP64
-// residual, so the final answer is FP64-verified.
+// precision a molecule runs three phases:
+//   LOW   3-slice tensor-core contractions (~FP32 accuracy) until its residual
+//         falls below mixed_switch or stops improving for mixed_patience
+//         iterations; DIIS restarts (its error vectors are too noisy to mix
+//         with more accurate ones);
+//   HIGH  5-slice tensor-core contractions (residuals as accurate as FP64
+//         ones) until the residual is below kHighMargin * eps (or stops
+//         improving): the iteration is not monotone, and one more HIGH
+//         iteration costs far less than an FP64 iteration whose residual
+//         lands just above eps;
+//   FP64  CUDA-core FP64 iterations: convergence is declared only here, so the
+//         final residual and energy are plain FP64 (the defect correction).
+static const double kHighMargin = 0.1;
+
 static int solve_all(hx_ccsd *h, int maxiter, double eps)
 {
     if (h->p.projection_type != 2) { hx_set_error("projection-type 1 is not built on the GPU path"); return HX_ERR_UNSUPPORTED; }
@@ -700,7 +719,7 @@ static int solve_all(hx_ccsd *h, int maxiter, double eps)
     int remaining = 0;
     for (int mi = 0; mi < h->nmol; ++mi) {
         remaining += h->active[mi];
-        h->phase_tc[mi] = mixed ? 1 : 0;
+        h->phase[mi] = mixed ? PH_LOW : PH_FP64;
         h->stall[mi] = 0;
         h->best[mi] = 1e300;
         h->trace[mi].clear();
@@ -723,20 +742,23 @@ static int solve_all(hx_ccsd *h, int maxiter, double eps)
             if (!h->active[mi]) continue;
             const double *r = &h->res[(size_t)mi * 8];
             const double a = std::max(r[0], r[1]);
-            h->trace[mi].push_back({r[0], r[1], r[2], secs, (double)h->phase_tc[mi]});
-            if (h->phase_tc[mi] && !cancel) {
-                // tensor-core phase: no convergence claim, hand over to FP64 instead
+            const int ph = h->phase[mi];
+            h->trace[mi].push_back({r[0], r[1], r[2], secs, (double)ph});
+            if (ph != PH_FP64 && !cancel) {
+                // tensor-core phases never claim convergence: they hand over
                 if (a < h->best[mi]) { h->best[mi] = a; h->stall[mi] = 0; } else ++h->stall[mi];
-                const bool handover = a < h->p.mixed_switch || a < eps || h->stall[mi] >= h->p.mixed_patience;
+                const double target = ph == PH_LOW ? std::max(h->p.mixed_switch, eps) : kHighMargin * eps;
+                const bool handover = a < target || h->stall[mi] >= h->p.mixed_patience;
                 Rules &R = h->rules[mi];
                 int s = R.update(handover ? std::max(a, eps * 2) : a, h->p, maxiter, eps, false);
                 if (s == HX_DIVERGED || s == HX_STAGNATED || s == HX_FAILED_MAXITER) {
                     h->status[mi] = s; h->active[mi] = 0; --remaining; changed = true;
                 } else if (handover) {
-                    // FP64 iterations restart DIIS: error vectors of the tensor-core
-                    // phase are not comparable with FP64 residuals
-                    h->phase_tc[mi] = 0; changed = true;
-                    HX_CU(cudaMemsetAsync(h->diis[mi].count, 0, sizeof(int), h->st));
+                    h->phase[mi] = ph == PH_LOW ? PH_HIGH : PH_FP64;
+                    h->stall[mi] = 0;
+                    h->best[mi] = 1e300;
+                    changed = true;
+                    if (ph == PH_LOW) HX_CU(cudaMemsetAsync(h->diis[mi].count, 0, sizeof(int), h->st));
                 }
                 continue;
             }
@@ -754,7 +776,7 @@ static int solve_all(hx_ccsd *h, int maxiter, double eps)
     HX_CU(cudaEventSynchronize(h->ev[3]));
     cudaEventElapsedTime(&h->solve_ms, h->ev[2], h->ev[3]);
     // keep every molecule addressable for getters / energy after the solve
-    for (int mi = 0; mi < h->nmol; ++mi) { h->active[mi] = 1; h->phase_tc[mi] = 0; }
+    for (int mi = 0; mi < h->nmol; ++mi) { h->active[mi] = 1; h->phase[mi] = PH_FP64; }
     HX_TRY(upload_masks(h));
     return HX_OK;
 }
@@ -890,7 +912,8 @@ void hx_ccsd_destroy(hx_ccsd *h)
     cudaFree(h->d_cc);
     cudaFree(h->d_diis);
     cudaFree(h->d_active);
-    cudaFree(h->d_act_tc);
+    cudaFree(h->d_act_lo);
+    cudaFree(h->d_act_hi);
     cudaFree(h->d_act_fp);
     cudaFree(h->d_part);
     if (h->st) cudaStreamDestroy(h->st);
@@ -930,10 +953,10 @@ int hx_gemm(const double *A, const double *B, double *C, int32_t M, int32_t N, i
         plan[0].h.push_back(tg(dA, dB, dC, 1, M, N, K, M, N, K, {0, K, 0, 1, 0}, {0, K, 0, 1, 0}, {0, N, 0, 1, 0}, 1.0, 1.0, 0));
         rc = upload_group(plan[0]);
     }
-    if (rc == HX_OK && precision == HX_PRECISION_MIXED) rc = tc::create(&te, plan, st);
+    if (rc == HX_OK && precision != HX_PRECISION_FP64) rc = tc::create(&te, plan, st);
     if (rc == HX_OK) {
         auto launch = [&]() -> cudaError_t {
-            if (te) return tc::run_group(te, plan[0].h.data(), 1, dact, st);
+            if (te) return tc::run_group(te, plan[0].h.data(), 1, dact, st, precision == 2 ? 1 : 0);
             return hx_tgemm_f64_launch(plan[0].d, 1, plan[0].tiles, dact, st);
         };
         cudaError_t ce = launch();               // warm-up

@@ -46,20 +46,34 @@
 
 namespace tc {
 
-constexpr int S = 3;                 // integer slices per FP64 operand
-constexpr int QMAX = 3;              // slice pairs with i + j <= QMAX are multiplied
-constexpr int NQ = QMAX + 1;         // accumulator classes q = i + j
-constexpr int BM = 128, BN = 64, BK = 64;
-constexpr int KC = 4;                // k-blocks per exact chunk: 3 pairs * 256 * 2^14 < 2^24
-constexpr int STAGES = 3;
-constexpr int ATILE = BM * BK * 2;                   // 16 KB per A slice
-constexpr int BTILE = BN * BK * 2;                   // 8 KB per B slice
-constexpr int STAGE_BYTES = S * (ATILE + BTILE);
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+// Two precisions of the same kernel. LOW: 3 slices, pairs i + j <= 3 (8 MMAs
+// per k-step), about 2^-24 of the row maxima. HIGH: 5 slices, pairs
+// i + j <= 5 (19 MMAs), about 2^-44: residuals as accurate as FP64 ones.
+template <int S_, int QMAX_, int BN_, int STAGES_, int KC_>
+struct Cfg {
+    static constexpr int S = S_;                     // integer slices per FP64 operand
+    static constexpr int QMAX = QMAX_;               // slice pairs with i + j <= QMAX are multiplied
+    static constexpr int NQ = QMAX_ + 1;             // accumulator classes q = i + j
+    static constexpr int BM = 128, BN = BN_, BK = 64;
+    static constexpr int KC = KC_;                   // k-blocks per exact chunk
+    static constexpr int STAGES = STAGES_;
+    static constexpr int ATILE = BM * BK * 2;        // bytes per A slice tile
+    static constexpr int BTILE = BN * BK * 2;        // bytes per B slice tile
+    static constexpr int STAGE_BYTES = S * (ATILE + BTILE);
+    static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+    static constexpr int EPI_COLS = BN / 2;          // columns drained per epilogue thread
+    static constexpr int PRODUCTS = [] { int n = 0; for (int i = 0; i < S_; ++i) for (int j = 0; j < S_; ++j) n += (i + j <= QMAX_); return n; }();
+    // exactness of a chunk: (pairs per class) * KC*64 * 2^14 < 2^24
+    static_assert(KC_ * 64 * 16384LL * (QMAX_ + 1 < S_ ? QMAX_ + 1 : S_) < (1LL << 24), "chunk too deep for exact sums");
+    static_assert(2 * NQ * BN_ <= 512, "two TMEM buffers must fit in 512 columns");
+    static_assert(STAGES_ * S_ * (128 * 64 * 2 + BN_ * 64 * 2) + 1280 <= 232448, "shared memory");
+};
+using Low = Cfg<3, 3, 64, 3, 4>;
+using High = Cfg<5, 5, 32, 2, 3>;
 constexpr int NTHREADS = 320;                       // 8 epilogue warps, producer, MMA issuer
 constexpr int EPI_THREADS = 256;
-constexpr int EPI_COLS = BN / 2;                     // columns drained per epilogue thread
-constexpr int TMEM_COLS = 512;                       // 2 buffers x NQ classes x 64 columns
+constexpr int TMEM_COLS = 512;
+constexpr int BM = 128, BK = 64, SMAX = 5;
 constexpr unsigned long long WAIT_NS = 4000000000ull; // a wait longer than 4 s is declared failed
 
 struct TcDesc {
@@ -225,6 +239,7 @@ __global__ void __launch_bounds__(256) row_scale(const PrepDesc *__restrict__ pd
     }
 }
 
+template <int S>
 __global__ void __launch_bounds__(256) split_gather(const PrepDesc *__restrict__ pd, int n, long long total,
                                                     const int *__restrict__ active)
 {
@@ -263,14 +278,15 @@ __global__ void __launch_bounds__(256) split_gather(const PrepDesc *__restrict__
 }
 
 // ------------------------------------------------------------------ the GEMM
+template <class C>
 __global__ void __launch_bounds__(NTHREADS, 1) tc_gemm(const TcDesc *__restrict__ descs, int ndesc,
                                                         const int *__restrict__ active, int *err)
 {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t *full = (uint64_t *)(smem + STAGES * STAGE_BYTES);
-    uint64_t *empty = full + STAGES;
-    uint64_t *acc_full = empty + STAGES;      // [2] MMA -> epilogue: chunk done in buffer b
+    uint64_t *full = (uint64_t *)(smem + C::STAGES * C::STAGE_BYTES);
+    uint64_t *empty = full + C::STAGES;
+    uint64_t *acc_full = empty + C::STAGES;      // [2] MMA -> epilogue: chunk done in buffer b
     uint64_t *acc_empty = acc_full + 2;       // [2] epilogue -> MMA: buffer b drained
     uint32_t *tmem_slot = (uint32_t *)(acc_empty + 2);
     __shared__ int s_d;
@@ -303,10 +319,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gemm(const TcDesc *__restrict_
     const int tm = first_m + in_g % gsz, tn = in_g / gsz;
     const int kb0 = ks * d.kb_per;
     const int nkb = min(d.Kp / BK - kb0, d.kb_per);     // >= 1 by construction
-    const int nchunk = (nkb + KC - 1) / KC;
+    const int nchunk = (nkb + C::KC - 1) / C::KC;
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
+        for (int s = 0; s < C::STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
         for (int b = 0; b < 2; ++b) { mbar_init(&acc_full[b], 1); mbar_init(&acc_empty[b], EPI_THREADS); }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -323,54 +339,54 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gemm(const TcDesc *__restrict_
 
     if (warp == 8) {
         if (lane == 0) {
-            const int arow0 = bt * d.Mp + tm * BM, brow0 = bt * d.Np + tn * BN;
+            const int arow0 = bt * d.Mp + tm * BM, brow0 = bt * d.Np + tn * C::BN;
             const int aplane = d.batch * d.Mp, bplane = d.batch * d.Np;
             for (int kb = 0; kb < nkb && ok; ++kb) {
-                const int st = kb % STAGES;
-                const uint32_t ph = (kb / STAGES) & 1;
+                const int st = kb % C::STAGES;
+                const uint32_t ph = (kb / C::STAGES) & 1;
                 ok = mbar_wait(&empty[st], ph ^ 1, err, 1);
                 if (!ok) break;
-                uint8_t *sa = smem + st * STAGE_BYTES;
-                uint8_t *sb = sa + S * ATILE;
-                mbar_expect_tx(&full[st], STAGE_BYTES);
-                for (int p = 0; p < S; ++p) {
-                    tma_load_2d(sa + p * ATILE, &d.mapA, &full[st], (kb0 + kb) * BK, p * aplane + arow0);
-                    tma_load_2d(sb + p * BTILE, &d.mapB, &full[st], (kb0 + kb) * BK, p * bplane + brow0);
+                uint8_t *sa = smem + st * C::STAGE_BYTES;
+                uint8_t *sb = sa + C::S * C::ATILE;
+                mbar_expect_tx(&full[st], C::STAGE_BYTES);
+                for (int p = 0; p < C::S; ++p) {
+                    tma_load_2d(sa + p * C::ATILE, &d.mapA, &full[st], (kb0 + kb) * BK, p * aplane + arow0);
+                    tma_load_2d(sb + p * C::BTILE, &d.mapB, &full[st], (kb0 + kb) * BK, p * bplane + brow0);
                 }
             }
         }
     } else if (warp == 9) {
         if (lane == 0) {
-            const uint32_t idesc = idesc_bf16(BM, BN);
+            const uint32_t idesc = idesc_bf16(BM, C::BN);
             for (int c = 0; c < nchunk && ok; ++c) {
                 const int buf = c & 1;
                 const uint32_t use = (uint32_t)(c >> 1);
                 ok = mbar_wait(&acc_empty[buf], (use & 1) ^ 1, err, 4);
                 if (!ok) break;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const uint32_t dbase = tmem + (uint32_t)(buf * NQ * BN);
-                const int kend = min(nkb, (c + 1) * KC);
-                for (int kb = c * KC; kb < kend && ok; ++kb) {
-                    const int st = kb % STAGES;
-                    const uint32_t ph = (kb / STAGES) & 1;
+                const uint32_t dbase = tmem + (uint32_t)(buf * C::NQ * C::BN);
+                const int kend = min(nkb, (c + 1) * C::KC);
+                for (int kb = c * C::KC; kb < kend && ok; ++kb) {
+                    const int st = kb % C::STAGES;
+                    const uint32_t ph = (kb / C::STAGES) & 1;
                     ok = mbar_wait(&full[st], ph, err, 2);
                     if (!ok) break;
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                    const uint32_t sa = smem_u32(smem + st * STAGE_BYTES);
-                    const uint32_t sb = sa + S * ATILE;
+                    const uint32_t sa = smem_u32(smem + st * C::STAGE_BYTES);
+                    const uint32_t sb = sa + C::S * C::ATILE;
 #pragma unroll
                     for (int kk = 0; kk < BK / 16; ++kk) {
 #pragma unroll
-                        for (int i = 0; i < S; ++i) {
+                        for (int i = 0; i < C::S; ++i) {
 #pragma unroll
-                            for (int j = 0; j < S; ++j) {
+                            for (int j = 0; j < C::S; ++j) {
                                 const int q = i + j;
-                                if (q > QMAX) continue;
-                                const uint64_t ad = sw128_desc(sa + i * ATILE + kk * 32);
-                                const uint64_t bd = sw128_desc(sb + j * BTILE + kk * 32);
+                                if (q > C::QMAX) continue;
+                                const uint64_t ad = sw128_desc(sa + i * C::ATILE + kk * 32);
+                                const uint64_t bd = sw128_desc(sb + j * C::BTILE + kk * 32);
                                 // the first product of a class in the chunk overwrites its accumulator
-                                const bool first = (kb == c * KC) && kk == 0 && i == (q < S ? 0 : q - (S - 1));
-                                mma_bf16(dbase + q * BN, ad, bd, idesc, first ? 0u : 1u);
+                                const bool first = (kb == c * C::KC) && kk == 0 && i == (q < C::S ? 0 : q - (C::S - 1));
+                                mma_bf16(dbase + q * C::BN, ad, bd, idesc, first ? 0u : 1u);
                             }
                         }
                     }
@@ -383,33 +399,48 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gemm(const TcDesc *__restrict_
         // epilogue: warps 0-7; warp w drains TMEM lanes 32*(w%4).. (output rows) and
         // the column half w/4 of the tile
         const int row = (warp & 3) * 32 + lane;
-        const int col0 = (warp >> 2) * EPI_COLS;
+        const int col0 = (warp >> 2) * C::EPI_COLS;
         const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
-        float hi[EPI_COLS], lo[EPI_COLS];
+        float hi[C::EPI_COLS], lo[C::EPI_COLS];
 #pragma unroll
-        for (int e = 0; e < EPI_COLS; ++e) { hi[e] = 0.f; lo[e] = 0.f; }
+        for (int e = 0; e < C::EPI_COLS; ++e) { hi[e] = 0.f; lo[e] = 0.f; }
         for (int c = 0; c < nchunk; ++c) {
             const int buf = c & 1;
             const uint32_t use = (uint32_t)(c >> 1);
             if (ok) ok = mbar_wait(&acc_full[buf], use & 1, err, 3);
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
-            for (int c0 = 0; c0 < EPI_COLS; c0 += 16) {
+            for (int c0 = 0; c0 < C::EPI_COLS; c0 += 16) {
                 // chunk value: exact integer classes combined with weights 2^-8q
-                float x[16], t[16];
-                tmem_ld16(tmem + lane_base + (uint32_t)(buf * NQ * BN + (NQ - 1) * BN + col0 + c0), x);
+                float x[16], t[16], xl[16];
+                tmem_ld16(tmem + lane_base + (uint32_t)(buf * C::NQ * C::BN + (C::NQ - 1) * C::BN + col0 + c0), x);
 #pragma unroll
-                for (int q = NQ - 2; q >= 0; --q) {
-                    tmem_ld16(tmem + lane_base + (uint32_t)(buf * NQ * BN + q * BN + col0 + c0), t);
+                for (int e = 0; e < 16; ++e) xl[e] = 0.f;
 #pragma unroll
-                    for (int e = 0; e < 16; ++e) x[e] = fmaf(x[e], 0.00390625f, t[e]);
+                for (int q = C::NQ - 2; q >= 0; --q) {
+                    tmem_ld16(tmem + lane_base + (uint32_t)(buf * C::NQ * C::BN + q * C::BN + col0 + c0), t);
+                    if constexpr (C::S > 3) {
+                        // float-float Horner step: (x, xl) = (x, xl) * 2^-8 + t, error of
+                        // the sum kept by TwoSum (the scaling is exact)
+#pragma unroll
+                        for (int e = 0; e < 16; ++e) {
+                            const float a = x[e] * 0.00390625f;
+                            const float s = a + t[e];
+                            const float bb = s - a;
+                            xl[e] = fmaf(xl[e], 0.00390625f, (a - (s - bb)) + (t[e] - bb));
+                            x[e] = s;
+                        }
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < 16; ++e) x[e] = fmaf(x[e], 0.00390625f, t[e]);
+                    }
                 }
 #pragma unroll
                 for (int e = 0; e < 16; ++e) {
                     // TwoSum of the chunk value into (hi, lo)
                     const float s = hi[c0 + e] + x[e];
                     const float bb = s - hi[c0 + e];
-                    lo[c0 + e] += (hi[c0 + e] - (s - bb)) + (x[e] - bb);
+                    lo[c0 + e] += ((hi[c0 + e] - (s - bb)) + (x[e] - bb)) + xl[e];
                     hi[c0 + e] = s;
                 }
             }
@@ -422,8 +453,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gemm(const TcDesc *__restrict_
             const long long offm = split_off(m, d.Mi, d.c[0], d.c[1]);
             const int ea = d.expA[(long long)bt * d.Mp + m];
 #pragma unroll
-            for (int e = 0; e < EPI_COLS; ++e) {
-                const int n = tn * BN + col0 + e;
+            for (int e = 0; e < C::EPI_COLS; ++e) {
+                const int n = tn * C::BN + col0 + e;
                 if (n >= d.N) continue;
                 const int eb = d.expB[(long long)bt * d.Np + n];
                 double *p = C + offm + split_off(n, d.Ni, d.c[2], d.c[3]);
@@ -457,15 +488,18 @@ struct SubGroup {
     Group fp64;                       // problems too small for the tensor cores
 };
 
-struct Engine {
-    __nv_bfloat16 *scratch = nullptr;
-    size_t scratch_elems = 0;
-    int *rexp = nullptr;              // per-row exponents of every operand of the largest group
-    size_t rexp_elems = 0;
-    __nv_bfloat16 *fixed = nullptr;   // slices of the constant operands of every group (persistent)
+struct Mode {                        // one precision: descriptors of every plan group
+    int S = 0, BN = 0, products = 0, smem = 0;
+    __nv_bfloat16 *fixed = nullptr;  // slices of the constant operands (persistent)
     int *fixed_rexp = nullptr;
+    std::vector<SubGroup> groups;    // one per plan group, same order
+};
+
+struct Engine {
+    __nv_bfloat16 *scratch = nullptr;   // slices of the variable operands (shared by groups and modes)
+    int *rexp = nullptr;
     int *d_err = nullptr;
-    std::vector<SubGroup> groups;     // one per plan group, same order
+    Mode mode[2];                        // 0 = LOW, 1 = HIGH
     std::vector<const Group *> keys;
     bool profile = false;
     int generation = 0;
@@ -535,50 +569,32 @@ static inline long long rup(long long x, long long m) { return (x + m - 1) / m *
 // Problems below this many multiply-adds stay on the FP64 CUDA-core kernel.
 static const double kMinTcWork = 4.0e6;
 
-int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s)
+static bool on_tc(const TgemmDesc &t) { return (double)t.batch * t.M * t.N * t.K >= kMinTcWork; }
+
+// Descriptors, tensor maps and slice storage of one precision mode.
+static int build_mode(Engine *e, Mode &md, const std::vector<Group> &plan, size_t var_elems_cap)
 {
-    *out = nullptr;
-    Engine *e = new Engine();
-    // pass 1: sizes
-    // variable operands share one scratch (groups run one after another);
-    // constant operands keep their slices for the life of the engine
-    size_t need = 0, need_rows = 0, fneed = 0, frows = 0;
-    for (const Group &g : plan) {
-        size_t gneed = 0, grows = 0;
+    const int S = md.S, BN = md.BN;
+    size_t fneed = 0, frows = 0;
+    for (const Group &g : plan)
         for (const TgemmDesc &t : g.h) {
-            double work = (double)t.batch * t.M * t.N * t.K;
-            if (work < kMinTcWork) continue;
+            if (!on_tc(t)) continue;
             const size_t Kp = rup(t.K, BK), Ma = rup(t.M, BM), Nb = rup(t.N, BN);
-            (t.a_const ? fneed : gneed) += (size_t)S * t.batch * Ma * Kp;
-            (t.b_const ? fneed : gneed) += (size_t)S * t.batch * Nb * Kp;
-            (t.a_const ? frows : grows) += (size_t)t.batch * Ma;
-            (t.b_const ? frows : grows) += (size_t)t.batch * Nb;
+            if (t.a_const) { fneed += (size_t)S * t.batch * Ma * Kp; frows += (size_t)t.batch * Ma; }
+            if (t.b_const) { fneed += (size_t)S * t.batch * Nb * Kp; frows += (size_t)t.batch * Nb; }
         }
-        need = std::max(need, gneed);
-        need_rows = std::max(need_rows, grows);
-    }
-    e->scratch_elems = need;
-    e->rexp_elems = need_rows;
-    if ((need && cudaMalloc(&e->scratch, need * sizeof(__nv_bfloat16)) != cudaSuccess) ||
-        (need_rows && cudaMalloc(&e->rexp, need_rows * sizeof(int)) != cudaSuccess) ||
-        (fneed && cudaMalloc(&e->fixed, fneed * sizeof(__nv_bfloat16)) != cudaSuccess) ||
-        (frows && cudaMalloc(&e->fixed_rexp, frows * sizeof(int)) != cudaSuccess)) {
-        hx_set_error("cudaMalloc of %zu bytes of tensor-core scratch failed",
-                     (need + fneed) * 2 + (need_rows + frows) * 4);
-        destroy(e);
+    if ((fneed && cudaMalloc(&md.fixed, fneed * sizeof(__nv_bfloat16)) != cudaSuccess) ||
+        (frows && cudaMalloc(&md.fixed_rexp, frows * sizeof(int)) != cudaSuccess)) {
+        hx_set_error("cudaMalloc of %zu bytes of constant slices failed", fneed * 2 + frows * 4);
         return HX_ERR_NOMEM;
     }
     size_t foff = 0, froff = 0;
-    if (cudaMalloc(&e->d_err, sizeof(int)) != cudaSuccess) { delete e; return HX_ERR_NOMEM; }
-    cudaMemsetAsync(e->d_err, 0, sizeof(int), s);
-    // pass 2: descriptors and tensor maps
     for (const Group &g : plan) {
         SubGroup sg;
         size_t off = 0, roff = 0;
         long long tiles = 0;
         for (const TgemmDesc &t : g.h) {
-            double w = (double)t.batch * t.M * t.N * t.K;
-            if (w < kMinTcWork) { sg.fp64.h.push_back(t); continue; }
+            if (!on_tc(t)) { sg.fp64.h.push_back(t); continue; }
             TcDesc d;
             memset(&d, 0, sizeof(d));
             d.batch = t.batch; d.M = t.M; d.N = t.N; d.K = t.K;
@@ -600,13 +616,14 @@ int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s)
             const size_t bsz = (size_t)S * d.batch * d.Np * d.Kp;
             __nv_bfloat16 *abuf, *bbuf;
             int *aexp, *bexp;
-            if (t.a_const) { abuf = e->fixed + foff; foff += asz; aexp = e->fixed_rexp + froff; froff += (size_t)t.batch * d.Mp; }
+            if (t.a_const) { abuf = md.fixed + foff; foff += asz; aexp = md.fixed_rexp + froff; froff += (size_t)t.batch * d.Mp; }
             else { abuf = e->scratch + off; off += asz; aexp = e->rexp + roff; roff += (size_t)t.batch * d.Mp; }
-            if (t.b_const) { bbuf = e->fixed + foff; foff += bsz; bexp = e->fixed_rexp + froff; froff += (size_t)t.batch * d.Np; }
+            if (t.b_const) { bbuf = md.fixed + foff; foff += bsz; bexp = md.fixed_rexp + froff; froff += (size_t)t.batch * d.Np; }
             else { bbuf = e->scratch + off; off += bsz; bexp = e->rexp + roff; roff += (size_t)t.batch * d.Np; }
+            if (off > var_elems_cap) { hx_set_error("tensor-core scratch overflow"); return HX_ERR_STATE; }
             int rc = make_map(&d.mapA, abuf, (long long)S * d.batch * d.Mp, d.Kp, BM);
             if (rc == HX_OK) rc = make_map(&d.mapB, bbuf, (long long)S * d.batch * d.Np, d.Kp, BN);
-            if (rc < 0) { destroy(e); return rc; }
+            if (rc < 0) return rc;
             PrepDesc pa, pb;
             memset(&pa, 0, sizeof(pa));
             pa.src = t.A; pa.dst = abuf; pa.batch = t.batch; pa.R = t.M; pa.K = t.K;
@@ -633,7 +650,6 @@ int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s)
         sg.tiles = tiles;
         if (!sg.tcd.empty()) {
             if (cudaMalloc(&sg.d_tcd, sizeof(TcDesc) * sg.tcd.size()) != cudaSuccess) {
-                destroy(e);
                 hx_set_error("descriptor allocation failed");
                 return HX_ERR_NOMEM;
             }
@@ -641,7 +657,6 @@ int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s)
             for (PrepList *L : {&sg.var, &sg.fixed}) {
                 if (L->h.empty()) continue;
                 if (cudaMalloc(&L->d, sizeof(PrepDesc) * L->h.size()) != cudaSuccess) {
-                    destroy(e);
                     hx_set_error("descriptor allocation failed");
                     return HX_ERR_NOMEM;
                 }
@@ -656,26 +671,62 @@ int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s)
             sg.fp64.d = nullptr;
             sg.fp64.tiles = 0;
         }
-        e->groups.push_back(sg);
-        e->keys.push_back(&g);
+        md.groups.push_back(std::move(sg));
     }
-    if (cudaFuncSetAttribute(tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) != cudaSuccess) {
+    return HX_OK;
+}
+
+int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s)
+{
+    *out = nullptr;
+    Engine *e = new Engine();
+    e->mode[0].S = Low::S; e->mode[0].BN = Low::BN; e->mode[0].products = Low::PRODUCTS; e->mode[0].smem = Low::SMEM_BYTES;
+    e->mode[1].S = High::S; e->mode[1].BN = High::BN; e->mode[1].products = High::PRODUCTS; e->mode[1].smem = High::SMEM_BYTES;
+    // variable operands share one scratch: the largest group of either mode
+    size_t need = 0, need_rows = 0;
+    for (const Mode &md : e->mode)
+        for (const Group &g : plan) {
+            size_t gneed = 0, grows = 0;
+            for (const TgemmDesc &t : g.h) {
+                if (!on_tc(t)) continue;
+                const size_t Kp = rup(t.K, BK), Ma = rup(t.M, BM), Nb = rup(t.N, md.BN);
+                if (!t.a_const) { gneed += (size_t)md.S * t.batch * Ma * Kp; grows += (size_t)t.batch * Ma; }
+                if (!t.b_const) { gneed += (size_t)md.S * t.batch * Nb * Kp; grows += (size_t)t.batch * Nb; }
+            }
+            need = std::max(need, gneed);
+            need_rows = std::max(need_rows, grows);
+        }
+    if ((need && cudaMalloc(&e->scratch, need * sizeof(__nv_bfloat16)) != cudaSuccess) ||
+        (need_rows && cudaMalloc(&e->rexp, need_rows * sizeof(int)) != cudaSuccess) ||
+        cudaMalloc(&e->d_err, sizeof(int)) != cudaSuccess) {
+        hx_set_error("cudaMalloc of %zu bytes of tensor-core scratch failed", need * 2 + need_rows * 4);
         destroy(e);
-        hx_set_error("cannot reserve %d bytes of shared memory for tc_gemm", SMEM_BYTES);
+        return HX_ERR_NOMEM;
+    }
+    cudaMemsetAsync(e->d_err, 0, sizeof(int), s);
+    for (Mode &md : e->mode) {
+        int rc = build_mode(e, md, plan, need);
+        if (rc < 0) { destroy(e); return rc; }
+    }
+    for (const Group &g : plan) e->keys.push_back(&g);
+    if (cudaFuncSetAttribute(tc_gemm<Low>, cudaFuncAttributeMaxDynamicSharedMemorySize, Low::SMEM_BYTES) != cudaSuccess ||
+        cudaFuncSetAttribute(tc_gemm<High>, cudaFuncAttributeMaxDynamicSharedMemorySize, High::SMEM_BYTES) != cudaSuccess) {
+        destroy(e);
+        hx_set_error("cannot reserve shared memory for tc_gemm");
         return HX_ERR_CUDA;
     }
     *out = e;
     return HX_OK;
 }
 
-cudaError_t run_group(Engine *e, const TgemmDesc *descs, int n, const int *d_active, cudaStream_t s)
+cudaError_t run_group(Engine *e, const TgemmDesc *descs, int n, const int *d_active, cudaStream_t s, int mode)
 {
-    // find the sub-group built for this plan group (same descriptor array)
     int gi = -1;
     for (size_t k = 0; k < e->keys.size(); ++k)
         if (e->keys[k]->h.data() == descs) { gi = (int)k; break; }
-    if (gi < 0) return cudaErrorInvalidValue;
-    SubGroup &sg = e->groups[gi];
+    if (gi < 0 || mode < 0 || mode > 1) return cudaErrorInvalidValue;
+    Mode &md = e->mode[mode];
+    SubGroup &sg = md.groups[gi];
     if (sg.fp64.tiles > 0) {
         cudaError_t r = hx_tgemm_f64_launch(sg.fp64.d, (int)sg.fp64.h.size(), sg.fp64.tiles, d_active, s);
         if (r != cudaSuccess) return r;
@@ -689,10 +740,12 @@ cudaError_t run_group(Engine *e, const TgemmDesc *descs, int n, const int *d_act
         cudaError_t x = cudaGetLastError();
         if (x != cudaSuccess) return x;
         long long blocks = std::min<long long>((L.work + 255) / 256, 1 << 16);
-        split_gather<<<(unsigned)blocks, 256, 0, s>>>(L.d, (int)L.h.size(), L.work, d_active);
+        if (md.S == Low::S) split_gather<Low::S><<<(unsigned)blocks, 256, 0, s>>>(L.d, (int)L.h.size(), L.work, d_active);
+        else split_gather<High::S><<<(unsigned)blocks, 256, 0, s>>>(L.d, (int)L.h.size(), L.work, d_active);
         hx_count_launches(2);
         return cudaGetLastError();
     };
+    // constant slices of this mode are made once per initialisation
     if (sg.fixed_gen != e->generation) {
         if ((r = prep(sg.fixed)) != cudaSuccess) return r;
         sg.fixed_gen = e->generation;
@@ -704,13 +757,13 @@ cudaError_t run_group(Engine *e, const TgemmDesc *descs, int n, const int *d_act
         pend.a = take_event(e);
         pend.b = take_event(e);
         for (const TcDesc &d : sg.tcd) {
-            double f = 2.0 * d.batch * (double)d.M * d.N * d.K;
-            pend.flops += f;
-            pend.hwflops += 2.0 * d.batch * (double)d.Mp * d.Np * d.Kp * 8;   // 8 slice products
+            pend.flops += 2.0 * d.batch * (double)d.M * d.N * d.K;
+            pend.hwflops += 2.0 * d.batch * (double)d.Mp * d.Np * d.Kp * md.products;
         }
         cudaEventRecord(pend.a, s);
     }
-    tc_gemm<<<(unsigned)sg.tiles, NTHREADS, SMEM_BYTES, s>>>(sg.d_tcd, (int)sg.tcd.size(), d_active, e->d_err);
+    if (mode == 0) tc_gemm<Low><<<(unsigned)sg.tiles, NTHREADS, Low::SMEM_BYTES, s>>>(sg.d_tcd, (int)sg.tcd.size(), d_active, e->d_err);
+    else tc_gemm<High><<<(unsigned)sg.tiles, NTHREADS, High::SMEM_BYTES, s>>>(sg.d_tcd, (int)sg.tcd.size(), d_active, e->d_err);
     r = cudaGetLastError();
     if (e->profile) {
         cudaEventRecord(pend.b, s);
@@ -729,18 +782,20 @@ int error_word(Engine *e)
 void destroy(Engine *e)
 {
     if (!e) return;
-    for (auto &g : e->groups) {
-        cudaFree(g.d_tcd);
-        cudaFree(g.var.d);
-        cudaFree(g.fixed.d);
-        if (g.fp64.d) cudaFree(g.fp64.d);
+    for (Mode &md : e->mode) {
+        for (auto &g : md.groups) {
+            cudaFree(g.d_tcd);
+            cudaFree(g.var.d);
+            cudaFree(g.fixed.d);
+            if (g.fp64.d) cudaFree(g.fp64.d);
+        }
+        cudaFree(md.fixed);
+        cudaFree(md.fixed_rexp);
     }
     for (auto &p : e->pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
     for (auto x : e->pool) cudaEventDestroy(x);
     cudaFree(e->scratch);
     cudaFree(e->rexp);
-    cudaFree(e->fixed);
-    cudaFree(e->fixed_rexp);
     cudaFree(e->d_err);
     delete e;
 }

@@ -7,8 +7,10 @@ namespace tc {
 struct Engine;
 // Build the backend for the GEMM groups of a plan (scratch sized to the largest operand).
 int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s);
-// Run one group: gather + split the operands to BF16 hi/lo, tcgen05 GEMM, FP64 epilogue.
-cudaError_t run_group(Engine *e, const TgemmDesc *descs, int n, const int *active_host, cudaStream_t s);
+// Run one plan group on the tensor cores: slice the operands, tcgen05 GEMM,
+// FP64 epilogue. mode 0 = LOW (3 slices, ~FP32 accuracy), 1 = HIGH (5 slices,
+// residuals as accurate as FP64 ones).
+cudaError_t run_group(Engine *e, const TgemmDesc *descs, int n, const int *d_active, cudaStream_t s, int mode);
 void destroy(Engine *e);
 // Device error word of the tensor-core kernels (0 = no wait timed out).
 int error_word(Engine *e);
