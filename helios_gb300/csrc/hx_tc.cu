@@ -38,6 +38,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "hx_common.cuh"
@@ -801,3 +802,136 @@ void destroy(Engine *e)
 }
 
 }  // namespace tc
+
+// ------------------------------------------------------------------ allocation-free single GEMM
+// hx_gemm_noalloc: one C = A B^T on the tensor cores with every piece of
+// scratch (operand slices, row exponents, the error word, the descriptors) in
+// one file-scope device array, so that a call allocates no memory. Its size
+// bounds the problem: M, N, K <= HX_NOALLOC_MAX_DIM (512), about 5.3 MB.
+namespace tc {
+namespace {
+
+constexpr size_t na_rup(size_t x, size_t m) { return (x + m - 1) / m * m; }
+constexpr int NA_DIM = HX_NOALLOC_MAX_DIM;
+constexpr size_t NA_SLICE_BYTES = (size_t)SMAX * NA_DIM * NA_DIM * sizeof(__nv_bfloat16);   // one operand
+constexpr size_t NA_OFF_A = 0;
+constexpr size_t NA_OFF_B = NA_OFF_A + NA_SLICE_BYTES;
+constexpr size_t NA_OFF_REXP = NA_OFF_B + NA_SLICE_BYTES;                    // int[2][NA_DIM]
+constexpr size_t NA_OFF_ERR = NA_OFF_REXP + 2 * NA_DIM * sizeof(int);
+constexpr size_t NA_OFF_TCD = na_rup(NA_OFF_ERR + sizeof(int), 256);
+constexpr size_t NA_OFF_PREP = na_rup(NA_OFF_TCD + sizeof(TcDesc), 256);
+constexpr size_t NA_BYTES = na_rup(NA_OFF_PREP + 2 * sizeof(PrepDesc), 256);
+
+__device__ __align__(256) unsigned char g_na_scratch[NA_BYTES];
+
+constexpr int NA_MAX_DEVICES = 64;
+std::mutex g_na_mutex;
+unsigned char *g_na_base[NA_MAX_DEVICES] = {};
+
+// Address of the static scratch on the current device, looked up once per
+// device (the first call on a device must not be inside a stream capture).
+int na_setup(unsigned char **base)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NA_MAX_DEVICES) {
+        hx_set_error("hx_gemm_noalloc: no usable current device");
+        return HX_ERR_CUDA;
+    }
+    std::lock_guard<std::mutex> lock(g_na_mutex);
+    if (!g_na_base[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_na_scratch);
+        if (e != cudaSuccess || !p) {
+            hx_set_error("hx_gemm_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+            return HX_ERR_CUDA;
+        }
+        if (cudaFuncSetAttribute(tc_gemm<Low>, cudaFuncAttributeMaxDynamicSharedMemorySize, Low::SMEM_BYTES) != cudaSuccess ||
+            cudaFuncSetAttribute(tc_gemm<High>, cudaFuncAttributeMaxDynamicSharedMemorySize, High::SMEM_BYTES) != cudaSuccess) {
+            hx_set_error("hx_gemm_noalloc: cannot reserve shared memory for tc_gemm");
+            return HX_ERR_CUDA;
+        }
+        g_na_base[dev] = (unsigned char *)p;
+    }
+    *base = g_na_base[dev];
+    return HX_OK;
+}
+
+}  // namespace
+}  // namespace tc
+
+extern "C" int hx_gemm_noalloc(const double *dA, const double *dB, double *dC, int32_t M, int32_t N, int32_t K,
+                               int32_t precision, void *stream)
+{
+    using namespace tc;
+    if (!dA || !dB || !dC || M <= 0 || N <= 0 || K <= 0) { hx_set_error("hx_gemm_noalloc: bad arguments"); return HX_ERR_ARG; }
+    if (M > HX_NOALLOC_MAX_DIM || N > HX_NOALLOC_MAX_DIM || K > HX_NOALLOC_MAX_DIM) {
+        hx_set_error("hx_gemm_noalloc: M=%d N=%d K=%d exceeds the static scratch limit of %d per dimension", M, N, K,
+                     HX_NOALLOC_MAX_DIM);
+        return HX_ERR_ARG;
+    }
+    if (precision != HX_PRECISION_MIXED && precision != 2) {
+        hx_set_error("hx_gemm_noalloc: precision must be 1 (3 slices) or 2 (5 slices)");
+        return HX_ERR_ARG;
+    }
+    unsigned char *base = nullptr;
+    int rc = na_setup(&base);
+    if (rc != HX_OK) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    const bool high = precision == 2;
+    const int S = high ? High::S : Low::S, BN = high ? High::BN : Low::BN;
+
+    __nv_bfloat16 *abuf = (__nv_bfloat16 *)(base + NA_OFF_A), *bbuf = (__nv_bfloat16 *)(base + NA_OFF_B);
+    int *aexp = (int *)(base + NA_OFF_REXP), *bexp = aexp + NA_DIM;
+    int *err = (int *)(base + NA_OFF_ERR);
+    TcDesc *d_tcd = (TcDesc *)(base + NA_OFF_TCD);
+    PrepDesc *d_prep = (PrepDesc *)(base + NA_OFF_PREP);
+
+    // the descriptor of hx_gemm's single problem: C = 1 * A B^T + 1 * C on a zeroed C
+    TcDesc d;
+    memset(&d, 0, sizeof(d));
+    d.batch = 1; d.M = M; d.N = N; d.K = K;
+    d.Mp = (int)rup(M, BM); d.Np = (int)rup(N, BN); d.Kp = (int)rup(K, BK);
+    d.Mi = M; d.Ni = N;
+    d.c[0] = 0; d.c[1] = N; d.c[2] = 0; d.c[3] = 1; d.c[4] = 0;
+    d.alpha = 1.0; d.beta = 1.0; d.C = dC; d.mol = 0;
+    d.tiles_m = d.Mp / BM; d.tiles_n = d.Np / BN;
+    d.kb_per = d.Kp / BK;            // K <= 512: at most 8 k-blocks, never split
+    d.ksplit = 1;
+    d.tile_start = 0;
+    d.expA = aexp; d.expB = bexp;
+    if ((rc = make_map(&d.mapA, abuf, (long long)S * d.Mp, d.Kp, BM)) != HX_OK) return rc;
+    if ((rc = make_map(&d.mapB, bbuf, (long long)S * d.Np, d.Kp, BN)) != HX_OK) return rc;
+    PrepDesc p[2];
+    memset(p, 0, sizeof(p));
+    p[0].src = dA; p[0].dst = abuf; p[0].rexp = aexp; p[0].batch = 1; p[0].R = M; p[0].K = K;
+    p[0].Rp = d.Mp; p[0].Kp = d.Kp; p[0].Ri = M; p[0].Ki = K;
+    p[0].s[0] = 0; p[0].s[1] = K; p[0].s[2] = 0; p[0].s[3] = 1; p[0].s[4] = 0;
+    p[1] = p[0];
+    p[1].src = dB; p[1].dst = bbuf; p[1].rexp = bexp; p[1].R = N; p[1].Rp = d.Np; p[1].Ri = N;
+    p[1].work_start = (long long)d.Mp * (d.Kp / 8);
+    p[1].row_start = d.Mp;
+    const long long rows = (long long)d.Mp + d.Np;
+    const long long work = rows * (d.Kp / 8);
+    const long long tiles = (long long)d.tiles_m * d.tiles_n;
+
+    // what must start at zero: the error word and C (accumulated with beta = 1)
+    cudaError_t ce = cudaMemsetAsync(err, 0, sizeof(int), s);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(dC, 0, sizeof(double) * (size_t)M * N, s);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_tcd, &d, sizeof(d), cudaMemcpyHostToDevice, s);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_prep, p, sizeof(p), cudaMemcpyHostToDevice, s);
+    if (ce == cudaSuccess) {
+        row_scale<<<(unsigned)((rows * 32 + 255) / 256), 256, 0, s>>>(d_prep, 2, rows, nullptr);
+        if (high) split_gather<High::S><<<(unsigned)((work + 255) / 256), 256, 0, s>>>(d_prep, 2, work, nullptr);
+        else split_gather<Low::S><<<(unsigned)((work + 255) / 256), 256, 0, s>>>(d_prep, 2, work, nullptr);
+        if (high) tc_gemm<High><<<(unsigned)tiles, NTHREADS, High::SMEM_BYTES, s>>>(d_tcd, 1, nullptr, err);
+        else tc_gemm<Low><<<(unsigned)tiles, NTHREADS, Low::SMEM_BYTES, s>>>(d_tcd, 1, nullptr, err);
+        hx_count_launches(3);
+        ce = cudaGetLastError();
+    }
+    int werr = 0;
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(&werr, err, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+    if (ce != cudaSuccess) { hx_set_error("hx_gemm_noalloc: %s", cudaGetErrorString(ce)); return HX_ERR_CUDA; }
+    if (werr) { hx_set_error("hx_gemm_noalloc: tensor-core wait timed out (code %d)", werr); return HX_ERR_KERNEL; }
+    return HX_OK;
+}

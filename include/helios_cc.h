@@ -187,6 +187,24 @@ void hx_ccsd_destroy(hx_ccsd *h);
 int hx_gemm(const double *A, const double *B, double *C, int32_t M, int32_t N, int32_t K, int32_t precision,
             int32_t reps, double *ms);
 
+/* Allocation-free variant of hx_gemm; it has no counterpart in the
+ * reference. C = A B^T for row-major FP64 matrices already in DEVICE memory
+ * (A: M x K, B: N x K, C: M x N), always on the tcgen05 exact-slice GEMM
+ * (precision 1: 3 slices, 2: 5 slices; FP64 is rejected). It calls no
+ * allocator: the operand slices, row exponents, error word and descriptors
+ * live in one static device array of about 5.3 MB, whose address is looked
+ * up once per device (cudaGetSymbolAddress) on the first call; make that
+ * first call before any stream capture. Dimensions above
+ * HX_NOALLOC_MAX_DIM return HX_ERR_ARG. C is zeroed and accumulated on
+ * `stream` (a cudaStream_t; NULL = the legacy default stream), and the call
+ * returns after the stream has synchronised. Results equal hx_gemm's bit for
+ * bit wherever hx_gemm uses the tensor cores (M*N*K >= 4e6). The scratch is
+ * shared: calls that overlap in time, on any streams or host threads, race
+ * and corrupt each other's results. */
+#define HX_NOALLOC_MAX_DIM 512
+int hx_gemm_noalloc(const double *A, const double *B, double *C, int32_t M, int32_t N, int32_t K,
+                    int32_t precision, void *stream);
+
 /* Copy the message of the last error (thread-local) into buf; returns its length. */
 int hx_last_error(char *buf, size_t len);
 
