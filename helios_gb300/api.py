@@ -30,6 +30,8 @@ COULOMB = {"ohno-klopman": 0, "mataga-nishimoto": 1, "hubbard": 2}
 
 _c_d = ctypes.POINTER(ctypes.c_double)
 _c_i = ctypes.POINTER(ctypes.c_int32)
+_c_f = ctypes.POINTER(ctypes.c_float)
+_c_l = ctypes.POINTER(ctypes.c_int64)
 
 
 class PPPModel(ctypes.Structure):
@@ -73,7 +75,8 @@ def library():
         for name in ("hx_ccsd_create", "hx_ccsd_create_batch", "hx_ccsd_init", "hx_ccsd_set_guess",
                      "hx_ccsd_iterate", "hx_ccsd_energy", "hx_ccsd_solve", "hx_ccsd_solve_batch",
                      "hx_ccsd_get_amplitudes", "hx_ccsd_get_scf", "hx_ccsd_dims", "hx_ccsd_trace",
-                     "hx_gemm", "hx_ccsd_timing", "hx_last_error"):
+                     "hx_gemm", "hx_ccsd_timing", "hx_last_error", "hx_ccsd_set_model", "hx_ccsd_training_rows",
+                     "hx_mlp_nparam", "hx_mlp_predict", "hx_mlp_grad", "hx_mlp_train"):
             getattr(lib, name).restype = ctypes.c_int
         _lib = lib
     return _lib
@@ -91,6 +94,44 @@ def gemm(A, B, precision="fp64", reps=1):
     _check(library().hx_gemm(A.ctypes.data_as(_c_d), B.ctypes.data_as(_c_d), C.ctypes.data_as(_c_d), M, N, K,
                              {"fp64": 0, "mixed": 1, "high": 2}[precision], reps, ctypes.byref(ms)))
     return C, ms.value
+
+
+def mlp_nparam() -> int:
+    return library().hx_mlp_nparam()
+
+
+def mlp_predict(params, X):
+    """Learned-guess network on input rows X [n, 8] (tcgen05 inference kernel)."""
+    P = np.ascontiguousarray(params, dtype=np.float32)
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    Y = np.zeros(X.shape[0], dtype=np.float32)
+    _check(library().hx_mlp_predict(P.ctypes.data_as(_c_f), X.ctypes.data_as(_c_f), ctypes.c_int64(X.shape[0]),
+                                    Y.ctypes.data_as(_c_f)))
+    return Y
+
+
+def mlp_grad(params, X, T):
+    """(loss, gradient blob) of the mean-squared error on rows X, T (GPU training kernels)."""
+    P = np.ascontiguousarray(params, dtype=np.float32)
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    T = np.ascontiguousarray(T, dtype=np.float32)
+    loss = ctypes.c_float()
+    G = np.zeros_like(P)
+    _check(library().hx_mlp_grad(P.ctypes.data_as(_c_f), X.ctypes.data_as(_c_f), T.ctypes.data_as(_c_f),
+                                 X.shape[0], ctypes.byref(loss), G.ctypes.data_as(_c_f)))
+    return float(loss.value), G
+
+
+def mlp_train(params, X, T, epochs=10, batch=4096, lr=1e-3, seed=0):
+    """Train on the GPU (Adam, cosine decay); returns (new params, per-epoch mean loss)."""
+    P = np.array(params, dtype=np.float32)
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    T = np.ascontiguousarray(T, dtype=np.float32)
+    L = np.zeros(epochs, dtype=np.float32)
+    _check(library().hx_mlp_train(P.ctypes.data_as(_c_f), X.ctypes.data_as(_c_f), T.ctypes.data_as(_c_f),
+                                  ctypes.c_int64(X.shape[0]), epochs, batch, ctypes.c_float(lr),
+                                  ctypes.c_uint64(seed), L.ctypes.data_as(_c_f)))
+    return P, L
 
 
 def last_error() -> str:
@@ -128,6 +169,7 @@ class Keywords:
     stagnation_check_after: int = 200            # iteration:stagnation-check-after
     precision: str = "fp64"                      # engine: "fp64" or "mixed"
     guess: str = "reference"                     # engine: "reference" (guessCC) or "learned"
+    model: object = None                         # engine: learned-guess parameters (None = the shipped model)
     mixed_switch: float = 1e-6                   # engine: residual where 3-slice hands over to 5-slice
     mixed_patience: int = 3                      # engine: non-improving iterations before the next phase
 
@@ -190,6 +232,8 @@ class CoupledCluster:
         models = (PPPModel * len(arrs))(*[a.c for a in arrs])
         self._params = self.keywords.to_c()
         _check(library().hx_ccsd_create_batch(models, len(arrs), ctypes.byref(self._params), ctypes.byref(self._h)))
+        if self.keywords.guess == "learned":
+            self.set_model(self.keywords.model)
         self.dims = []
         for k in range(len(arrs)):
             d = (ctypes.c_int32 * 4)()
@@ -229,6 +273,26 @@ class CoupledCluster:
         _check(library().hx_ccsd_solve_batch(self._h, st.ctypes.data_as(_c_i), it.ctypes.data_as(_c_i),
                                              e.ctypes.data_as(_c_d)))
         return {"status": st, "iterations": it, "energy": e}
+
+    def set_model(self, params=None):
+        """Install the learned-guess network (a float32 blob; None = the shipped model)."""
+        if params is None:
+            from .learned import default_model
+            params = default_model()
+        blob = np.ascontiguousarray(params, dtype=np.float32)
+        if blob.size != mlp_nparam():
+            raise ValueError(f"model blob has {blob.size} values, expected {mlp_nparam()}")
+        self._model = blob
+        _check(library().hx_ccsd_set_model(self._h, blob.ctypes.data_as(_c_f)))
+
+    def training_rows(self, mol: int, rows):
+        """Inputs X [n, 8] and targets t2 - guess [n] of canonical pairs `rows` of molecule mol."""
+        rows = np.ascontiguousarray(rows, dtype=np.int64)
+        X = np.zeros((rows.size, 8), dtype=np.float32)
+        T = np.zeros(rows.size, dtype=np.float32)
+        _check(library().hx_ccsd_training_rows(self._h, mol, rows.size, rows.ctypes.data_as(_c_l),
+                                               X.ctypes.data_as(_c_f), T.ctypes.data_as(_c_f)))
+        return X, T
 
     def set_guess(self, mol: int, t1, t2):
         t1 = np.asfortranarray(t1, dtype=np.float64)

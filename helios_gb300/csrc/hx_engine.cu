@@ -12,7 +12,11 @@
 
 #include "../../include/helios_cc.h"
 #include "hx_kernels.h"
+#include "hx_mlp.h"
 #include "hx_tc.h"
+
+cudaError_t hx_mlp_sample(const CCMol *d_mols, int mol, const long long *d_rows, int n, float *dX, float *dT,
+                          cudaStream_t s);
 
 // ---------------------------------------------------------------- errors
 static thread_local char g_err[1024];
@@ -195,6 +199,7 @@ struct hx_ccsd {
     std::vector<Rules> rules;
     std::vector<int> status;
     tc::Engine *tce = nullptr;           // tensor-core backend (mixed precision)
+    mlp::Model *model = nullptr;         // learned T2 guess (guess = 1)
     // mixed precision: per-molecule phase (PH_LOW / PH_HIGH tensor-core
     // iterations, PH_FP64 CUDA-core FP64) and the matching launch masks
     std::vector<int> phase, stall;
@@ -575,6 +580,27 @@ static int cc_setup(hx_ccsd *h, int guess)
     return HX_OK;
 }
 
+// Learned T2 guess: after the reference guess, t2 <- guess + network
+// prediction on every canonical pair of every molecule (inference on the
+// tensor cores, features from the device state).
+static int apply_learned_guess(hx_ccsd *h)
+{
+    if (!h->model) {
+        hx_set_error("guess = 1 (learned) but no model was given (hx_ccsd_set_model)");
+        return HX_ERR_STATE;
+    }
+    for (int mi = 0; mi < h->nmol; ++mi) {
+        const long long ov = (long long)h->o[mi] * h->v[mi];
+        HX_CU(h->model->apply(h->d_cc, mi, ov * (ov + 1) / 2, h->st));
+    }
+    HX_CU(cudaStreamSynchronize(h->st));
+    if (int w = h->model->error_word()) {
+        hx_set_error("learned guess: a tensor-core wait timed out (code %d)", w);
+        return HX_ERR_KERNEL;
+    }
+    return HX_OK;
+}
+
 int hx_ccsd_init(hx_ccsd *h)
 {
     if (!h) { hx_set_error("NULL handle"); return HX_ERR_ARG; }
@@ -606,6 +632,7 @@ int hx_ccsd_init(hx_ccsd *h)
     }
     HX_TRY(upload_views(h));
     HX_TRY(cc_setup(h, 1));
+    if (h->p.guess == 1) HX_TRY(apply_learned_guess(h));
     if (h->tce) tc::invalidate(h->tce);          // new orbitals: re-slice the constant operands
     for (int mi = 0; mi < h->nmol; ++mi) { h->rules[mi] = Rules(); h->status[mi] = 0; h->active[mi] = 1; }
     for (int mi = 0; mi < h->nmol; ++mi) HX_CU(cudaMemsetAsync(h->diis[mi].count, 0, sizeof(int), h->st));
@@ -900,11 +927,53 @@ void hx_ccsd_cancel(hx_ccsd *h)
     if (h) h->cancel.store(1);
 }
 
+int hx_ccsd_set_model(hx_ccsd *h, const float *params)
+{
+    if (!h) { hx_set_error("NULL handle"); return HX_ERR_ARG; }
+    if (!params) {
+        if (h->model) { h->model->release(); delete h->model; h->model = nullptr; }
+        return HX_OK;
+    }
+    if (!h->model) h->model = new mlp::Model();
+    return h->model->load(params);
+}
+
+int hx_ccsd_training_rows(hx_ccsd *h, int32_t mol, int32_t n, const int64_t *rows, float *X, float *T)
+{
+    if (!h || !h->initialized || mol < 0 || mol >= h->nmol || n <= 0 || !rows || !X || !T) {
+        hx_set_error("hx_ccsd_training_rows: bad arguments or state");
+        return HX_ERR_ARG;
+    }
+    const long long ov = (long long)h->o[mol] * h->v[mol], npairs = ov * (ov + 1) / 2;
+    for (int k = 0; k < n; ++k)
+        if (rows[k] < 0 || rows[k] >= npairs) { hx_set_error("hx_ccsd_training_rows: row %d out of range", k); return HX_ERR_ARG; }
+    long long *dr = nullptr;
+    float *dX = nullptr, *dT = nullptr;
+    int rc = HX_OK;
+    if (cudaMalloc(&dr, sizeof(long long) * n) != cudaSuccess || cudaMalloc(&dX, sizeof(float) * 8 * n) != cudaSuccess ||
+        cudaMalloc(&dT, sizeof(float) * n) != cudaSuccess) {
+        hx_set_error("hx_ccsd_training_rows: allocation failed");
+        rc = HX_ERR_NOMEM;
+    }
+    cudaError_t e = cudaSuccess;
+    if (rc == HX_OK) e = cudaMemcpyAsync(dr, rows, sizeof(long long) * n, cudaMemcpyHostToDevice, h->st);
+    if (rc == HX_OK && e == cudaSuccess) e = hx_mlp_sample(h->d_cc, mol, dr, n, dX, dT, h->st);
+    if (rc == HX_OK && e == cudaSuccess) e = cudaMemcpyAsync(X, dX, sizeof(float) * 8 * n, cudaMemcpyDeviceToHost, h->st);
+    if (rc == HX_OK && e == cudaSuccess) e = cudaMemcpyAsync(T, dT, sizeof(float) * n, cudaMemcpyDeviceToHost, h->st);
+    if (rc == HX_OK && e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    if (rc == HX_OK && e != cudaSuccess) { hx_set_error("hx_ccsd_training_rows: %s", cudaGetErrorString(e)); rc = HX_ERR_CUDA; }
+    cudaFree(dr);
+    cudaFree(dX);
+    cudaFree(dT);
+    return rc;
+}
+
 void hx_ccsd_destroy(hx_ccsd *h)
 {
     if (!h) return;
     if (h->st) cudaStreamSynchronize(h->st);
     if (h->tce) tc::destroy(h->tce);
+    if (h->model) { h->model->release(); delete h->model; }
     for (int k = 0; k < 4; ++k) if (h->ev[k]) cudaEventDestroy(h->ev[k]);
     for (auto &g : h->plan) if (g.d) cudaFree(g.d);
     cudaFree(h->arena);

@@ -3,33 +3,38 @@
 // FP64 operands are turned into integer slices (an error-free splitting in
 // the spirit of the Ozaki scheme): row r of A is scaled by 2^-e_r so that its
 // largest entry is below 1, then a = 2^-7 (s0 + 2^-8 s1 + 2^-16 s2 + ...)
-// with S = 3 integer slices |s_k| <= 128, each exactly representable in bf16
-// (the representation error is below 2^-24 of the row maximum). The product
-// keeps every slice pair (i, j) with i + j <= 3 (eight of the nine; the one
-// dropped weighs 2^-32). Products of such slices are integers below 2^14, so a
-// tensor-core accumulation of a few hundred of them is exact in FP32 (checked
-// on the hardware: integer inputs give bit-exact sums, while general bf16
-// inputs lose low bits as K grows). Pairs of equal weight 2^-8q (q = i + j)
-// share one TMEM accumulator; every 256-deep K chunk the four accumulators
-// are combined and added into an FP32 (hi, lo) pair per output by TwoSum, so
-// the result carries about FP32 accuracy relative to the operands' row maxima
-// without the tensor core's accumulation error. (A drain in FP64 would be
-// exact too, but at GB300's FP64 rate it costs more than the MMAs.)
+// with S integer digits |s_p| <= 128 (hx_slice.h), stored as s_p 2^-8p, each
+// exactly representable in bf16 (the representation error is below 2^-8S+1
+// of the row maximum). The product keeps the slice pairs (i, j) with
+// i + j <= QMAX. Products of such slices are integers times 2^-8(i+j) with
+// at most 15 significant bits, so a tensor-core accumulation of a few hundred
+// of them with equal weight is exact in FP32 (checked on the hardware:
+// integer inputs give bit-exact sums, while general bf16 inputs lose low bits
+// as K grows). The leading weights (q = i + j < NX) therefore get one exact
+// TMEM accumulator each; the rest share one accumulator whose rounding is
+// scaled down by 2^-8NX. Every chunk of KC k-blocks the accumulators are
+// summed by TwoSum and added into an FP32 (hi, lo) pair per output, so the
+// result carries the accuracy of the splitting relative to the operands' row
+// maxima without the tensor core's accumulation error. (A drain in FP64 would
+// be exact too, but at GB300's FP64 rate it costs more than the MMAs.)
 //
 // Per group of TgemmDesc problems:
 //   1. row_scale: per row of A and B (through the descriptor's strides) the
-//      binary exponent of the largest |entry|.
-//   2. split_gather: scaled integer slices, K-major, zero-padded:
-//      [slice][batch][rows][Kp] (rows to 128 for A, 64 for B; Kp to 64).
-//   3. tc_gemm: one CTA per 128x64 output tile (or per K slice of it).
-//      Warp 8 streams 64-deep k-blocks of all slices with TMA
-//      (cp.async.bulk.tensor, 128-byte swizzle) through a 3-stage ring; one
-//      thread of warp 9 issues tcgen05.mma (kind::f16, BF16 x BF16 -> FP32,
-//      M=128, N=64, K=16) into four class accumulators of 64 columns,
-//      alternating between two TMEM buffers per chunk; warps 0-7 drain a
-//      finished buffer with tcgen05.ld (a TMEM lane is an output row; two
-//      warps share a lane quarter and split its columns) while the next chunk
-//      runs, then write C = alpha*2^(e_m+f_n-14)*(hi+lo) + beta*C in FP64.
+//      binary exponent of the largest |entry|, over 32 x 64 tiles staged in
+//      shared memory (coalesced along the source's contiguous dimension).
+//   2. split_gather: the slices, K-major, zero-padded, from the same tiles:
+//      [slice][batch][rows][Kp] (rows to 128 for A, to the tile width for B;
+//      Kp to 64). Integer arithmetic only.
+//   3. tc_gemm: one CTA per 128 x BN output tile (or per K slice of it).
+//      A producer warp streams 64-deep k-blocks of all slices with TMA
+//      (cp.async.bulk.tensor, 128-byte swizzle) through a ring of stages; one
+//      thread of the MMA warp issues tcgen05.mma (kind::f16, BF16 x BF16 ->
+//      FP32, M = 128, N = BN, K = 16) into the class accumulators, alternating
+//      between two TMEM buffers per chunk; the epilogue warps drain a finished
+//      buffer with tcgen05.ld (a TMEM lane is an output row; the warps of a
+//      lane quarter split its columns) while the next chunk runs, then stage
+//      the tile in the idle ring and write C = alpha*2^(e_m+f_n-14)*(hi+lo) +
+//      beta*C in FP64 with consecutive threads on consecutive columns.
 //   Every mbarrier wait is bounded by wall time; a wait that runs out records
 //   a code in a device error word and the CTA still frees its TMEM.
 #include <cuda.h>
@@ -37,44 +42,61 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <climits>
 #include <cstring>
 #include <mutex>
 #include <vector>
 
 #include "hx_common.cuh"
 #include "hx_kernels.h"
+#include "hx_slice.h"
 #include "hx_tc.h"
 
 namespace tc {
 
-// Two precisions of the same kernel. LOW: 3 slices, pairs i + j <= 3 (8 MMAs
-// per k-step), about 2^-24 of the row maxima. HIGH: 5 slices, pairs
-// i + j <= 5 (19 MMAs), about 2^-44: residuals as accurate as FP64 ones.
-template <int S_, int QMAX_, int BN_, int STAGES_, int KC_>
+// Two precisions of the same kernel. Slice p of an operand is stored as
+// s_p 2^-8p (exact in bf16), so the product of slices i and j weighs
+// 2^-8(i+j) by itself and a class accumulator needs no further weight.
+// Classes q = i + j < NX are kept exact (their partial sums are integers
+// times 2^-8q below 2^24 per chunk); all products with q >= NX share one
+// more accumulator, whose FP32 accumulation error (about K * 2^-32 relative
+// for a chunk of depth K) is scaled down by 2^-8NX.
+//   LOW:  3 slices, pairs i + j <= 3 (8 MMAs per k-step), NX = 1: about 2^-24
+//         of the row maxima; 128 x 96 tiles.
+//   HIGH: 5 slices, pairs i + j <= 5 (19 MMAs), NX = 3: about 2^-40; residuals
+//         as accurate as FP64 ones; 128 x 32 tiles.
+template <int S_, int QMAX_, int NX_, int BN_, int STAGES_, int KC_, int EPIW_>
 struct Cfg {
     static constexpr int S = S_;                     // integer slices per FP64 operand
     static constexpr int QMAX = QMAX_;               // slice pairs with i + j <= QMAX are multiplied
-    static constexpr int NQ = QMAX_ + 1;             // accumulator classes q = i + j
+    static constexpr int NX = NX_;                   // exact classes q = 0 .. NX-1
+    static constexpr int NQ = QMAX_ >= NX_ ? NX_ + 1 : QMAX_ + 1;   // TMEM accumulators per buffer
     static constexpr int BM = 128, BN = BN_, BK = 64;
-    static constexpr int KC = KC_;                   // k-blocks per exact chunk
+    static constexpr int KC = KC_;                   // k-blocks per chunk (exact classes stay exact)
     static constexpr int STAGES = STAGES_;
+    static constexpr int EPI_WARPS = EPIW_;          // epilogue warps (a multiple of 4)
+    static constexpr int NTHREADS = (EPIW_ + 2) * 32; // + TMA producer warp + MMA warp
+    static constexpr int EPI_THREADS = EPIW_ * 32;
     static constexpr int ATILE = BM * BK * 2;        // bytes per A slice tile
     static constexpr int BTILE = BN * BK * 2;        // bytes per B slice tile
     static constexpr int STAGE_BYTES = S * (ATILE + BTILE);
     static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
-    static constexpr int EPI_COLS = BN / 2;          // columns drained per epilogue thread
+    static constexpr int EPI_COLS = BN / (EPIW_ / 4); // columns drained per epilogue thread
     static constexpr int PRODUCTS = [] { int n = 0; for (int i = 0; i < S_; ++i) for (int j = 0; j < S_; ++j) n += (i + j <= QMAX_); return n; }();
-    // exactness of a chunk: (pairs per class) * KC*64 * 2^14 < 2^24
-    static_assert(KC_ * 64 * 16384LL * (QMAX_ + 1 < S_ ? QMAX_ + 1 : S_) < (1LL << 24), "chunk too deep for exact sums");
+    __host__ __device__ static constexpr int cls(int q) { return q < NX_ ? q : NX_; }
+    // pairs in the largest exact class
+    static constexpr int XPAIRS = [] { int m = 0; for (int q = 0; q < NX_; ++q) { int n = 0; for (int i = 0; i < S_; ++i) n += (q - i >= 0 && q - i < S_); m = n > m ? n : m; } return m; }();
+    // exactness of a chunk: (pairs per exact class) * KC*64 * 2^14 < 2^24
+    static_assert((long long)XPAIRS * KC_ * 64 * 16384LL < (1LL << 24), "chunk too deep for exact sums");
     static_assert(2 * NQ * BN_ <= 512, "two TMEM buffers must fit in 512 columns");
     static_assert(STAGES_ * S_ * (128 * 64 * 2 + BN_ * 64 * 2) + 1280 <= 232448, "shared memory");
+    static_assert(EPIW_ % 4 == 0 && EPI_COLS % 8 == 0, "epilogue split");
+    static_assert(128 * (BN_ + 1) * 8 <= STAGES_ * STAGE_BYTES, "output tile staging fits in the TMA ring");
 };
-using Low = Cfg<3, 3, 64, 3, 4>;
-using High = Cfg<5, 5, 32, 2, 3>;
-constexpr int NTHREADS = 320;                       // 8 epilogue warps, producer, MMA issuer
-constexpr int EPI_THREADS = 256;
+using Low = Cfg<3, 3, 1, 96, 2, 8, 12>;
+using High = Cfg<5, 5, 3, 32, 2, 3, 8>;
 constexpr int TMEM_COLS = 512;
-constexpr int BM = 128, BK = 64, SMAX = 5;
+constexpr int BM = 128, BK = 64;
 constexpr unsigned long long WAIT_NS = 4000000000ull; // a wait longer than 4 s is declared failed
 
 struct TcDesc {
@@ -188,99 +210,170 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v)
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v)
+{
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 __device__ __forceinline__ long long split_off(int x, int xi, long long s0, long long s1)
 {
     return (long long)(x / xi) * s0 + (long long)(x % xi) * s1;
 }
 
 // ------------------------------------------------------------------ split + gather
+// Both kernels walk the operand in tiles of PT_R rows x PT_K k staged in
+// shared memory: the global reads run along whichever of the two dimensions
+// is contiguous in the FP64 source (rfast), the slice writes along k, so
+// transposed operands are read as coalesced as plain ones.
+constexpr int PT_R = 32, PT_K = 64, PT_THREADS = 256;
+
 struct PrepDesc {
     const double *src;
     __nv_bfloat16 *dst;              // [S][batch][Rp][Kp]
     int *rexp;                       // [batch][Rp] binary exponent of each row's largest entry
     int batch, R, K, Rp, Kp, Ri, Ki;
     long long s[5];                  // r0, r1, k0, k1, batch strides of the FP64 source
-    long long work_start;            // prefix of batch*Rp*(Kp/8) over the launch
+    long long work_start;            // prefix of tiles (batch * Rp/PT_R * Kp/PT_K) over the launch
     long long row_start;             // prefix of batch*Rp over the launch
     int mol;
+    int rfast;                       // rows (1) or k (0) are the contiguous dimension of the source
 };
 
-__device__ __forceinline__ int find_desc(const PrepDesc *pd, int n, long long w, bool rows)
+__device__ __forceinline__ int find_desc(const PrepDesc *pd, int n, long long w)
 {
     int lo = 0, hi = n - 1;
     while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;
-        if ((rows ? pd[mid].row_start : pd[mid].work_start) <= w) lo = mid; else hi = mid - 1;
+        if (pd[mid].work_start <= w) lo = mid; else hi = mid - 1;
     }
     return lo;
 }
 
-// One warp per row: e with max|x| < 2^e (0 for an all-zero row).
-__global__ void __launch_bounds__(256) row_scale(const PrepDesc *__restrict__ pd, int n, long long rows,
-                                                 const int *__restrict__ active)
+struct PrepTile {
+    double x[PT_R][PT_K + 1];
+    long long roff[PT_R], koff[PT_K];
+    int desc;
+};
+
+// Stage tile `u` of the launch in shared memory (zero outside R x K); returns
+// false (uniformly) when its molecule is inactive.
+__device__ __forceinline__ bool load_tile(const PrepDesc *__restrict__ pd, int n, long long u, const int *active,
+                                          PrepTile &t, int &b, int &r0, int &k0)
 {
-    const int lane = threadIdx.x & 31;
-    for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < rows;
-         w += ((long long)gridDim.x * blockDim.x) >> 5) {
-        const PrepDesc &d = pd[find_desc(pd, n, w, true)];
+    if (threadIdx.x == 0) t.desc = find_desc(pd, n, u);
+    __syncthreads();
+    const PrepDesc &d = pd[t.desc];
+    if (active && !active[d.mol]) return false;
+    long long local = u - d.work_start;
+    const int tk = d.Kp / PT_K, tr = d.Rp / PT_R;
+    k0 = (int)(local % tk) * PT_K;
+    local /= tk;
+    r0 = (int)(local % tr) * PT_R;
+    b = (int)(local / tr);
+    for (int e = threadIdx.x; e < PT_R + PT_K; e += PT_THREADS) {
+        if (e < PT_R) t.roff[e] = split_off(r0 + e, d.Ri, d.s[0], d.s[1]) + (long long)b * d.s[4];
+        else t.koff[e - PT_R] = split_off(k0 + e - PT_R, d.Ki, d.s[2], d.s[3]);
+    }
+    __syncthreads();
+    const int rlim = d.R - r0, klim = d.K - k0;
+    for (int e = threadIdx.x; e < PT_R * PT_K; e += PT_THREADS) {
+        int rr, kk;
+        if (d.rfast) { rr = e % PT_R; kk = e / PT_R; } else { kk = e % PT_K; rr = e / PT_K; }
+        t.x[rr][kk] = (rr < rlim && kk < klim) ? __ldg(d.src + t.roff[rr] + t.koff[kk]) : 0.0;
+    }
+    __syncthreads();
+    return true;
+}
+
+// Every row exponent of the launch's operands starts at INT_MIN.
+__global__ void rexp_init(const PrepDesc *__restrict__ pd, int n, long long rows, const int *__restrict__ active)
+{
+    for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < rows; w += (long long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = n - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (pd[mid].row_start <= w) lo = mid; else hi = mid - 1;
+        }
+        const PrepDesc &d = pd[lo];
         if (active && !active[d.mol]) continue;
-        const long long local = w - d.row_start;
-        const int r = (int)(local % d.Rp), b = (int)(local / d.Rp);
-        double mx = 0.0;
-        if (r < d.R) {
-            const long long base = split_off(r, d.Ri, d.s[0], d.s[1]) + (long long)b * d.s[4];
-            for (int k = lane; k < d.K; k += 32) mx = fmax(mx, fabs(d.src[base + split_off(k, d.Ki, d.s[2], d.s[3])]));
-        }
-        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        if (lane == 0) {
-            int e = 0;
-            if (mx > 0.0) frexp(mx, &e);      // mx = f 2^e with f in [0.5, 1)
-            d.rexp[local] = e;
-        }
+        d.rexp[w - d.row_start] = INT_MIN;
     }
 }
 
-template <int S>
-__global__ void __launch_bounds__(256) split_gather(const PrepDesc *__restrict__ pd, int n, long long total,
-                                                    const int *__restrict__ active)
+// Row exponents: e with max|row| < 2^e (frexp), combined over the k tiles of a row by
+// atomicMax (the list's exponents start at INT_MIN; a row that stays there is
+// all zero and is treated as e = 0).
+__global__ void __launch_bounds__(PT_THREADS) row_scale(const PrepDesc *__restrict__ pd, int n, long long units,
+                                                        const int *__restrict__ active)
 {
-    for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < total;
-         w += (long long)gridDim.x * blockDim.x) {
-        const PrepDesc &d = pd[find_desc(pd, n, w, false)];
-        if (active && !active[d.mol]) continue;
-        long long local = w - d.work_start;
-        const int kc = d.Kp / 8;
-        const int k8 = (int)(local % kc) * 8;
-        long long rr = local / kc;
-        const int r = (int)(rr % d.Rp);
-        const int b = (int)(rr / d.Rp);
-        const int e = d.rexp[(long long)b * d.Rp + r];
-        __align__(16) __nv_bfloat16 out[S][8];
+    __shared__ PrepTile t;
+    const int rr = threadIdx.x >> 3, part = threadIdx.x & 7;
+    for (long long u = blockIdx.x; u < units; u += gridDim.x) {
+        int b, r0, k0;
+        if (load_tile(pd, n, u, active, t, b, r0, k0)) {
+            const PrepDesc &d = pd[t.desc];
+            // magnitudes compare as their bit patterns with the sign cleared
+            unsigned long long mb = 0;
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            int k = k8 + q;
-            double x = 0.0;
-            if (r < d.R && k < d.K)
-                x = d.src[split_off(r, d.Ri, d.s[0], d.s[1]) + split_off(k, d.Ki, d.s[2], d.s[3]) + (long long)b * d.s[4]];
-            double a = ldexp(x, 7 - e);       // |a| < 128
-#pragma unroll
-            for (int p = 0; p < S; ++p) {
-                double sl = rint(a);          // integer slice, |sl| <= 128
-                out[p][q] = __float2bfloat16_rn((float)sl);
-                a = (a - sl) * 256.0;
+            for (int kk = part; kk < PT_K; kk += 8) {
+                const unsigned long long v = dbits(t.x[rr][kk]) & 0x7FFFFFFFFFFFFFFFull;
+                mb = v > mb ? v : mb;
             }
-        }
-        const long long plane = (long long)d.batch * d.Rp * d.Kp;
-        const long long off = ((long long)b * d.Rp + r) * d.Kp + k8;
 #pragma unroll
-        for (int p = 0; p < S; ++p)
-            *reinterpret_cast<uint4 *>(d.dst + p * plane + off) = *reinterpret_cast<const uint4 *>(out[p]);
+            for (int o = 1; o < 8; o <<= 1) {
+                const unsigned long long v = __shfl_xor_sync(0xffffffffu, mb, o);
+                mb = v > mb ? v : mb;
+            }
+            if (part == 0 && mb != 0 && r0 + rr < d.R)
+                atomicMax(&d.rexp[(long long)b * d.Rp + r0 + rr], exp_of_bits(mb));
+        }
+        __syncthreads();
+    }
+}
+
+// Slices of each tile, K-major: the digits of x 2^(7-e) (slice_digits),
+// stored as s_p 2^-8p (exact in bf16); thread = (row, 8-wide k chunk), one
+// 16-byte store per slice.
+template <int S>
+__global__ void __launch_bounds__(PT_THREADS) split_gather(const PrepDesc *__restrict__ pd, int n, long long units,
+                                                           const int *__restrict__ active)
+{
+    __shared__ PrepTile t;
+    const int rr = threadIdx.x >> 3, c8 = (threadIdx.x & 7) * 8;
+    for (long long u = blockIdx.x; u < units; u += gridDim.x) {
+        int b, r0, k0;
+        if (load_tile(pd, n, u, active, t, b, r0, k0)) {
+            const PrepDesc &d = pd[t.desc];
+            int e = d.rexp[(long long)b * d.Rp + r0 + rr];
+            if (e == INT_MIN) e = 0;
+            __align__(16) __nv_bfloat16 out[S][8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                int dg[S];
+                slice_digits<S>(t.x[rr][c8 + q], e, dg);
+#pragma unroll
+                for (int p = 0; p < S; ++p)                     // s_p 2^-8p, exact in bf16
+                    out[p][q] = __float2bfloat16_rn((float)dg[p] * (p == 0 ? 1.f : __int_as_float((127 - 8 * p) << 23)));
+            }
+            const long long plane = (long long)d.batch * d.Rp * d.Kp;
+            const long long off = ((long long)b * d.Rp + r0 + rr) * d.Kp + k0 + c8;
+#pragma unroll
+            for (int p = 0; p < S; ++p)
+                *reinterpret_cast<uint4 *>(d.dst + p * plane + off) = *reinterpret_cast<const uint4 *>(out[p]);
+        }
+        __syncthreads();
     }
 }
 
 // ------------------------------------------------------------------ the GEMM
 template <class C>
-__global__ void __launch_bounds__(NTHREADS, 1) tc_gemm(const TcDesc *__restrict__ descs, int ndesc,
+__global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restrict__ descs, int ndesc,
                                                         const int *__restrict__ active, int *err)
 {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -324,10 +417,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gemm(const TcDesc *__restrict_
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < C::STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
-        for (int b = 0; b < 2; ++b) { mbar_init(&acc_full[b], 1); mbar_init(&acc_empty[b], EPI_THREADS); }
+        for (int b = 0; b < 2; ++b) { mbar_init(&acc_full[b], 1); mbar_init(&acc_empty[b], C::EPI_THREADS); }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 9) {
+    constexpr int WP = C::EPI_WARPS, WM = C::EPI_WARPS + 1;   // producer and MMA warps
+    if (warp == WM) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                      "r"(TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
@@ -338,7 +432,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gemm(const TcDesc *__restrict_
     const uint32_t tmem = *tmem_slot;
     bool ok = true;
 
-    if (warp == 8) {
+    if (warp == WP) {
         if (lane == 0) {
             const int arow0 = bt * d.Mp + tm * BM, brow0 = bt * d.Np + tn * C::BN;
             const int aplane = d.batch * d.Mp, bplane = d.batch * d.Np;
@@ -356,7 +450,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gemm(const TcDesc *__restrict_
                 }
             }
         }
-    } else if (warp == 9) {
+    } else if (warp == WM) {
         if (lane == 0) {
             const uint32_t idesc = idesc_bf16(BM, C::BN);
             for (int c = 0; c < nchunk && ok; ++c) {
@@ -375,7 +469,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gemm(const TcDesc *__restrict_
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                     const uint32_t sa = smem_u32(smem + st * C::STAGE_BYTES);
                     const uint32_t sb = sa + C::S * C::ATILE;
-#pragma unroll
+                    const bool chunk_start = kb == c * C::KC;
+#pragma unroll 1
                     for (int kk = 0; kk < BK / 16; ++kk) {
 #pragma unroll
                         for (int i = 0; i < C::S; ++i) {
@@ -383,11 +478,17 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gemm(const TcDesc *__restrict_
                             for (int j = 0; j < C::S; ++j) {
                                 const int q = i + j;
                                 if (q > C::QMAX) continue;
+                                const int cl = C::cls(q);
+                                // the first product of a class in the chunk overwrites its
+                                // accumulator: issue order is kk, i, j, so that is the pair
+                                // with the smallest i of the class at kk = 0
+                                const int i_first = cl < C::NX ? (cl < C::S ? 0 : cl - (C::S - 1))
+                                                               : (C::NX < C::S ? 0 : C::NX - (C::S - 1));
+                                const bool first = chunk_start && kk == 0 && i == i_first &&
+                                                   (cl < C::NX || j == C::NX - i_first);
                                 const uint64_t ad = sw128_desc(sa + i * C::ATILE + kk * 32);
                                 const uint64_t bd = sw128_desc(sb + j * C::BTILE + kk * 32);
-                                // the first product of a class in the chunk overwrites its accumulator
-                                const bool first = (kb == c * C::KC) && kk == 0 && i == (q < C::S ? 0 : q - (C::S - 1));
-                                mma_bf16(dbase + q * C::BN, ad, bd, idesc, first ? 0u : 1u);
+                                mma_bf16(dbase + cl * C::BN, ad, bd, idesc, first ? 0u : 1u);
                             }
                         }
                     }
@@ -397,8 +498,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gemm(const TcDesc *__restrict_
             }
         }
     } else {
-        // epilogue: warps 0-7; warp w drains TMEM lanes 32*(w%4).. (output rows) and
-        // the column half w/4 of the tile
+        // epilogue: warps 0 .. EPI_WARPS-1; warp w drains TMEM lanes 32*(w%4)..
+        // (output rows) and the column block w/4 of the tile
         const int row = (warp & 3) * 32 + lane;
         const int col0 = (warp >> 2) * C::EPI_COLS;
         const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
@@ -411,64 +512,55 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gemm(const TcDesc *__restrict_
             if (ok) ok = mbar_wait(&acc_full[buf], use & 1, err, 3);
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
-            for (int c0 = 0; c0 < C::EPI_COLS; c0 += 16) {
-                // chunk value: exact integer classes combined with weights 2^-8q
-                float x[16], t[16], xl[16];
-                tmem_ld16(tmem + lane_base + (uint32_t)(buf * C::NQ * C::BN + (C::NQ - 1) * C::BN + col0 + c0), x);
+            for (int c0 = 0; c0 < C::EPI_COLS; c0 += 8) {
+                // chunk value of 8 columns: the classes (exact ones first) summed
+                // by TwoSum, then added into (hi, lo); rounding errors go to lo
+                float a[C::NQ][8];
 #pragma unroll
-                for (int e = 0; e < 16; ++e) xl[e] = 0.f;
+                for (int q = 0; q < C::NQ; ++q)
+                    tmem_ld8(tmem + lane_base + (uint32_t)(buf * C::NQ * C::BN + q * C::BN + col0 + c0), a[q]);
 #pragma unroll
-                for (int q = C::NQ - 2; q >= 0; --q) {
-                    tmem_ld16(tmem + lane_base + (uint32_t)(buf * C::NQ * C::BN + q * C::BN + col0 + c0), t);
-                    if constexpr (C::S > 3) {
-                        // float-float Horner step: (x, xl) = (x, xl) * 2^-8 + t, error of
-                        // the sum kept by TwoSum (the scaling is exact)
+                for (int e = 0; e < 8; ++e) {
+                    float x = a[0][e], err = 0.f;
 #pragma unroll
-                        for (int e = 0; e < 16; ++e) {
-                            const float a = x[e] * 0.00390625f;
-                            const float s = a + t[e];
-                            const float bb = s - a;
-                            xl[e] = fmaf(xl[e], 0.00390625f, (a - (s - bb)) + (t[e] - bb));
-                            x[e] = s;
-                        }
-                    } else {
-#pragma unroll
-                        for (int e = 0; e < 16; ++e) x[e] = fmaf(x[e], 0.00390625f, t[e]);
+                    for (int q = 1; q < C::NQ; ++q) {
+                        const float sq = x + a[q][e];
+                        const float bq = sq - x;
+                        err += (x - (sq - bq)) + (a[q][e] - bq);
+                        x = sq;
                     }
-                }
-#pragma unroll
-                for (int e = 0; e < 16; ++e) {
-                    // TwoSum of the chunk value into (hi, lo)
-                    const float s = hi[c0 + e] + x[e];
-                    const float bb = s - hi[c0 + e];
-                    lo[c0 + e] += ((hi[c0 + e] - (s - bb)) + (x[e] - bb)) + xl[e];
-                    hi[c0 + e] = s;
+                    const float sh = hi[c0 + e] + x;
+                    const float bh = sh - hi[c0 + e];
+                    lo[c0 + e] += ((hi[c0 + e] - (sh - bh)) + (x - bh)) + err;
+                    hi[c0 + e] = sh;
                 }
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             mbar_arrive(&acc_empty[buf]);
         }
-        const int m = tm * BM + row;
-        if (ok && m < d.M) {
-            double *C = d.C + (long long)bt * d.c[4];
-            const long long offm = split_off(m, d.Mi, d.c[0], d.c[1]);
-            const int ea = d.expA[(long long)bt * d.Mp + m];
+        // every chunk is drained, so the TMA ring is idle: stage the tile in its
+        // shared memory and write C with consecutive threads on consecutive n
+        constexpr int LD = C::BN + 1;
+        double *stile = (double *)smem;                      // [BM][BN + 1]
 #pragma unroll
-            for (int e = 0; e < C::EPI_COLS; ++e) {
-                const int n = tn * C::BN + col0 + e;
-                if (n >= d.N) continue;
-                const int eb = d.expB[(long long)bt * d.Np + n];
-                double *p = C + offm + split_off(n, d.Ni, d.c[2], d.c[3]);
-                double r = d.alpha * ldexp((double)hi[e] + (double)lo[e], ea + eb - 14);
-                if (d.ksplit > 1) { atomicAdd(p, r); continue; }
-                if (d.beta != 0.0) r += d.beta * *p;
-                *p = r;
-            }
+        for (int e = 0; e < C::EPI_COLS; ++e) stile[row * LD + col0 + e] = (double)hi[e] + (double)lo[e];
+        asm volatile("bar.sync 1, %0;" ::"r"(C::EPI_THREADS) : "memory");
+        double *Cp = d.C + (long long)bt * d.c[4];
+        for (int idx = threadIdx.x; idx < BM * C::BN && ok; idx += C::EPI_THREADS) {
+            const int mm = idx / C::BN, nn = idx - mm * C::BN;
+            const int m = tm * BM + mm, n = tn * C::BN + nn;
+            if (m >= d.M || n >= d.N) continue;
+            const int ea = d.expA[(long long)bt * d.Mp + m], eb = d.expB[(long long)bt * d.Np + n];
+            double *p = Cp + split_off(m, d.Mi, d.c[0], d.c[1]) + split_off(n, d.Ni, d.c[2], d.c[3]);
+            double r = d.alpha * ldexp(stile[mm * LD + nn], ea + eb - 14);
+            if (d.ksplit > 1) { atomicAdd(p, r); continue; }
+            if (d.beta != 0.0) r += d.beta * *p;
+            *p = r;
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (warp == 9) {
+    if (warp == WM) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
     }
 }
@@ -567,6 +659,30 @@ static int make_map(CUtensorMap *map, void *base, long long rows, int kp, int bo
 
 static inline long long rup(long long x, long long m) { return (x + m - 1) / m * m; }
 
+// Which dimension of a source is contiguous: the one whose consecutive
+// elements are closer in memory.
+static int prep_rfast(const PrepDesc &p)
+{
+    const long long rs = p.Ri > 1 ? p.s[1] : p.s[0], ks = p.Ki > 1 ? p.s[3] : p.s[2];
+    return std::llabs(rs) < std::llabs(ks) ? 1 : 0;
+}
+
+// Row exponents then slices of one list of operands (n descriptors, `tiles`
+// PT_R x PT_K tiles, `rows` padded rows).
+static cudaError_t prep_launch(const PrepDesc *d, int n, long long tiles, long long rows, int S, const int *active,
+                               cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    const unsigned rb = (unsigned)std::min<long long>((rows + 255) / 256, 1 << 14);
+    const unsigned tb = (unsigned)std::min<long long>(tiles, 1 << 16);
+    rexp_init<<<rb, 256, 0, s>>>(d, n, rows, active);
+    row_scale<<<tb, PT_THREADS, 0, s>>>(d, n, tiles, active);
+    if (S == Low::S) split_gather<Low::S><<<tb, PT_THREADS, 0, s>>>(d, n, tiles, active);
+    else split_gather<High::S><<<tb, PT_THREADS, 0, s>>>(d, n, tiles, active);
+    hx_count_launches(3);
+    return cudaGetLastError();
+}
+
 // Problems below this many multiply-adds stay on the FP64 CUDA-core kernel.
 static const double kMinTcWork = 4.0e6;
 
@@ -640,7 +756,8 @@ static int build_mode(Engine *e, Mode &md, const std::vector<Group> &plan, size_
             auto add = [&](PrepList &L, PrepDesc p) {
                 p.work_start = L.work;
                 p.row_start = L.rows;
-                L.work += (long long)p.batch * p.Rp * (p.Kp / 8);
+                p.rfast = prep_rfast(p);
+                L.work += (long long)p.batch * (p.Rp / PT_R) * (p.Kp / PT_K);
                 L.rows += (long long)p.batch * p.Rp;
                 L.h.push_back(p);
             };
@@ -734,24 +851,15 @@ cudaError_t run_group(Engine *e, const TgemmDesc *descs, int n, const int *d_act
     }
     if (sg.tiles == 0) return cudaSuccess;
     cudaError_t r = cudaSuccess;
-    auto prep = [&](PrepList &L) -> cudaError_t {
-        if (L.h.empty()) return cudaSuccess;
-        long long rblocks = std::min<long long>((L.rows * 32 + 255) / 256, 1 << 16);
-        row_scale<<<(unsigned)rblocks, 256, 0, s>>>(L.d, (int)L.h.size(), L.rows, d_active);
-        cudaError_t x = cudaGetLastError();
-        if (x != cudaSuccess) return x;
-        long long blocks = std::min<long long>((L.work + 255) / 256, 1 << 16);
-        if (md.S == Low::S) split_gather<Low::S><<<(unsigned)blocks, 256, 0, s>>>(L.d, (int)L.h.size(), L.work, d_active);
-        else split_gather<High::S><<<(unsigned)blocks, 256, 0, s>>>(L.d, (int)L.h.size(), L.work, d_active);
-        hx_count_launches(2);
-        return cudaGetLastError();
-    };
-    // constant slices of this mode are made once per initialisation
+    // constant slices of this mode are made once per initialisation, for every
+    // molecule (molecules enter a mode at different iterations)
     if (sg.fixed_gen != e->generation) {
-        if ((r = prep(sg.fixed)) != cudaSuccess) return r;
+        if ((r = prep_launch(sg.fixed.d, (int)sg.fixed.h.size(), sg.fixed.work, sg.fixed.rows, md.S, nullptr, s)) != cudaSuccess)
+            return r;
         sg.fixed_gen = e->generation;
     }
-    if ((r = prep(sg.var)) != cudaSuccess) return r;
+    if ((r = prep_launch(sg.var.d, (int)sg.var.h.size(), sg.var.work, sg.var.rows, md.S, d_active, s)) != cudaSuccess)
+        return r;
     hx_count_launches(1);
     Engine::Pending pend{};
     if (e->profile) {
@@ -763,8 +871,8 @@ cudaError_t run_group(Engine *e, const TgemmDesc *descs, int n, const int *d_act
         }
         cudaEventRecord(pend.a, s);
     }
-    if (mode == 0) tc_gemm<Low><<<(unsigned)sg.tiles, NTHREADS, Low::SMEM_BYTES, s>>>(sg.d_tcd, (int)sg.tcd.size(), d_active, e->d_err);
-    else tc_gemm<High><<<(unsigned)sg.tiles, NTHREADS, High::SMEM_BYTES, s>>>(sg.d_tcd, (int)sg.tcd.size(), d_active, e->d_err);
+    if (mode == 0) tc_gemm<Low><<<(unsigned)sg.tiles, Low::NTHREADS, Low::SMEM_BYTES, s>>>(sg.d_tcd, (int)sg.tcd.size(), d_active, e->d_err);
+    else tc_gemm<High><<<(unsigned)sg.tiles, High::NTHREADS, High::SMEM_BYTES, s>>>(sg.d_tcd, (int)sg.tcd.size(), d_active, e->d_err);
     r = cudaGetLastError();
     if (e->profile) {
         cudaEventRecord(pend.b, s);
@@ -813,11 +921,18 @@ namespace {
 
 constexpr size_t na_rup(size_t x, size_t m) { return (x + m - 1) / m * m; }
 constexpr int NA_DIM = HX_NOALLOC_MAX_DIM;
-constexpr size_t NA_SLICE_BYTES = (size_t)SMAX * NA_DIM * NA_DIM * sizeof(__nv_bfloat16);   // one operand
+constexpr int na_max(int a, int b) { return a > b ? a : b; }
+// padded rows of A (to 128) and of B (to either mode's tile width), padded K
+constexpr int NA_AROWS = (int)na_rup(NA_DIM, BM);
+constexpr int NA_BROWS = na_max((int)na_rup(NA_DIM, Low::BN), (int)na_rup(NA_DIM, High::BN));
+constexpr int NA_KP = (int)na_rup(NA_DIM, BK);
+constexpr size_t NA_A_BYTES = (size_t)na_max(Low::S, High::S) * NA_AROWS * NA_KP * sizeof(__nv_bfloat16);
+constexpr size_t NA_B_BYTES = (size_t)na_max(Low::S * (int)na_rup(NA_DIM, Low::BN), High::S * (int)na_rup(NA_DIM, High::BN)) *
+                              NA_KP * sizeof(__nv_bfloat16);
 constexpr size_t NA_OFF_A = 0;
-constexpr size_t NA_OFF_B = NA_OFF_A + NA_SLICE_BYTES;
-constexpr size_t NA_OFF_REXP = NA_OFF_B + NA_SLICE_BYTES;                    // int[2][NA_DIM]
-constexpr size_t NA_OFF_ERR = NA_OFF_REXP + 2 * NA_DIM * sizeof(int);
+constexpr size_t NA_OFF_B = na_rup(NA_OFF_A + NA_A_BYTES, 1024);
+constexpr size_t NA_OFF_REXP = na_rup(NA_OFF_B + NA_B_BYTES, 256);          // int[NA_AROWS + NA_BROWS]
+constexpr size_t NA_OFF_ERR = NA_OFF_REXP + (size_t)(NA_AROWS + NA_BROWS) * sizeof(int);
 constexpr size_t NA_OFF_TCD = na_rup(NA_OFF_ERR + sizeof(int), 256);
 constexpr size_t NA_OFF_PREP = na_rup(NA_OFF_TCD + sizeof(TcDesc), 256);
 constexpr size_t NA_BYTES = na_rup(NA_OFF_PREP + 2 * sizeof(PrepDesc), 256);
@@ -881,7 +996,7 @@ extern "C" int hx_gemm_noalloc(const double *dA, const double *dB, double *dC, i
     const int S = high ? High::S : Low::S, BN = high ? High::BN : Low::BN;
 
     __nv_bfloat16 *abuf = (__nv_bfloat16 *)(base + NA_OFF_A), *bbuf = (__nv_bfloat16 *)(base + NA_OFF_B);
-    int *aexp = (int *)(base + NA_OFF_REXP), *bexp = aexp + NA_DIM;
+    int *aexp = (int *)(base + NA_OFF_REXP), *bexp = aexp + NA_AROWS;
     int *err = (int *)(base + NA_OFF_ERR);
     TcDesc *d_tcd = (TcDesc *)(base + NA_OFF_TCD);
     PrepDesc *d_prep = (PrepDesc *)(base + NA_OFF_PREP);
@@ -908,10 +1023,12 @@ extern "C" int hx_gemm_noalloc(const double *dA, const double *dB, double *dC, i
     p[0].s[0] = 0; p[0].s[1] = K; p[0].s[2] = 0; p[0].s[3] = 1; p[0].s[4] = 0;
     p[1] = p[0];
     p[1].src = dB; p[1].dst = bbuf; p[1].rexp = bexp; p[1].R = N; p[1].Rp = d.Np; p[1].Ri = N;
-    p[1].work_start = (long long)d.Mp * (d.Kp / 8);
+    p[0].rfast = prep_rfast(p[0]);
+    p[1].rfast = prep_rfast(p[1]);
+    p[1].work_start = (long long)(d.Mp / PT_R) * (d.Kp / PT_K);
     p[1].row_start = d.Mp;
     const long long rows = (long long)d.Mp + d.Np;
-    const long long work = rows * (d.Kp / 8);
+    const long long work = (rows / PT_R) * (d.Kp / PT_K);
     const long long tiles = (long long)d.tiles_m * d.tiles_n;
 
     // what must start at zero: the error word and C (accumulated with beta = 1)
@@ -920,13 +1037,11 @@ extern "C" int hx_gemm_noalloc(const double *dA, const double *dB, double *dC, i
     if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_tcd, &d, sizeof(d), cudaMemcpyHostToDevice, s);
     if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_prep, p, sizeof(p), cudaMemcpyHostToDevice, s);
     if (ce == cudaSuccess) {
-        row_scale<<<(unsigned)((rows * 32 + 255) / 256), 256, 0, s>>>(d_prep, 2, rows, nullptr);
-        if (high) split_gather<High::S><<<(unsigned)((work + 255) / 256), 256, 0, s>>>(d_prep, 2, work, nullptr);
-        else split_gather<Low::S><<<(unsigned)((work + 255) / 256), 256, 0, s>>>(d_prep, 2, work, nullptr);
-        if (high) tc_gemm<High><<<(unsigned)tiles, NTHREADS, High::SMEM_BYTES, s>>>(d_tcd, 1, nullptr, err);
-        else tc_gemm<Low><<<(unsigned)tiles, NTHREADS, Low::SMEM_BYTES, s>>>(d_tcd, 1, nullptr, err);
-        hx_count_launches(3);
-        ce = cudaGetLastError();
+        ce = prep_launch(d_prep, 2, work, rows, S, nullptr, s);
+        if (ce == cudaSuccess && high) tc_gemm<High><<<(unsigned)tiles, High::NTHREADS, High::SMEM_BYTES, s>>>(d_tcd, 1, nullptr, err);
+        else if (ce == cudaSuccess) tc_gemm<Low><<<(unsigned)tiles, Low::NTHREADS, Low::SMEM_BYTES, s>>>(d_tcd, 1, nullptr, err);
+        hx_count_launches(1);
+        if (ce == cudaSuccess) ce = cudaGetLastError();
     }
     int werr = 0;
     if (ce == cudaSuccess) ce = cudaMemcpyAsync(&werr, err, sizeof(int), cudaMemcpyDeviceToHost, s);

@@ -123,6 +123,41 @@ int hx_ccsd_init(hx_ccsd *h);
 /* Replace molecule mol's amplitudes (reference layout, see above). */
 int hx_ccsd_set_guess(hx_ccsd *h, int32_t mol, const double *t1, const double *t2);
 
+/* ---- Learned T2 guess (no counterpart in the reference; it replaces the
+ * MP2-like guessCC amplitudes when hx_cc_params.guess = 1). The network is
+ * 8 -> 256 -> 256 -> 256 -> 1 with SiLU, bf16 weights in layers 2 and 3,
+ * FP32 accumulation; its parameters are one float32 blob of
+ * hx_mlp_nparam() values: W1[256x8] b1 W2[256x256] b2 W3[256x256] b3 w4[256]
+ * b4 x_shift[8] x_scale[8] y_scale. Per amplitude (ia) <= (jb) it reads
+ * x = (guess, e_i, e_j, e_a, e_b, (ia|jb), (ib|ja), 8/N) and predicts
+ * t2 - guess; both t2 entries of the pair receive guess + prediction. */
+int hx_mlp_nparam(void);
+
+/* Install (params != NULL, copied) or remove (NULL) the network used by
+ * hx_ccsd_init when guess = 1. */
+int hx_ccsd_set_model(hx_ccsd *h, const float *params);
+
+/* Training rows of a solved molecule: for n canonical pair indices rows[k]
+ * (index r of the pair (p, q), p <= q, in row-major order of the upper
+ * triangle of the (ia) x (jb) matrix, p = i*v + a) the 8 inputs X[k][8] and
+ * the target T[k] = t2(current) - guess. */
+int hx_ccsd_training_rows(hx_ccsd *h, int32_t mol, int32_t n, const int64_t *rows, float *X, float *T);
+
+/* Network on n input rows X[n][8] (host arrays): Y[n] = predictions
+ * (tcgen05 inference kernel). */
+int hx_mlp_predict(const float *params, const float *X, int64_t n, float *Y);
+
+/* Mean-squared-error loss (in units of y_scale^2) and its gradient with
+ * respect to every blob entry (0 for the fixed normalisation constants) on
+ * n rows, computed on the GPU by the training kernels. */
+int hx_mlp_grad(const float *params, const float *X, const float *T, int32_t n, float *loss, float *grad);
+
+/* Train the network on the GPU: Adam (cosine-decayed learning rate lr) over
+ * `epochs` passes of shuffled mini-batches of `batch` rows; params is updated
+ * in place and epoch_loss[e] (if not NULL) receives each epoch's mean loss. */
+int hx_mlp_train(float *params, const float *X, const float *T, int64_t n, int32_t epochs, int32_t batch, float lr,
+                 uint64_t seed, float *epoch_loss);
+
 /* iterationCC (mod_cc.f90:820-891) for every active molecule: residuals,
  * Jacobi step, DIIS. acc[0] = max|d1|, acc[1] = max|d2| of molecule 0
  * (acc[2..4] = -1, as the reference fills them). */

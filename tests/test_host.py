@@ -162,3 +162,36 @@ def test_replicas_gather_over_gloo():
         p.join(timeout=60)
     assert sorted(out) == [0, 1, 2, 3, 4]
     assert out[0] == pytest.approx(out[3]) and out[1] == pytest.approx(out[4])
+
+
+def test_tensor_core_slicing_is_an_exact_digit_expansion(tmp_path):
+    """hx_slice.h on the host: |digits| <= 128 and sum_p s_p 2^-8p equals
+    x 2^(7-e) to within half a unit of the last digit; e is frexp's exponent."""
+    import shutil
+    import subprocess
+    if shutil.which("g++") is None:
+        pytest.skip("no host C++ compiler")
+    exe = tmp_path / "slice_harness"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "helios_gb300", "csrc"),
+                    os.path.join(ROOT, "tests", "slice_harness.cpp"), "-o", str(exe)], check=True)
+    rng = np.random.default_rng(4)
+    rows = []
+    for _ in range(4000):
+        mx = float(np.exp(rng.uniform(-40, 40)))
+        x = float(mx * rng.uniform(-1, 1))
+        rows.append((mx, x))
+    for mx in (1.0, 0.75, 3.0, 5e-324, 2.2250738585072014e-308, 1e300):
+        rows += [(mx, mx), (mx, -mx), (mx, 0.0), (mx, mx * 0.5), (mx, float(np.nextafter(mx, 0)))]
+    rows += [(2.0 ** 10, (2 ** 3 + 0.5) * 2.0 ** -13), (1.0, 2.0 ** -30), (1.0, -(2.0 ** -17) * 1.5)]
+    inp = "".join(f"{mx.hex()} {x.hex()}\n" for mx, x in rows)
+    out = subprocess.run([str(exe)], input=inp, capture_output=True, text=True, check=True).stdout.split("\n")
+    for (mx, x), line in zip(rows, out):
+        v = [int(t) for t in line.split()]
+        e = np.frexp(mx)[1] if mx != 0 else 0
+        assert v[0] == e
+        a = np.ldexp(x, 7 - e)
+        for digits in (v[1:4], v[4:9]):
+            S = len(digits)
+            assert max(abs(d) for d in digits) <= 128
+            recon = sum(np.ldexp(float(d), -8 * p) for p, d in enumerate(digits))
+            assert abs(recon - a) <= np.ldexp(1.0, -8 * (S - 1) - 1) * (1 + 1e-12)

@@ -177,3 +177,56 @@ def test_rhf_reference_scheme_converges():
         assert np.abs(F - np.diag(np.diag(F))).max() < 1e-9
         o = model["nel"] // 2
         assert scf["E"][o] - scf["E"][o - 1] > 1.0     # aufbau gap
+
+
+# ---------------------------------------------------------------- learned-guess network oracle
+def test_mlp_oracle_backward_matches_finite_differences():
+    from oracle import mlp
+    rng = np.random.default_rng(0)
+    X = rng.normal(size=(64, 8))
+    T = rng.normal(size=64) * 0.01
+    p = mlp.init(rng, X.mean(0), 1 / X.std(0), 0.01)
+    p["w4"] = rng.normal(size=256) * 0.2
+    _, g = mlp.loss_and_grads(p, X, T, rounding=False)
+    for name, idx in [("W1", (3, 2)), ("b1", (5,)), ("W2", (4, 4)), ("b2", (9,)), ("W3", (1, 2)),
+                      ("b3", (7,)), ("w4", (7,)), ("b4", (0,))]:
+        h = 1e-6
+        pp = {k: v.copy() for k, v in p.items()}
+        pm = {k: v.copy() for k, v in p.items()}
+        pp[name][idx] += h
+        pm[name][idx] -= h
+        fd = (mlp.loss_and_grads(pp, X, T, False)[0] - mlp.loss_and_grads(pm, X, T, False)[0]) / (2 * h)
+        assert abs(fd - g[name][idx]) <= 1e-5 * abs(g[name][idx]) + 1e-12, name
+
+
+def test_mlp_oracle_pack_round_trip_and_bf16_rounding():
+    from oracle import mlp
+    rng = np.random.default_rng(1)
+    p = mlp.init(rng, np.zeros(8), np.ones(8), 1.0)
+    blob = mlp.pack(p)
+    assert blob.size == mlp.NPARAM == 134162
+    q = mlp.unpack(blob)
+    assert all(np.array_equal(np.float32(p[k]), np.float32(q[k])) for k in p)
+    # ties to even: 1 + 2^-8 is halfway between bf16 neighbours 1 and 1 + 2^-7
+    assert mlp.bf16(np.float32(1 + 2 ** -8)) == 1.0
+    assert mlp.bf16(np.float32(1 + 3 * 2 ** -8)) == 1 + 2 ** -6
+
+
+def test_mlp_features_restate_the_guess():
+    from oracle import mlp
+    mol = molecules.polyene(8)
+    model = build_model(mol, alternation=0.1)
+    scf = rhf(model)
+    F, _ = mo_fock(model, scf["V"], scf["D"])
+    o = model["nel"] // 2
+    I = ccsd_fact.Integrals(scf["V"], model["G"], o)
+    v = F.shape[0] - o
+    ov = o * v
+    gov = I.coulomb("ovov").reshape(ov, ov)
+    rows = np.arange(ov * (ov + 1) // 2)
+    X, guess = mlp.features(F, gov, o, rows)
+    _, t2 = ccsd_fact.guess(F, I, o)                  # t2[i, j, a, b]
+    t2p = t2.transpose(0, 2, 1, 3).reshape(ov, ov)    # rows (ia), columns (jb)
+    iu = np.triu_indices(ov)
+    assert np.allclose(guess, t2p[iu], rtol=1e-12, atol=1e-15)
+    assert np.allclose(X[:, 7], 1.0)                  # 8 / N with N = 8
