@@ -141,8 +141,10 @@ def run_gb300(args):
         torch.cuda.synchronize()
 
     mol = molecules.polyene(N_SITES)
-    kw = api.Keywords(bond_alternation=0.1, accuracy=-__import__("math").log10(EPS_TIMED), precision="mixed",
-                      mixed_switch=1e-6)
+    from helios_gb300 import learned
+    guess = "learned" if os.path.exists(learned.MODEL_PATH) else "reference"
+    acc_timed = -__import__("math").log10(EPS_TIMED)
+    kw = api.Keywords(bond_alternation=0.1, accuracy=acc_timed, precision="mixed", guess=guess)
     cc = api.CoupledCluster(mol, kw)
 
     def step():
@@ -213,7 +215,8 @@ def run_gb300(args):
     tr = traces[-1]
     t_mixed = time_to_tolerance(tr, e_ref) if e_ref is not None else None
     mixed = {"status": int(last["status"]), "iterations": int(last["iterations"]),
-             "iterations_3slice": int((tr[:, 4] == 2).sum()), "iterations_5slice": int((tr[:, 4] == 1).sum()),
+             "iterations_3slice": int((tr[:, 4] == 3).sum()), "iterations_4slice": int((tr[:, 4] == 2).sum()),
+             "iterations_5slice": int((tr[:, 4] == 1).sum()),
              "fp64_iterations": int((tr[:, 4] == 0).sum()),
              "E_total": e_final,
              "dE_vs_fp64_oracle_eV": None if e_ref is None else abs(e_final - e_ref),
@@ -226,20 +229,33 @@ def run_gb300(args):
     if args.fp64_compare and extra["fp64_plain"]["converged_solve_s"]:
         # both solves stop on an FP64 residual below EPS_TIMED
         extra["speedup_converged_solve"] = extra["fp64_plain"]["converged_solve_s"] / mixed["solve_s"]
-    # --- ensemble of 512 random molecules (8..64 sites) in one batched handle
+    # --- the same mixed solve from the reference guess (what the learned guess gains)
+    if guess == "learned":
+        cr = api.CoupledCluster(mol, api.Keywords(bond_alternation=0.1, accuracy=acc_timed, precision="mixed"))
+        cr.initCC()
+        rr = cr.iterate()
+        trr = cr.timing()
+        cr.finalizeCC()
+        extra["mixed_reference_guess"] = {"status": int(rr["status"]), "iterations": int(rr["iterations"]),
+                                          "solve_s": (trr["init_ms"] + trr["solve_ms"]) / 1e3,
+                                          "E_total": float(rr["energy"][0])}
+    # --- ensemble of seeded random molecules (8..64 sites) in one batched handle,
+    # held out from the learned guess's training seeds
     if args.batch > 0:
-        mols = molecules.ensemble(20261203, args.batch)
-        cb = api.CoupledCluster(mols, api.Keywords(bond_alternation=0.1, accuracy=8, precision="mixed"))
-        cb.initCC()
-        cb.solve_batch()
-        cb.initCC()
-        out = cb.solve_batch()
-        tb = cb.timing()
-        cb.finalizeCC()
-        secs = (tb["init_ms"] + tb["solve_ms"]) / 1e3
-        extra["batch"] = {"molecules": args.batch, "seconds": secs, "molecules_per_s": args.batch / secs,
-                          "converged": int((out["status"] == 1).sum()),
-                          "mean_iterations": float(out["iterations"].mean())}
+        mols = molecules.ensemble(learned.HELD_OUT_SEED, args.batch)
+        extra["batch"] = {"molecules": args.batch, "seeds": [learned.HELD_OUT_SEED, learned.HELD_OUT_SEED + args.batch - 1]}
+        for g in (["learned", "reference"] if guess == "learned" else ["reference"]):
+            cb = api.CoupledCluster(mols, api.Keywords(bond_alternation=0.1, accuracy=8, precision="mixed", guess=g))
+            cb.initCC()
+            cb.solve_batch()
+            cb.initCC()
+            out = cb.solve_batch()
+            tb = cb.timing()
+            cb.finalizeCC()
+            secs = (tb["init_ms"] + tb["solve_ms"]) / 1e3
+            extra["batch"][g + "_guess"] = {"seconds": secs, "molecules_per_s": args.batch / secs,
+                                            "converged": int((out["status"] == 1).sum()),
+                                            "mean_iterations": float(out["iterations"].mean())}
     # --- end to end through the C ABI with host buffers
     e2e = run_e2e(api, mol, kw, max(1, min(args.steps, 3)))
     # --- roofline of the tcgen05 GEMM, live over the timed steps
@@ -265,6 +281,7 @@ def run_gb300(args):
         "data": "synthetic (generated PPP polyene, no dataset)",
         "config": {"workload": f"polyene-{N_SITES} r-ccsd (o=v=80), bond-alternation 0.1, Ohno-Klopman, "
                                "mixed precision + FP64 finish, stop at FP64 residual 1e-7",
+                   "guess": guess,
                    "step": "RHF SCF + integrals + guess + CCSD to convergence (device time)",
                    "l2": "inputs larger than L2 (t2 alone is 328 MB)", "parallelism": f"replicas x{world}"},
         "roofline": roof, "cpu_baseline": cpu,

@@ -167,7 +167,9 @@ struct Rules {   // gIterator.f90:88-210
     }
 };
 
-enum { PH_FP64 = 0, PH_HIGH = 1, PH_LOW = 2 };
+enum { PH_FP64 = 0, PH_HIGH = 1, PH_MID = 2, PH_LOW = 3, PH_COUNT = 4 };
+// tensor-core mode (tc::run_group) of a phase: LOW 0, MID 1, HIGH 2
+static inline int tc_mode(int ph) { return PH_LOW - ph; }
 
 struct hx_ccsd {
     hx_cc_params p{};
@@ -200,11 +202,17 @@ struct hx_ccsd {
     std::vector<int> status;
     tc::Engine *tce = nullptr;           // tensor-core backend (mixed precision)
     mlp::Model *model = nullptr;         // learned T2 guess (guess = 1)
-    // mixed precision: per-molecule phase (PH_LOW / PH_HIGH tensor-core
-    // iterations, PH_FP64 CUDA-core FP64) and the matching launch masks
+    // mixed precision: per-molecule phase (PH_LOW / PH_MID / PH_HIGH
+    // tensor-core iterations, PH_FP64 CUDA-core FP64) and one launch mask per phase
     std::vector<int> phase, stall;
     std::vector<double> best;
-    int *d_act_lo = nullptr, *d_act_hi = nullptr, *d_act_fp = nullptr;
+    // host mirror of each molecule's DIIS ring: pushes so far and the phase
+    // that produced each slot (-1 empty or purged); residual at which each
+    // phase ended (0 = not ended, -1 = its vectors purged)
+    std::vector<long long> dcount;
+    std::vector<std::vector<int>> slot_phase;
+    std::vector<std::array<double, 4>> ph_end;
+    int *d_act_ph[PH_COUNT] = {nullptr, nullptr, nullptr, nullptr};
     std::vector<std::vector<std::array<double, 5>>> trace;
     // device time of the last hx_ccsd_init and solve (events on st)
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -258,24 +266,21 @@ static int upload_group(Group &g)
 }
 
 // Each molecule runs the group in its current phase: the tensor-core modes
-// on tcgen05 (d_act_lo / d_act_hi), the others on the FP64 kernel (d_act_fp);
-// every launch skips the molecules that are not its own.
+// on tcgen05, FP64 on the CUDA-core kernel; one launch per phase in use, with
+// that phase's mask (every launch skips the molecules that are not its own).
 static int run_group(hx_ccsd *h, Group &g)
 {
     if (g.tiles == 0) return HX_OK;
     if (h->tce) {
-        int n[3] = {0, 0, 0};
+        int n[PH_COUNT] = {0, 0, 0, 0};
         for (int mi = 0; mi < h->nmol; ++mi)
             if (h->active[mi]) ++n[h->phase[mi]];
-        if (n[PH_LOW]) {
-            cudaError_t e = tc::run_group(h->tce, g.h.data(), (int)g.h.size(), h->d_act_lo, h->st, 0);
+        for (int ph = PH_LOW; ph >= PH_HIGH; --ph) {
+            if (!n[ph]) continue;
+            cudaError_t e = tc::run_group(h->tce, g.h.data(), (int)g.h.size(), h->d_act_ph[ph], h->st, tc_mode(ph));
             if (e != cudaSuccess) { hx_set_error("tensor-core group: %s", cudaGetErrorString(e)); return HX_ERR_CUDA; }
         }
-        if (n[PH_HIGH]) {
-            cudaError_t e = tc::run_group(h->tce, g.h.data(), (int)g.h.size(), h->d_act_hi, h->st, 1);
-            if (e != cudaSuccess) { hx_set_error("tensor-core group: %s", cudaGetErrorString(e)); return HX_ERR_CUDA; }
-        }
-        if (n[PH_FP64]) HX_CU(hx_tgemm_f64_launch(g.d, (int)g.h.size(), g.tiles, h->d_act_fp, h->st));
+        if (n[PH_FP64]) HX_CU(hx_tgemm_f64_launch(g.d, (int)g.h.size(), g.tiles, h->d_act_ph[PH_FP64], h->st));
         return HX_OK;
     }
     HX_CU(hx_tgemm_f64_launch(g.d, (int)g.h.size(), g.tiles, h->d_active, h->st));
@@ -284,18 +289,14 @@ static int run_group(hx_ccsd *h, Group &g)
 
 static int upload_masks(hx_ccsd *h)
 {
-    std::vector<int> lo(h->nmol), hi(h->nmol), fp(h->nmol);
-    for (int mi = 0; mi < h->nmol; ++mi) {
-        lo[mi] = h->active[mi] && h->phase[mi] == PH_LOW;
-        hi[mi] = h->active[mi] && h->phase[mi] == PH_HIGH;
-        fp[mi] = h->active[mi] && h->phase[mi] == PH_FP64;
-    }
+    std::vector<int> m((size_t)PH_COUNT * h->nmol);
+    for (int ph = 0; ph < PH_COUNT; ++ph)
+        for (int mi = 0; mi < h->nmol; ++mi) m[(size_t)ph * h->nmol + mi] = h->active[mi] && h->phase[mi] == ph;
     HX_CU(cudaMemcpyAsync(h->d_active, h->active.data(), sizeof(int) * h->nmol, cudaMemcpyHostToDevice, h->st));
-    if (h->d_act_lo) {
-        HX_CU(cudaMemcpyAsync(h->d_act_lo, lo.data(), sizeof(int) * h->nmol, cudaMemcpyHostToDevice, h->st));
-        HX_CU(cudaMemcpyAsync(h->d_act_hi, hi.data(), sizeof(int) * h->nmol, cudaMemcpyHostToDevice, h->st));
-        HX_CU(cudaMemcpyAsync(h->d_act_fp, fp.data(), sizeof(int) * h->nmol, cudaMemcpyHostToDevice, h->st));
-    }
+    if (h->d_act_ph[0])
+        for (int ph = 0; ph < PH_COUNT; ++ph)
+            HX_CU(cudaMemcpyAsync(h->d_act_ph[ph], &m[(size_t)ph * h->nmol], sizeof(int) * h->nmol,
+                                  cudaMemcpyHostToDevice, h->st));
     // the masks are pageable host vectors: wait so they may go out of scope
     HX_CU(cudaStreamSynchronize(h->st));
     return HX_OK;
@@ -450,11 +451,12 @@ static int allocate(hx_ccsd *h)
     for (int mi = 0; mi < h->nmol; ++mi) maxpair = std::max<long long>(maxpair, (long long)h->o[mi] * h->v[mi] * h->o[mi] * h->v[mi]);
     h->nblk = (int)std::max<long long>(1, std::min<long long>(std::max(1, 1216 / h->nmol), (maxpair + 4095) / 4096));
     HX_CU(cudaMalloc(&h->d_part, sizeof(double) * std::max<size_t>((size_t)h->nmol * h->nblk * HX_MAX_DIIS, 2 * HX_SCF_GRID_MAX)));
-    HX_CU(cudaMalloc(&h->d_act_lo, sizeof(int) * h->nmol));
-    HX_CU(cudaMalloc(&h->d_act_hi, sizeof(int) * h->nmol));
-    HX_CU(cudaMalloc(&h->d_act_fp, sizeof(int) * h->nmol));
+    for (int ph = 0; ph < PH_COUNT; ++ph) HX_CU(cudaMalloc(&h->d_act_ph[ph], sizeof(int) * h->nmol));
     h->active.assign(h->nmol, 1);
     h->phase.assign(h->nmol, PH_FP64);
+    h->dcount.assign(h->nmol, 0);
+    h->slot_phase.assign(h->nmol, {});
+    h->ph_end.assign(h->nmol, {0.0, 0.0, 0.0, 0.0});
     h->stall.assign(h->nmol, 0);
     h->best.assign(h->nmol, 1e300);
     h->trace.assign(h->nmol, {});
@@ -498,7 +500,7 @@ void hx_cc_params_default(hx_cc_params *p)
     p->stagnation_after = 200;
     p->precision = HX_PRECISION_FP64;
     p->guess = 0;
-    p->mixed_switch = 1e-6;
+    p->mixed_switch = 1e-4;
     p->mixed_patience = 3;
 }
 
@@ -601,6 +603,8 @@ static int apply_learned_guess(hx_ccsd *h)
     return HX_OK;
 }
 
+static void diis_mirror_reset(hx_ccsd *h, int mi);
+
 int hx_ccsd_init(hx_ccsd *h)
 {
     if (!h) { hx_set_error("NULL handle"); return HX_ERR_ARG; }
@@ -635,7 +639,10 @@ int hx_ccsd_init(hx_ccsd *h)
     if (h->p.guess == 1) HX_TRY(apply_learned_guess(h));
     if (h->tce) tc::invalidate(h->tce);          // new orbitals: re-slice the constant operands
     for (int mi = 0; mi < h->nmol; ++mi) { h->rules[mi] = Rules(); h->status[mi] = 0; h->active[mi] = 1; }
-    for (int mi = 0; mi < h->nmol; ++mi) HX_CU(cudaMemsetAsync(h->diis[mi].count, 0, sizeof(int), h->st));
+    for (int mi = 0; mi < h->nmol; ++mi) {
+        HX_CU(cudaMemsetAsync(h->diis[mi].count, 0, sizeof(int), h->st));
+        diis_mirror_reset(h, mi);
+    }
     HX_TRY(upload_views(h));
     HX_CU(cudaEventRecord(h->ev[1], h->st));
     HX_TRY(upload_masks(h));
@@ -724,20 +731,65 @@ int hx_ccsd_energy(hx_ccsd *h, double e[5])
     return HX_OK;
 }
 
+static void diis_mirror_reset(hx_ccsd *h, int mi)
+{
+    h->dcount[mi] = 0;
+    h->slot_phase[mi].assign((size_t)h->diis[mi].nd, -1);
+    h->ph_end[mi] = {0.0, 0.0, 0.0, 0.0};
+}
+
+// Mixed precision keeps the DIIS history across a precision switch (a plain
+// "2-1" step is unstable, so a restart costs iterations), but a vector made
+// in a cheaper phase carries that phase's error. Once the residual has fallen
+// to kPurge of the level at which that phase ended, its vectors are taken out
+// of the extrapolation: their Gram row and column are cleared and the
+// diagonal made huge, so their DIIS coefficients vanish; the slots are
+// reused by later pushes as usual.
+static const double kPurge = 0.1;
+
+static int diis_purge(hx_ccsd *h, int mi, double a)
+{
+    const int nd = h->diis[mi].nd;
+    const int valid = (int)std::min<long long>(h->dcount[mi], nd);
+    std::vector<int> drop;
+    for (int ph = 1; ph < PH_COUNT; ++ph) {
+        if (!(h->ph_end[mi][ph] > 0.0) || !(a < kPurge * h->ph_end[mi][ph])) continue;
+        for (int k = 0; k < valid; ++k)
+            if (h->slot_phase[mi][k] == ph) drop.push_back(k);
+        h->ph_end[mi][ph] = -1.0;
+    }
+    if (drop.empty()) return HX_OK;
+    std::vector<double> g((size_t)nd * nd);
+    HX_CU(cudaMemcpyAsync(g.data(), h->diis[mi].gram, sizeof(double) * g.size(), cudaMemcpyDeviceToHost, h->st));
+    HX_CU(cudaStreamSynchronize(h->st));
+    for (int p : drop) {
+        for (int q = 0; q < nd; ++q) g[(size_t)p * nd + q] = g[(size_t)q * nd + p] = 0.0;
+        g[(size_t)p * nd + p] = 1e100;
+        h->slot_phase[mi][p] = -1;
+    }
+    HX_CU(cudaMemcpyAsync(h->diis[mi].gram, g.data(), sizeof(double) * g.size(), cudaMemcpyHostToDevice, h->st));
+    HX_CU(cudaStreamSynchronize(h->st));
+    return HX_OK;
+}
+
 // The iterator (gIterator.f90:88-210) over every active molecule. In mixed
-// precision a molecule runs three phases:
-//   LOW   3-slice tensor-core contractions (~FP32 accuracy) until its residual
-//         falls below mixed_switch or stops improving for mixed_patience
-//         iterations; DIIS restarts (its error vectors are too noisy to mix
-//         with more accurate ones);
-//   HIGH  5-slice tensor-core contractions (residuals as accurate as FP64
-//         ones) until the residual is below kHighMargin * eps (or stops
-//         improving): the iteration is not monotone, and one more HIGH
-//         iteration costs far less than an FP64 iteration whose residual
-//         lands just above eps;
+// precision a molecule walks down a ladder of phases:
+//   LOW   3-slice tensor-core contractions (about 2^-24 of the operands' row
+//         maxima) until the residual falls below mixed_switch;
+//   MID   4-slice (about 2^-32) until it falls below kMidSpan * mixed_switch;
+//   HIGH  5-slice (about 2^-40: residuals as accurate as FP64 ones);
 //   FP64  CUDA-core FP64 iterations: convergence is declared only here, so the
 //         final residual and energy are plain FP64 (the defect correction).
+// Every tensor-core phase hands over to FP64 once the residual is below
+// kHighMargin * eps (the iteration is not monotone, and one more
+// tensor-core iteration costs far less than an FP64 iteration whose
+// residual lands just above eps). A phase switches while its own error is
+// still about 1 % of the residual, so the DIIS history is kept; a phase
+// that stops improving for mixed_patience iterations hands over early and
+// the DIIS history restarts (its error vectors are then too noisy to mix
+// with more accurate ones).
 static const double kHighMargin = 0.1;
+static const double kMidSpan = 1e-2;
 
 static int solve_all(hx_ccsd *h, int maxiter, double eps)
 {
@@ -771,21 +823,35 @@ static int solve_all(hx_ccsd *h, int maxiter, double eps)
             const double a = std::max(r[0], r[1]);
             const int ph = h->phase[mi];
             h->trace[mi].push_back({r[0], r[1], r[2], secs, (double)ph});
+            if (h->p.diis_enabled && a >= eps) {          // the step pushed (t, error) into the ring
+                const int nd = h->diis[mi].nd;
+                h->slot_phase[mi][(size_t)(h->dcount[mi] % nd)] = ph;
+                ++h->dcount[mi];
+            }
+            if (mixed) HX_TRY(diis_purge(h, mi, a));
             if (ph != PH_FP64 && !cancel) {
                 // tensor-core phases never claim convergence: they hand over
                 if (a < h->best[mi]) { h->best[mi] = a; h->stall[mi] = 0; } else ++h->stall[mi];
-                const double target = ph == PH_LOW ? std::max(h->p.mixed_switch, eps) : kHighMargin * eps;
-                const bool handover = a < target || h->stall[mi] >= h->p.mixed_patience;
+                const double fin = kHighMargin * eps;
+                const double below = ph == PH_LOW ? h->p.mixed_switch : ph == PH_MID ? kMidSpan * h->p.mixed_switch : 0.0;
+                const bool stalled = h->stall[mi] >= h->p.mixed_patience;
+                int next = ph;
+                if (a < fin) next = PH_FP64;
+                else if (a < below || stalled) next = ph - 1;
                 Rules &R = h->rules[mi];
-                int s = R.update(handover ? std::max(a, eps * 2) : a, h->p, maxiter, eps, false);
+                int s = R.update(next != ph ? std::max(a, eps * 2) : a, h->p, maxiter, eps, false);
                 if (s == HX_DIVERGED || s == HX_STAGNATED || s == HX_FAILED_MAXITER) {
                     h->status[mi] = s; h->active[mi] = 0; --remaining; changed = true;
-                } else if (handover) {
-                    h->phase[mi] = ph == PH_LOW ? PH_HIGH : PH_FP64;
+                } else if (next != ph) {
+                    h->phase[mi] = next;
                     h->stall[mi] = 0;
                     h->best[mi] = 1e300;
                     changed = true;
-                    if (ph == PH_LOW) HX_CU(cudaMemsetAsync(h->diis[mi].count, 0, sizeof(int), h->st));
+                    h->ph_end[mi][ph] = a;
+                    if (stalled && a >= fin) {
+                        HX_CU(cudaMemsetAsync(h->diis[mi].count, 0, sizeof(int), h->st));
+                        diis_mirror_reset(h, mi);
+                    }
                 }
                 continue;
             }
@@ -878,6 +944,7 @@ int hx_ccsd_set_guess(hx_ccsd *h, int32_t mol, const double *t1, const double *t
     HX_CU(cudaMemcpyAsync(h->cc[mol].t1, a.data(), sizeof(double) * ov, cudaMemcpyHostToDevice, h->st));
     HX_CU(cudaMemcpyAsync(h->cc[mol].t2, b.data(), sizeof(double) * ov * ov, cudaMemcpyHostToDevice, h->st));
     HX_CU(cudaMemsetAsync(h->diis[mol].count, 0, sizeof(int), h->st));
+    diis_mirror_reset(h, mol);
     HX_CU(cudaStreamSynchronize(h->st));
     h->rules[mol] = Rules();
     return HX_OK;
@@ -981,9 +1048,7 @@ void hx_ccsd_destroy(hx_ccsd *h)
     cudaFree(h->d_cc);
     cudaFree(h->d_diis);
     cudaFree(h->d_active);
-    cudaFree(h->d_act_lo);
-    cudaFree(h->d_act_hi);
-    cudaFree(h->d_act_fp);
+    for (int ph = 0; ph < PH_COUNT; ++ph) cudaFree(h->d_act_ph[ph]);
     cudaFree(h->d_part);
     if (h->st) cudaStreamDestroy(h->st);
     delete h;
@@ -994,7 +1059,10 @@ void hx_ccsd_destroy(hx_ccsd *h)
 int hx_gemm(const double *A, const double *B, double *C, int32_t M, int32_t N, int32_t K, int32_t precision,
             int32_t reps, double *ms)
 {
-    if (!A || !B || !C || M <= 0 || N <= 0 || K <= 0 || reps < 1) { hx_set_error("hx_gemm: bad arguments"); return HX_ERR_ARG; }
+    if (!A || !B || !C || M <= 0 || N <= 0 || K <= 0 || reps < 1 || precision < 0 || precision > 3) {
+        hx_set_error("hx_gemm: bad arguments");
+        return HX_ERR_ARG;
+    }
     cudaStream_t st;
     HX_CU(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     double *dA = nullptr, *dB = nullptr, *dC = nullptr;
@@ -1025,7 +1093,7 @@ int hx_gemm(const double *A, const double *B, double *C, int32_t M, int32_t N, i
     if (rc == HX_OK && precision != HX_PRECISION_FP64) rc = tc::create(&te, plan, st);
     if (rc == HX_OK) {
         auto launch = [&]() -> cudaError_t {
-            if (te) return tc::run_group(te, plan[0].h.data(), 1, dact, st, precision == 2 ? 1 : 0);
+            if (te) return tc::run_group(te, plan[0].h.data(), 1, dact, st, precision == 2 ? 2 : precision == 3 ? 1 : 0);
             return hx_tgemm_f64_launch(plan[0].d, 1, plan[0].tiles, dact, st);
         };
         cudaError_t ce = launch();               // warm-up

@@ -63,15 +63,19 @@ namespace tc {
 // for a chunk of depth K) is scaled down by 2^-8NX.
 //   LOW:  3 slices, pairs i + j <= 3 (8 MMAs per k-step), NX = 1: about 2^-24
 //         of the row maxima; 128 x 96 tiles.
+//   MID:  4 slices, pairs i + j <= 3 (10 MMAs), NX = 2: about 2^-32; 128 x 80.
 //   HIGH: 5 slices, pairs i + j <= 5 (19 MMAs), NX = 3: about 2^-40; residuals
-//         as accurate as FP64 ones; 128 x 32 tiles.
-template <int S_, int QMAX_, int NX_, int BN_, int STAGES_, int KC_, int EPIW_>
+//         as accurate as FP64 ones; 128 x 64 tiles fed by 32-deep k-blocks
+//         (64-byte swizzle) so that three stages of five slices fit.
+template <int S_, int QMAX_, int NX_, int BN_, int STAGES_, int KC_, int EPIW_, int BK_ = 64>
 struct Cfg {
     static constexpr int S = S_;                     // integer slices per FP64 operand
     static constexpr int QMAX = QMAX_;               // slice pairs with i + j <= QMAX are multiplied
     static constexpr int NX = NX_;                   // exact classes q = 0 .. NX-1
     static constexpr int NQ = QMAX_ >= NX_ ? NX_ + 1 : QMAX_ + 1;   // TMEM accumulators per buffer
-    static constexpr int BM = 128, BN = BN_, BK = 64;
+    static constexpr int BM = 128, BN = BN_, BK = BK_;   // BK: k-block depth (64 or 32)
+    static constexpr uint64_t SWZ = BK_ == 64 ? 2 : 4;     // smem descriptor layout: 128- or 64-byte swizzle
+    static constexpr int SBO = 8 * BK_ * 2;                 // bytes between 8-row core-matrix groups
     static constexpr int KC = KC_;                   // k-blocks per chunk (exact classes stay exact)
     static constexpr int STAGES = STAGES_;
     static constexpr int EPI_WARPS = EPIW_;          // epilogue warps (a multiple of 4)
@@ -87,16 +91,18 @@ struct Cfg {
     // pairs in the largest exact class
     static constexpr int XPAIRS = [] { int m = 0; for (int q = 0; q < NX_; ++q) { int n = 0; for (int i = 0; i < S_; ++i) n += (q - i >= 0 && q - i < S_); m = n > m ? n : m; } return m; }();
     // exactness of a chunk: (pairs per exact class) * KC*64 * 2^14 < 2^24
-    static_assert((long long)XPAIRS * KC_ * 64 * 16384LL < (1LL << 24), "chunk too deep for exact sums");
+    static_assert((long long)XPAIRS * KC_ * BK_ * 16384LL < (1LL << 24), "chunk too deep for exact sums");
+    static_assert(BK_ == 64 || BK_ == 32, "k-block depth");
     static_assert(2 * NQ * BN_ <= 512, "two TMEM buffers must fit in 512 columns");
-    static_assert(STAGES_ * S_ * (128 * 64 * 2 + BN_ * 64 * 2) + 1280 <= 232448, "shared memory");
+    static_assert(STAGES_ * S_ * (128 * BK_ * 2 + BN_ * BK_ * 2) + 1280 <= 232448, "shared memory");
     static_assert(EPIW_ % 4 == 0 && EPI_COLS % 8 == 0, "epilogue split");
     static_assert(128 * (BN_ + 1) * 8 <= STAGES_ * STAGE_BYTES, "output tile staging fits in the TMA ring");
 };
 using Low = Cfg<3, 3, 1, 96, 2, 8, 12>;
-using High = Cfg<5, 5, 3, 32, 2, 3, 8>;
+using Mid = Cfg<4, 3, 2, 80, 2, 6, 8>;
+using High = Cfg<5, 5, 3, 64, 3, 8, 8, 32>;
 constexpr int TMEM_COLS = 512;
-constexpr int BM = 128, BK = 64;
+constexpr int BM = 128, KPAD = 64;   // K is padded to KPAD (the slicing tile depth)
 constexpr unsigned long long WAIT_NS = 4000000000ull; // a wait longer than 4 s is declared failed
 
 struct TcDesc {
@@ -179,6 +185,15 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t addr)
     d |= (uint64_t)2 << 61;                    // SWIZZLE_128B
     return d;
 }
+// The same for a configuration's k-block depth: 128-byte rows (BK = 64,
+// SWIZZLE_128B) or 64-byte rows (BK = 32, SWIZZLE_64B); K-major, 8-row groups
+// SBO bytes apart, descriptor version 1.
+template <class C>
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr)
+{
+    return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(C::SBO >> 4) << 32) |
+           ((uint64_t)1 << 46) | (C::SWZ << 61);
+}
 // Instruction descriptor: kind::f16, D=F32, A=B=BF16, both K-major, M x N.
 __host__ __device__ constexpr uint32_t idesc_bf16(int m, int n)
 {
@@ -239,7 +254,7 @@ struct PrepDesc {
     int *rexp;                       // [batch][Rp] binary exponent of each row's largest entry
     int batch, R, K, Rp, Kp, Ri, Ki;
     long long s[5];                  // r0, r1, k0, k1, batch strides of the FP64 source
-    long long work_start;            // prefix of tiles (batch * Rp/PT_R * Kp/PT_K) over the launch
+    long long work_start;            // prefix of tiles (batch * ceil(Rp/PT_R) * Kp/PT_K) over the launch
     long long row_start;             // prefix of batch*Rp over the launch
     int mol;
     int rfast;                       // rows (1) or k (0) are the contiguous dimension of the source
@@ -271,7 +286,7 @@ __device__ __forceinline__ bool load_tile(const PrepDesc *__restrict__ pd, int n
     const PrepDesc &d = pd[t.desc];
     if (active && !active[d.mol]) return false;
     long long local = u - d.work_start;
-    const int tk = d.Kp / PT_K, tr = d.Rp / PT_R;
+    const int tk = d.Kp / PT_K, tr = (d.Rp + PT_R - 1) / PT_R;
     k0 = (int)(local % tk) * PT_K;
     local /= tk;
     r0 = (int)(local % tr) * PT_R;
@@ -348,7 +363,8 @@ __global__ void __launch_bounds__(PT_THREADS) split_gather(const PrepDesc *__res
     const int rr = threadIdx.x >> 3, c8 = (threadIdx.x & 7) * 8;
     for (long long u = blockIdx.x; u < units; u += gridDim.x) {
         int b, r0, k0;
-        if (load_tile(pd, n, u, active, t, b, r0, k0)) {
+        // (a partial last row tile has rows beyond Rp: they write nothing)
+        if (load_tile(pd, n, u, active, t, b, r0, k0) && r0 + rr < pd[t.desc].Rp) {
             const PrepDesc &d = pd[t.desc];
             int e = d.rexp[(long long)b * d.Rp + r0 + rr];
             if (e == INT_MIN) e = 0;
@@ -412,7 +428,7 @@ __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restri
     const int in_g = (int)(local % (GM * d.tiles_n));
     const int tm = first_m + in_g % gsz, tn = in_g / gsz;
     const int kb0 = ks * d.kb_per;
-    const int nkb = min(d.Kp / BK - kb0, d.kb_per);     // >= 1 by construction
+    const int nkb = min(d.Kp / C::BK - kb0, d.kb_per);  // >= 1 by construction
     const int nchunk = (nkb + C::KC - 1) / C::KC;
 
     if (threadIdx.x == 0) {
@@ -445,8 +461,8 @@ __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restri
                 uint8_t *sb = sa + C::S * C::ATILE;
                 mbar_expect_tx(&full[st], C::STAGE_BYTES);
                 for (int p = 0; p < C::S; ++p) {
-                    tma_load_2d(sa + p * C::ATILE, &d.mapA, &full[st], (kb0 + kb) * BK, p * aplane + arow0);
-                    tma_load_2d(sb + p * C::BTILE, &d.mapB, &full[st], (kb0 + kb) * BK, p * bplane + brow0);
+                    tma_load_2d(sa + p * C::ATILE, &d.mapA, &full[st], (kb0 + kb) * C::BK, p * aplane + arow0);
+                    tma_load_2d(sb + p * C::BTILE, &d.mapB, &full[st], (kb0 + kb) * C::BK, p * bplane + brow0);
                 }
             }
         }
@@ -471,7 +487,7 @@ __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restri
                     const uint32_t sb = sa + C::S * C::ATILE;
                     const bool chunk_start = kb == c * C::KC;
 #pragma unroll 1
-                    for (int kk = 0; kk < BK / 16; ++kk) {
+                    for (int kk = 0; kk < C::BK / 16; ++kk) {
 #pragma unroll
                         for (int i = 0; i < C::S; ++i) {
 #pragma unroll
@@ -486,8 +502,8 @@ __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restri
                                                                : (C::NX < C::S ? 0 : C::NX - (C::S - 1));
                                 const bool first = chunk_start && kk == 0 && i == i_first &&
                                                    (cl < C::NX || j == C::NX - i_first);
-                                const uint64_t ad = sw128_desc(sa + i * C::ATILE + kk * 32);
-                                const uint64_t bd = sw128_desc(sb + j * C::BTILE + kk * 32);
+                                const uint64_t ad = smem_desc<C>(sa + i * C::ATILE + kk * 32);
+                                const uint64_t bd = smem_desc<C>(sb + j * C::BTILE + kk * 32);
                                 mma_bf16(dbase + cl * C::BN, ad, bd, idesc, first ? 0u : 1u);
                             }
                         }
@@ -582,7 +598,7 @@ struct SubGroup {
 };
 
 struct Mode {                        // one precision: descriptors of every plan group
-    int S = 0, BN = 0, products = 0, smem = 0;
+    int S = 0, BN = 0, BK = 64, products = 0, smem = 0;
     __nv_bfloat16 *fixed = nullptr;  // slices of the constant operands (persistent)
     int *fixed_rexp = nullptr;
     std::vector<SubGroup> groups;    // one per plan group, same order
@@ -592,7 +608,7 @@ struct Engine {
     __nv_bfloat16 *scratch = nullptr;   // slices of the variable operands (shared by groups and modes)
     int *rexp = nullptr;
     int *d_err = nullptr;
-    Mode mode[2];                        // 0 = LOW, 1 = HIGH
+    Mode mode[3];                        // 0 = LOW, 1 = MID, 2 = HIGH (3, 4, 5 slices)
     std::vector<const Group *> keys;
     bool profile = false;
     int generation = 0;
@@ -642,17 +658,19 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
     return fn;
 }
 
-static int make_map(CUtensorMap *map, void *base, long long rows, int kp, int box_rows)
+// 2D map over slices [rows][kp] bf16: boxes of bk x box_rows, swizzled to the
+// k-block's row length (128 bytes for bk = 64, 64 bytes for bk = 32).
+static int make_map(CUtensorMap *map, void *base, long long rows, int kp, int box_rows, int bk)
 {
     auto fn = encode_fn();
     if (!fn) { hx_set_error("cuTensorMapEncodeTiled is unavailable"); return HX_ERR_CUDA; }
     cuuint64_t dims[2] = {(cuuint64_t)kp, (cuuint64_t)rows};
     cuuint64_t strides[1] = {(cuuint64_t)kp * 2};
-    cuuint32_t box[2] = {BK, (cuuint32_t)box_rows};
+    cuuint32_t box[2] = {(cuuint32_t)bk, (cuuint32_t)box_rows};
     cuuint32_t es[2] = {1, 1};
     CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, es,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, bk == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) { hx_set_error("cuTensorMapEncodeTiled failed (%d)", (int)r); return HX_ERR_CUDA; }
     return HX_OK;
 }
@@ -678,6 +696,7 @@ static cudaError_t prep_launch(const PrepDesc *d, int n, long long tiles, long l
     rexp_init<<<rb, 256, 0, s>>>(d, n, rows, active);
     row_scale<<<tb, PT_THREADS, 0, s>>>(d, n, tiles, active);
     if (S == Low::S) split_gather<Low::S><<<tb, PT_THREADS, 0, s>>>(d, n, tiles, active);
+    else if (S == Mid::S) split_gather<Mid::S><<<tb, PT_THREADS, 0, s>>>(d, n, tiles, active);
     else split_gather<High::S><<<tb, PT_THREADS, 0, s>>>(d, n, tiles, active);
     hx_count_launches(3);
     return cudaGetLastError();
@@ -696,7 +715,7 @@ static int build_mode(Engine *e, Mode &md, const std::vector<Group> &plan, size_
     for (const Group &g : plan)
         for (const TgemmDesc &t : g.h) {
             if (!on_tc(t)) continue;
-            const size_t Kp = rup(t.K, BK), Ma = rup(t.M, BM), Nb = rup(t.N, BN);
+            const size_t Kp = rup(t.K, KPAD), Ma = rup(t.M, BM), Nb = rup(t.N, BN);
             if (t.a_const) { fneed += (size_t)S * t.batch * Ma * Kp; frows += (size_t)t.batch * Ma; }
             if (t.b_const) { fneed += (size_t)S * t.batch * Nb * Kp; frows += (size_t)t.batch * Nb; }
         }
@@ -715,16 +734,16 @@ static int build_mode(Engine *e, Mode &md, const std::vector<Group> &plan, size_
             TcDesc d;
             memset(&d, 0, sizeof(d));
             d.batch = t.batch; d.M = t.M; d.N = t.N; d.K = t.K;
-            d.Mp = (int)rup(t.M, BM); d.Np = (int)rup(t.N, BN); d.Kp = (int)rup(t.K, BK);
+            d.Mp = (int)rup(t.M, BM); d.Np = (int)rup(t.N, BN); d.Kp = (int)rup(t.K, KPAD);
             d.Mi = t.Mi; d.Ni = t.Ni;
             for (int k = 0; k < 5; ++k) d.c[k] = t.c[k];
             d.alpha = t.alpha; d.beta = t.beta; d.C = t.C; d.mol = t.mol;
             d.tiles_m = d.Mp / BM; d.tiles_n = d.Np / BN;
             // long K over few output tiles: cut K into slices that fill the GPU
-            const int nkb = d.Kp / BK;
+            const int nkb = d.Kp / md.BK, n64 = d.Kp / KPAD;
             const long long out_tiles = (long long)d.batch * d.tiles_m * d.tiles_n;
             int ks = 1;
-            if (t.beta == 1.0 && out_tiles < 152 && nkb >= 16) ks = (int)std::min<long long>((152 + out_tiles - 1) / out_tiles, nkb / 8);
+            if (t.beta == 1.0 && out_tiles < 152 && n64 >= 16) ks = (int)std::min<long long>((152 + out_tiles - 1) / out_tiles, n64 / 8);
             d.kb_per = (nkb + ks - 1) / ks;
             d.ksplit = (nkb + d.kb_per - 1) / d.kb_per;
             d.tile_start = tiles;
@@ -738,8 +757,8 @@ static int build_mode(Engine *e, Mode &md, const std::vector<Group> &plan, size_
             if (t.b_const) { bbuf = md.fixed + foff; foff += bsz; bexp = md.fixed_rexp + froff; froff += (size_t)t.batch * d.Np; }
             else { bbuf = e->scratch + off; off += bsz; bexp = e->rexp + roff; roff += (size_t)t.batch * d.Np; }
             if (off > var_elems_cap) { hx_set_error("tensor-core scratch overflow"); return HX_ERR_STATE; }
-            int rc = make_map(&d.mapA, abuf, (long long)S * d.batch * d.Mp, d.Kp, BM);
-            if (rc == HX_OK) rc = make_map(&d.mapB, bbuf, (long long)S * d.batch * d.Np, d.Kp, BN);
+            int rc = make_map(&d.mapA, abuf, (long long)S * d.batch * d.Mp, d.Kp, BM, md.BK);
+            if (rc == HX_OK) rc = make_map(&d.mapB, bbuf, (long long)S * d.batch * d.Np, d.Kp, BN, md.BK);
             if (rc < 0) return rc;
             PrepDesc pa, pb;
             memset(&pa, 0, sizeof(pa));
@@ -757,7 +776,7 @@ static int build_mode(Engine *e, Mode &md, const std::vector<Group> &plan, size_
                 p.work_start = L.work;
                 p.row_start = L.rows;
                 p.rfast = prep_rfast(p);
-                L.work += (long long)p.batch * (p.Rp / PT_R) * (p.Kp / PT_K);
+                L.work += (long long)p.batch * ((p.Rp + PT_R - 1) / PT_R) * (p.Kp / PT_K);
                 L.rows += (long long)p.batch * p.Rp;
                 L.h.push_back(p);
             };
@@ -798,8 +817,10 @@ int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s)
 {
     *out = nullptr;
     Engine *e = new Engine();
+    e->mode[0].BK = Low::BK; e->mode[1].BK = Mid::BK; e->mode[2].BK = High::BK;
     e->mode[0].S = Low::S; e->mode[0].BN = Low::BN; e->mode[0].products = Low::PRODUCTS; e->mode[0].smem = Low::SMEM_BYTES;
-    e->mode[1].S = High::S; e->mode[1].BN = High::BN; e->mode[1].products = High::PRODUCTS; e->mode[1].smem = High::SMEM_BYTES;
+    e->mode[1].S = Mid::S; e->mode[1].BN = Mid::BN; e->mode[1].products = Mid::PRODUCTS; e->mode[1].smem = Mid::SMEM_BYTES;
+    e->mode[2].S = High::S; e->mode[2].BN = High::BN; e->mode[2].products = High::PRODUCTS; e->mode[2].smem = High::SMEM_BYTES;
     // variable operands share one scratch: the largest group of either mode
     size_t need = 0, need_rows = 0;
     for (const Mode &md : e->mode)
@@ -807,7 +828,7 @@ int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s)
             size_t gneed = 0, grows = 0;
             for (const TgemmDesc &t : g.h) {
                 if (!on_tc(t)) continue;
-                const size_t Kp = rup(t.K, BK), Ma = rup(t.M, BM), Nb = rup(t.N, md.BN);
+                const size_t Kp = rup(t.K, KPAD), Ma = rup(t.M, BM), Nb = rup(t.N, md.BN);
                 if (!t.a_const) { gneed += (size_t)md.S * t.batch * Ma * Kp; grows += (size_t)t.batch * Ma; }
                 if (!t.b_const) { gneed += (size_t)md.S * t.batch * Nb * Kp; grows += (size_t)t.batch * Nb; }
             }
@@ -828,6 +849,7 @@ int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s)
     }
     for (const Group &g : plan) e->keys.push_back(&g);
     if (cudaFuncSetAttribute(tc_gemm<Low>, cudaFuncAttributeMaxDynamicSharedMemorySize, Low::SMEM_BYTES) != cudaSuccess ||
+        cudaFuncSetAttribute(tc_gemm<Mid>, cudaFuncAttributeMaxDynamicSharedMemorySize, Mid::SMEM_BYTES) != cudaSuccess ||
         cudaFuncSetAttribute(tc_gemm<High>, cudaFuncAttributeMaxDynamicSharedMemorySize, High::SMEM_BYTES) != cudaSuccess) {
         destroy(e);
         hx_set_error("cannot reserve shared memory for tc_gemm");
@@ -842,7 +864,7 @@ cudaError_t run_group(Engine *e, const TgemmDesc *descs, int n, const int *d_act
     int gi = -1;
     for (size_t k = 0; k < e->keys.size(); ++k)
         if (e->keys[k]->h.data() == descs) { gi = (int)k; break; }
-    if (gi < 0 || mode < 0 || mode > 1) return cudaErrorInvalidValue;
+    if (gi < 0 || mode < 0 || mode > 2) return cudaErrorInvalidValue;
     Mode &md = e->mode[mode];
     SubGroup &sg = md.groups[gi];
     if (sg.fp64.tiles > 0) {
@@ -872,6 +894,7 @@ cudaError_t run_group(Engine *e, const TgemmDesc *descs, int n, const int *d_act
         cudaEventRecord(pend.a, s);
     }
     if (mode == 0) tc_gemm<Low><<<(unsigned)sg.tiles, Low::NTHREADS, Low::SMEM_BYTES, s>>>(sg.d_tcd, (int)sg.tcd.size(), d_active, e->d_err);
+    else if (mode == 1) tc_gemm<Mid><<<(unsigned)sg.tiles, Mid::NTHREADS, Mid::SMEM_BYTES, s>>>(sg.d_tcd, (int)sg.tcd.size(), d_active, e->d_err);
     else tc_gemm<High><<<(unsigned)sg.tiles, High::NTHREADS, High::SMEM_BYTES, s>>>(sg.d_tcd, (int)sg.tcd.size(), d_active, e->d_err);
     r = cudaGetLastError();
     if (e->profile) {
@@ -925,7 +948,7 @@ constexpr int na_max(int a, int b) { return a > b ? a : b; }
 // padded rows of A (to 128) and of B (to either mode's tile width), padded K
 constexpr int NA_AROWS = (int)na_rup(NA_DIM, BM);
 constexpr int NA_BROWS = na_max((int)na_rup(NA_DIM, Low::BN), (int)na_rup(NA_DIM, High::BN));
-constexpr int NA_KP = (int)na_rup(NA_DIM, BK);
+constexpr int NA_KP = (int)na_rup(NA_DIM, KPAD);
 constexpr size_t NA_A_BYTES = (size_t)na_max(Low::S, High::S) * NA_AROWS * NA_KP * sizeof(__nv_bfloat16);
 constexpr size_t NA_B_BYTES = (size_t)na_max(Low::S * (int)na_rup(NA_DIM, Low::BN), High::S * (int)na_rup(NA_DIM, High::BN)) *
                               NA_KP * sizeof(__nv_bfloat16);
@@ -1005,17 +1028,18 @@ extern "C" int hx_gemm_noalloc(const double *dA, const double *dB, double *dC, i
     TcDesc d;
     memset(&d, 0, sizeof(d));
     d.batch = 1; d.M = M; d.N = N; d.K = K;
-    d.Mp = (int)rup(M, BM); d.Np = (int)rup(N, BN); d.Kp = (int)rup(K, BK);
+    const int BK = high ? High::BK : Low::BK;
+    d.Mp = (int)rup(M, BM); d.Np = (int)rup(N, BN); d.Kp = (int)rup(K, KPAD);
     d.Mi = M; d.Ni = N;
     d.c[0] = 0; d.c[1] = N; d.c[2] = 0; d.c[3] = 1; d.c[4] = 0;
     d.alpha = 1.0; d.beta = 1.0; d.C = dC; d.mol = 0;
     d.tiles_m = d.Mp / BM; d.tiles_n = d.Np / BN;
-    d.kb_per = d.Kp / BK;            // K <= 512: at most 8 k-blocks, never split
+    d.kb_per = d.Kp / BK;            // K <= 512: at most 16 k-blocks, never split
     d.ksplit = 1;
     d.tile_start = 0;
     d.expA = aexp; d.expB = bexp;
-    if ((rc = make_map(&d.mapA, abuf, (long long)S * d.Mp, d.Kp, BM)) != HX_OK) return rc;
-    if ((rc = make_map(&d.mapB, bbuf, (long long)S * d.Np, d.Kp, BN)) != HX_OK) return rc;
+    if ((rc = make_map(&d.mapA, abuf, (long long)S * d.Mp, d.Kp, BM, BK)) != HX_OK) return rc;
+    if ((rc = make_map(&d.mapB, bbuf, (long long)S * d.Np, d.Kp, BN, BK)) != HX_OK) return rc;
     PrepDesc p[2];
     memset(p, 0, sizeof(p));
     p[0].src = dA; p[0].dst = abuf; p[0].rexp = aexp; p[0].batch = 1; p[0].R = M; p[0].K = K;
@@ -1025,10 +1049,12 @@ extern "C" int hx_gemm_noalloc(const double *dA, const double *dB, double *dC, i
     p[1].src = dB; p[1].dst = bbuf; p[1].rexp = bexp; p[1].R = N; p[1].Rp = d.Np; p[1].Ri = N;
     p[0].rfast = prep_rfast(p[0]);
     p[1].rfast = prep_rfast(p[1]);
-    p[1].work_start = (long long)(d.Mp / PT_R) * (d.Kp / PT_K);
+    const long long atiles = (long long)((d.Mp + PT_R - 1) / PT_R) * (d.Kp / PT_K);
+    const long long btiles = (long long)((d.Np + PT_R - 1) / PT_R) * (d.Kp / PT_K);
+    p[1].work_start = atiles;
     p[1].row_start = d.Mp;
     const long long rows = (long long)d.Mp + d.Np;
-    const long long work = (rows / PT_R) * (d.Kp / PT_K);
+    const long long work = atiles + btiles;
     const long long tiles = (long long)d.tiles_m * d.tiles_n;
 
     // what must start at zero: the error word and C (accumulated with beta = 1)

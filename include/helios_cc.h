@@ -98,8 +98,9 @@ typedef struct hx_cc_params {
     int32_t precision;            /* HX_PRECISION_FP64 (default) or HX_PRECISION_MIXED */
     int32_t guess;                /* 0 reference guess (guessCC), 1 learned guess */
     double mixed_switch;          /* mixed precision: residual at which a molecule moves from
-                                     3-slice to 5-slice tensor-core iterations (1e-6); 5-slice
-                                     iterations run to 0.1 eps, then FP64 iterations confirm */
+                                     3-slice to 4-slice tensor-core iterations (1e-4); 4-slice
+                                     run to 1e-2 mixed_switch, then 5-slice; any of them hands
+                                     over to FP64 iterations below 0.1 eps */
     int32_t mixed_patience;       /* mixed precision: iterations without a new lowest residual
                                      after which a molecule moves on to the next phase (3) */
 } hx_cc_params;
@@ -187,9 +188,9 @@ int hx_ccsd_get_scf(hx_ccsd *h, int32_t mol, double *C, double *eps, double *fmo
 
 /* Per-iteration record of molecule mol's last solve: for each iteration
  * k < cap, out[5k..5k+4] = max|d1|, max|d2|, E_total, seconds since the start
- * of the solve, phase of the iteration (0 FP64 CUDA cores, 1 five-slice and
- * 2 three-slice tensor-core contractions). Returns the number of iterations
- * recorded. */
+ * of the solve, phase of the iteration (0 FP64 CUDA cores; 1, 2, 3: five-,
+ * four- and three-slice tensor-core contractions). Returns the number of
+ * iterations recorded. */
 int hx_ccsd_trace(hx_ccsd *h, int32_t mol, double *out, int32_t cap);
 
 /* Engine utility with no counterpart in the reference: device timing.
@@ -216,8 +217,9 @@ void hx_ccsd_destroy(hx_ccsd *h);
 /* Engine utility with no counterpart in the reference: C = A B^T for
  * row-major FP64 host matrices (A: M x K, B: N x K, C: M x N) on the engine's
  * FP64 CUDA-core GEMM (precision 0) or its exact-slice tcgen05 GEMM with
- * 3 slices (precision 1, about FP32 accuracy) or 5 slices (precision 2,
- * about FP64 accuracy); the launch is repeated reps times after one warm-up and
+ * 3 slices (precision 1, about 2^-24 of the row maxima), 5 slices (precision
+ * 2, about 2^-40) or 4 slices (precision 3, about 2^-32); the launch is
+ * repeated reps times after one warm-up and
  * *ms (if not NULL) receives the mean device time per launch. */
 int hx_gemm(const double *A, const double *B, double *C, int32_t M, int32_t N, int32_t K, int32_t precision,
             int32_t reps, double *ms);

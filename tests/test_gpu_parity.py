@@ -132,7 +132,7 @@ def test_mixed_trace_starts_on_tensor_cores(api):
     tr = cc.trace(0)
     cc.finalizeCC()
     assert r["status"] == 1
-    assert tr[0, 4] == 2.0 and tr[-1, 4] == 0.0          # 3-slice tensor cores first, FP64 last
+    assert tr[0, 4] == 3.0 and tr[-1, 4] == 0.0          # 3-slice tensor cores first, FP64 last
     assert np.all(np.diff(tr[:, 4]) <= 0)                 # phases only move towards FP64
     assert np.all(np.diff(tr[:, 3]) >= 0)
 
@@ -145,6 +145,8 @@ def test_tensor_core_gemm_accuracy(api):
         ref = A @ B.T
         C, _ = api.gemm(A, B, "mixed")
         assert np.abs(C - ref).max() / np.abs(ref).max() < 1e-6
+        C, _ = api.gemm(A, B, "mid")
+        assert np.abs(C - ref).max() / np.abs(ref).max() < 1e-8
         C, _ = api.gemm(A, B, "high")
         assert np.abs(C - ref).max() / np.abs(ref).max() < 1e-10
         C64, _ = api.gemm(A, B, "fp64")
