@@ -937,8 +937,11 @@ void destroy(Engine *e)
 // ------------------------------------------------------------------ allocation-free single GEMM
 // hx_gemm_noalloc: one C = A B^T on the tensor cores with every piece of
 // scratch (operand slices, row exponents, the error word, the descriptors) in
-// one file-scope device array, so that a call allocates no memory. Its size
-// bounds the problem: M, N, K <= HX_NOALLOC_MAX_DIM (512), about 5.3 MB.
+// one file-scope device array, so that a call allocates no memory: for hosts
+// whose device memory belongs to their own pool allocator, or that must not
+// let a cudaFree synchronise the device. Every GPU that loads the library
+// holds the array until exit; its size bounds the problem: M, N, K <=
+// HX_NOALLOC_MAX_DIM (512), about 5.3 MB.
 namespace tc {
 namespace {
 
@@ -960,7 +963,7 @@ constexpr size_t NA_OFF_TCD = na_rup(NA_OFF_ERR + sizeof(int), 256);
 constexpr size_t NA_OFF_PREP = na_rup(NA_OFF_TCD + sizeof(TcDesc), 256);
 constexpr size_t NA_BYTES = na_rup(NA_OFF_PREP + 2 * sizeof(PrepDesc), 256);
 
-__device__ __align__(256) unsigned char g_na_scratch[NA_BYTES];
+static __device__ __align__(256) unsigned char g_na_scratch[NA_BYTES];
 
 constexpr int NA_MAX_DEVICES = 64;
 std::mutex g_na_mutex;

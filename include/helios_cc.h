@@ -225,7 +225,11 @@ int hx_gemm(const double *A, const double *B, double *C, int32_t M, int32_t N, i
             int32_t reps, double *ms);
 
 /* Allocation-free variant of hx_gemm; it has no counterpart in the
- * reference. C = A B^T for row-major FP64 matrices already in DEVICE memory
+ * reference. For callers that cannot allocate device memory at call time: a
+ * host that has handed the device's memory to its own pool allocator (so
+ * cudaMalloc would fail), or code that must not stall work on other streams
+ * (cudaFree synchronises the whole device). C = A B^T for row-major FP64
+ * matrices already in DEVICE memory
  * (A: M x K, B: N x K, C: M x N), always on the tcgen05 exact-slice GEMM
  * (precision 1: 3 slices, 2: 5 slices; FP64 is rejected). It calls no
  * allocator: the operand slices, row exponents, error word and descriptors

@@ -1,6 +1,9 @@
 """hx_gemm_noalloc through the C ABI: the allocation-free tensor-core GEMM.
 
-Operands live in device memory (allocated here by torch, outside the call).
+It serves callers that cannot allocate device memory when they call it (their
+memory belongs to their own pool allocator, or a cudaFree would synchronise
+the device under other streams' work). Operands live in device memory
+(allocated here by torch, before and outside the call).
 Each call must give exactly hx_gemm's result for the same problem, twice in a
 row (the static scratch is reused), must not change the device's free memory,
 and must reject problems larger than the static scratch.
