@@ -200,6 +200,7 @@ struct hx_ccsd {
     std::vector<double> res;             // nmol x 6
     std::vector<Rules> rules;
     std::vector<int> status;
+    std::vector<int> scf_failed;         // batches: molecules whose SCF did not converge are left out
     tc::Engine *tce = nullptr;           // tensor-core backend (mixed precision)
     mlp::Model *model = nullptr;         // learned T2 guess (guess = 1)
     // mixed precision: per-molecule phase (PH_LOW / PH_MID / PH_HIGH
@@ -453,6 +454,7 @@ static int allocate(hx_ccsd *h)
     HX_CU(cudaMalloc(&h->d_part, sizeof(double) * std::max<size_t>((size_t)h->nmol * h->nblk * HX_MAX_DIIS, 2 * HX_SCF_GRID_MAX)));
     for (int ph = 0; ph < PH_COUNT; ++ph) HX_CU(cudaMalloc(&h->d_act_ph[ph], sizeof(int) * h->nmol));
     h->active.assign(h->nmol, 1);
+    h->scf_failed.assign(h->nmol, 0);
     h->phase.assign(h->nmol, PH_FP64);
     h->dcount.assign(h->nmol, 0);
     h->slot_phase.assign(h->nmol, {});
@@ -592,6 +594,7 @@ static int apply_learned_guess(hx_ccsd *h)
         return HX_ERR_STATE;
     }
     for (int mi = 0; mi < h->nmol; ++mi) {
+        if (h->scf_failed[mi]) continue;
         const long long ov = (long long)h->o[mi] * h->v[mi];
         HX_CU(h->model->apply(h->d_cc, mi, ov * (ov + 1) / 2, h->st));
     }
@@ -625,20 +628,32 @@ int hx_ccsd_init(hx_ccsd *h)
     std::vector<double> out(4);
     std::vector<int> st(2);
     HX_CU(cudaStreamSynchronize(h->st));
+    // one molecule: an SCF that does not converge is an error (as in the
+    // reference); in a batch the molecule is left out with status HX_ERR_SCF
+    int failed = 0;
     for (int mi = 0; mi < h->nmol; ++mi) {
         HX_CU(cudaMemcpy(out.data(), h->scf[mi].out, sizeof(double) * 4, cudaMemcpyDeviceToHost));
         HX_CU(cudaMemcpy(st.data(), h->scf[mi].status, sizeof(int) * 2, cudaMemcpyDeviceToHost));
-        if (st[0] != HX_CONVERGED) {
+        h->scf_failed[mi] = st[0] != HX_CONVERGED;
+        if (h->scf_failed[mi]) {
             hx_set_error("SCF of molecule %d ended with status %d after %d iterations (accuracy %.3e)", mi, st[0], st[1], out[3]);
-            return HX_ERR_SCF;
+            if (h->nmol == 1) return HX_ERR_SCF;
+            ++failed;
         }
         h->cc[mi].eref = out[0];
+        h->active[mi] = !h->scf_failed[mi];
     }
+    if (failed == h->nmol) return HX_ERR_SCF;
+    HX_TRY(upload_masks(h));
     HX_TRY(upload_views(h));
     HX_TRY(cc_setup(h, 1));
     if (h->p.guess == 1) HX_TRY(apply_learned_guess(h));
     if (h->tce) tc::invalidate(h->tce);          // new orbitals: re-slice the constant operands
-    for (int mi = 0; mi < h->nmol; ++mi) { h->rules[mi] = Rules(); h->status[mi] = 0; h->active[mi] = 1; }
+    for (int mi = 0; mi < h->nmol; ++mi) {
+        h->rules[mi] = Rules();
+        h->status[mi] = h->scf_failed[mi] ? HX_ERR_SCF : 0;
+        h->active[mi] = !h->scf_failed[mi];
+    }
     for (int mi = 0; mi < h->nmol; ++mi) {
         HX_CU(cudaMemsetAsync(h->diis[mi].count, 0, sizeof(int), h->st));
         diis_mirror_reset(h, mi);
@@ -869,7 +884,7 @@ static int solve_all(hx_ccsd *h, int maxiter, double eps)
     HX_CU(cudaEventSynchronize(h->ev[3]));
     cudaEventElapsedTime(&h->solve_ms, h->ev[2], h->ev[3]);
     // keep every molecule addressable for getters / energy after the solve
-    for (int mi = 0; mi < h->nmol; ++mi) { h->active[mi] = 1; h->phase[mi] = PH_FP64; }
+    for (int mi = 0; mi < h->nmol; ++mi) { h->active[mi] = !h->scf_failed[mi]; h->phase[mi] = PH_FP64; }
     HX_TRY(upload_masks(h));
     return HX_OK;
 }

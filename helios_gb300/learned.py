@@ -129,11 +129,21 @@ def main():
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--held-out", type=int, default=512)
     ap.add_argument("--out", default=os.path.dirname(MODEL_PATH))
+    ap.add_argument("--data", help="reuse rows saved by --save-data instead of generating them")
+    ap.add_argument("--save-data", help="write the generated rows (X, T) to this .npz")
+    ap.add_argument("--save-rows", type=int, default=1_000_000, help="rows written by --save-data")
     args = ap.parse_args()
     log = lambda m: print(m, flush=True)
     t0 = time.perf_counter()
-    X, T, used = generate(args.molecules, args.rows, log=log)
+    if args.data:
+        d = np.load(args.data)
+        X, T, used = d["X"], d["T"], int(d["molecules"])
+    else:
+        X, T, used = generate(args.molecules, args.rows, log=log)
     t_gen = time.perf_counter() - t0
+    if args.save_data:
+        keep = np.random.default_rng(1).permutation(len(T))[:args.save_rows]
+        np.savez_compressed(args.save_data, X=X[keep], T=T[keep], molecules=used)
     n_test = max(1, len(T) // 20)
     Xtr, Ttr, Xte, Tte = X[n_test:], T[n_test:], X[:n_test], T[:n_test]
     t1 = time.perf_counter()
@@ -149,17 +159,23 @@ def main():
               "rows_mse_reference_guess": zero, "rows_mse_learned_guess": mse(P, Xte, Tte),
               "features": FEATURES}
     if args.held_out > 0:
-        ev = evaluate(molecules.ensemble(HELD_OUT_SEED, args.held_out), P)
-        r, l = ev["reference"], ev["learned"]
-        ok = (r["status"] == 1) & (l["status"] == 1)
+        mols = molecules.ensemble(HELD_OUT_SEED, args.held_out)
         report["held_out"] = {"molecules": args.held_out, "seeds": [HELD_OUT_SEED, HELD_OUT_SEED + args.held_out - 1],
-                              "mean_iterations_reference": float(r["iterations"].mean()),
-                              "mean_iterations_learned": float(l["iterations"].mean()),
-                              "solve_s_reference": r["solve_s"], "solve_s_learned": l["solve_s"],
-                              "init_s_reference": r["init_s"], "init_s_learned": l["init_s"],
-                              "converged_both": int(ok.sum()),
-                              "max_abs_dE_eV": float(np.abs(r["energy"][ok] - l["energy"][ok]).max())}
-        log(json.dumps(report["held_out"]))
+                              "accuracy": 8}
+        for prec in ("fp64", "mixed"):
+            ev = evaluate(mols, P, accuracy=8, precision=prec)
+            r, l = ev["reference"], ev["learned"]
+            ok = (r["status"] == 1) & (l["status"] == 1)
+            report["held_out"][prec] = {
+                "mean_iterations_reference": float(r["iterations"][ok].mean()),
+                "mean_iterations_learned": float(l["iterations"][ok].mean()),
+                "fewer_iterations": int((l["iterations"] < r["iterations"])[ok].sum()),
+                "more_iterations": int((l["iterations"] > r["iterations"])[ok].sum()),
+                "solve_s_reference": r["solve_s"], "solve_s_learned": l["solve_s"],
+                "init_s_reference": r["init_s"], "init_s_learned": l["init_s"],
+                "converged_both": int(ok.sum()),
+                "max_abs_dE_eV": float(np.abs(r["energy"][ok] - l["energy"][ok]).max())}
+            log(prec + " " + json.dumps(report["held_out"][prec]))
     json.dump(report, open(os.path.join(args.out, "t2_guess.json"), "w"), indent=1)
 
 

@@ -118,7 +118,10 @@ int hx_ccsd_create(const hx_ppp_model *m, const hx_cc_params *p, hx_ccsd **out);
 int hx_ccsd_create_batch(const hx_ppp_model *ms, int32_t n, const hx_cc_params *p, hx_ccsd **out);
 
 /* initCC r-ccsd (mod_cc.f90:489-603, :538-558, guessCC :634-650): RHF SCF,
- * MO Fock, reference energy, integrals and the starting amplitudes. */
+ * MO Fock, reference energy, integrals and the starting amplitudes. An SCF
+ * that does not converge returns HX_ERR_SCF; in a batch such a molecule is
+ * left out instead (hx_ccsd_solve_batch reports HX_ERR_SCF as its status)
+ * and the call fails only if no SCF converged. */
 int hx_ccsd_init(hx_ccsd *h);
 
 /* Replace molecule mol's amplitudes (reference layout, see above). */
