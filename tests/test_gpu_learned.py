@@ -145,11 +145,31 @@ def test_engine_guess_is_guess_plus_prediction(api):
 
 @pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(__file__), "..", "helios_gb300", "data",
                                                     "t2_guess.npy")), reason="no trained model shipped")
-def test_shipped_model_saves_iterations_on_held_out_molecules(api):
+def test_shipped_model_gain_on_held_out_molecules(api):
+    """What the trained network gains over guessCC on molecules it never saw
+    (seeds outside its training range): a starting t2 several times closer to
+    the converged one, the same converged energies, and no more iterations.
+    (Measured on 512 held-out molecules, the closer start saves almost no
+    iterations: the singles, which start at zero either way, and the DIIS
+    history set the pace; helios_gb300/data/t2_guess.json has the numbers.)"""
     from helios_gb300 import learned
-    mols = molecules.ensemble(learned.HELD_OUT_SEED + 1000, 64)
-    ev = learned.evaluate(mols, learned.default_model(), accuracy=8, precision="mixed")
-    r, l = ev["reference"], ev["learned"]
-    assert np.all(r["status"] == 1) and np.all(l["status"] == 1)
-    assert np.abs(r["energy"] - l["energy"]).max() < 1e-6
-    assert l["iterations"].mean() < r["iterations"].mean()
+    mols = molecules.ensemble(learned.HELD_OUT_SEED + 1000, 16)
+    model = learned.default_model()
+    kw = dict(bond_alternation=0.1, accuracy=8)
+    ref = api.CoupledCluster(mols, api.Keywords(**kw))
+    ref.initCC()
+    start_ref = [ref.amplitudes(k)[1] for k in range(len(mols))]
+    out_ref = ref.solve_batch()
+    conv = [ref.amplitudes(k)[1] for k in range(len(mols))]
+    ref.finalizeCC()
+    lrn = api.CoupledCluster(mols, api.Keywords(guess="learned", model=model, **kw))
+    lrn.initCC()
+    start_lrn = [lrn.amplitudes(k)[1] for k in range(len(mols))]
+    out_lrn = lrn.solve_batch()
+    lrn.finalizeCC()
+    assert np.all(out_ref["status"] == 1) and np.all(out_lrn["status"] == 1)
+    assert np.abs(out_ref["energy"][:, 0] - out_lrn["energy"][:, 0]).max() < 1e-7
+    err_ref = np.sqrt(sum(np.sum((a - c) ** 2) for a, c in zip(start_ref, conv)))
+    err_lrn = np.sqrt(sum(np.sum((a - c) ** 2) for a, c in zip(start_lrn, conv)))
+    assert err_lrn < 0.4 * err_ref
+    assert out_lrn["iterations"].mean() <= out_ref["iterations"].mean() + 1.0
