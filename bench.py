@@ -161,11 +161,13 @@ def run_gb300(args):
     t0 = time.perf_counter()
     dev_ms, results, traces = [], [], []
     with Clocks(local) as clk:
+        torch.cuda.nvtx.range_push("timed")           # lets a profiler capture exactly the timed steps
         for _ in range(args.steps):
             r, tm = step()
             dev_ms.append(tm["init_ms"] + tm["solve_ms"])
             results.append(r)
             traces.append(cc.trace(0))
+        torch.cuda.nvtx.range_pop()
     barrier_sync()
     wall = time.perf_counter() - t0
     prof = cc.timing(profile=0)
