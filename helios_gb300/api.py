@@ -84,7 +84,7 @@ def library():
 
 def gemm(A, B, precision="fp64", reps=1):
     """C = A @ B.T on the engine's FP64 ("fp64") or tensor-core GEMM ("mixed": 3 slices,
-    "mid": 4 slices, "high": 5 slices); returns (C, ms per launch)."""
+    "mid": 4 slices, "high": 6 slices); returns (C, ms per launch)."""
     A = np.ascontiguousarray(A, dtype=np.float64)
     B = np.ascontiguousarray(B, dtype=np.float64)
     M, K = A.shape
@@ -170,7 +170,7 @@ class Keywords:
     precision: str = "fp64"                      # engine: "fp64" or "mixed"
     guess: str = "reference"                     # engine: "reference" (guessCC) or "learned"
     model: object = None                         # engine: learned-guess parameters (None = the shipped model)
-    mixed_switch: float = 1e-4                   # engine: residual where 3-slice hands over to 4-slice
+    mixed_switch: float = 1e-3                   # engine: residual where 3-slice hands over to 4-slice
     mixed_patience: int = 3                      # engine: non-improving iterations before the next phase
 
     def to_c(self) -> CCParams:
@@ -318,7 +318,7 @@ class CoupledCluster:
 
     def trace(self, mol: int = 0) -> np.ndarray:
         """Per-iteration (max|d1|, max|d2|, E_total, seconds, phase) of the last solve;
-        phase 3, 2, 1 = 3-, 4-, 5-slice tensor cores, 0 = FP64."""
+        phase 3, 2, 1 = 3-, 4-, 6-slice tensor cores, 0 = FP64."""
         n = _check(library().hx_ccsd_trace(self._h, mol, None, 0))
         out = np.zeros((max(n, 1), 5))
         library().hx_ccsd_trace(self._h, mol, out.ctypes.data_as(_c_d), n)

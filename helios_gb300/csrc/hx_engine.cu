@@ -207,6 +207,8 @@ struct hx_ccsd {
     // tensor-core iterations, PH_FP64 CUDA-core FP64) and one launch mask per phase
     std::vector<int> phase, stall;
     std::vector<double> best;
+    std::vector<double> fin_scale;       // mixed: tightening of the hand-over target after a failed FP64 check
+    std::vector<int> fp_returns;          // mixed: FP64 checks that sent a molecule back to 6-slice iterations
     // host mirror of each molecule's DIIS ring: pushes so far and the phase
     // that produced each slot (-1 empty or purged); residual at which each
     // phase ended (0 = not ended, -1 = its vectors purged)
@@ -461,6 +463,8 @@ static int allocate(hx_ccsd *h)
     h->ph_end.assign(h->nmol, {0.0, 0.0, 0.0, 0.0});
     h->stall.assign(h->nmol, 0);
     h->best.assign(h->nmol, 1e300);
+    h->fin_scale.assign(h->nmol, 1.0);
+    h->fp_returns.assign(h->nmol, 0);
     h->trace.assign(h->nmol, {});
     h->res.assign((size_t)h->nmol * 8, 0.0);
     h->status.assign(h->nmol, 0);
@@ -502,7 +506,7 @@ void hx_cc_params_default(hx_cc_params *p)
     p->stagnation_after = 200;
     p->precision = HX_PRECISION_FP64;
     p->guess = 0;
-    p->mixed_switch = 1e-4;
+    p->mixed_switch = 1e-3;
     p->mixed_patience = 3;
 }
 
@@ -792,9 +796,13 @@ static int diis_purge(hx_ccsd *h, int mi, double a)
 //   LOW   3-slice tensor-core contractions (about 2^-24 of the operands' row
 //         maxima) until the residual falls below mixed_switch;
 //   MID   4-slice (about 2^-32) until it falls below kMidSpan * mixed_switch;
-//   HIGH  5-slice (about 2^-40: residuals as accurate as FP64 ones);
+//   HIGH  6-slice (about 2^-46: residuals as accurate as FP64 ones);
 //   FP64  CUDA-core FP64 iterations: convergence is declared only here, so the
-//         final residual and energy are plain FP64 (the defect correction).
+//         final residual and energy are plain FP64 (the defect correction). An
+//         FP64 residual that does not confirm convergence sends the molecule
+//         back to 6-slice iterations with a 10x tighter hand-over target (at
+//         most kMaxFp64Returns times): an FP64 iteration costs as much as
+//         tens of 6-slice ones.
 // Every tensor-core phase hands over to FP64 once the residual is below
 // kHighMargin * eps (the iteration is not monotone, and one more
 // tensor-core iteration costs far less than an FP64 iteration whose
@@ -804,7 +812,8 @@ static int diis_purge(hx_ccsd *h, int mi, double a)
 // the DIIS history restarts (its error vectors are then too noisy to mix
 // with more accurate ones).
 static const double kHighMargin = 0.1;
-static const double kMidSpan = 1e-2;
+static const double kMidSpan = 1e-3;
+static const int kMaxFp64Returns = 3;
 
 static int solve_all(hx_ccsd *h, int maxiter, double eps)
 {
@@ -816,6 +825,8 @@ static int solve_all(hx_ccsd *h, int maxiter, double eps)
         h->phase[mi] = mixed ? PH_LOW : PH_FP64;
         h->stall[mi] = 0;
         h->best[mi] = 1e300;
+        h->fin_scale[mi] = 1.0;
+        h->fp_returns[mi] = 0;
         h->trace[mi].clear();
     }
     HX_TRY(upload_masks(h));
@@ -847,7 +858,7 @@ static int solve_all(hx_ccsd *h, int maxiter, double eps)
             if (ph != PH_FP64 && !cancel) {
                 // tensor-core phases never claim convergence: they hand over
                 if (a < h->best[mi]) { h->best[mi] = a; h->stall[mi] = 0; } else ++h->stall[mi];
-                const double fin = kHighMargin * eps;
+                const double fin = kHighMargin * h->fin_scale[mi] * eps;
                 const double below = ph == PH_LOW ? h->p.mixed_switch : ph == PH_MID ? kMidSpan * h->p.mixed_switch : 0.0;
                 const bool stalled = h->stall[mi] >= h->p.mixed_patience;
                 int next = ph;
@@ -863,7 +874,7 @@ static int solve_all(hx_ccsd *h, int maxiter, double eps)
                     h->best[mi] = 1e300;
                     changed = true;
                     h->ph_end[mi][ph] = a;
-                    if (stalled && a >= fin) {
+                    if (stalled && a >= fin && ph != PH_HIGH) {
                         HX_CU(cudaMemsetAsync(h->diis[mi].count, 0, sizeof(int), h->st));
                         diis_mirror_reset(h, mi);
                     }
@@ -875,6 +886,15 @@ static int solve_all(hx_ccsd *h, int maxiter, double eps)
                 h->status[mi] = s;
                 h->active[mi] = 0;
                 --remaining;
+                changed = true;
+            } else if (mixed && h->fp_returns[mi] < kMaxFp64Returns) {
+                // the FP64 check did not confirm convergence: more 6-slice
+                // iterations to a 10x tighter target, then check again
+                h->phase[mi] = PH_HIGH;
+                h->fin_scale[mi] *= 0.1;
+                ++h->fp_returns[mi];
+                h->stall[mi] = 0;
+                h->best[mi] = 1e300;
                 changed = true;
             }
         }

@@ -63,10 +63,14 @@ namespace tc {
 // for a chunk of depth K) is scaled down by 2^-8NX.
 //   LOW:  3 slices, pairs i + j <= 3 (8 MMAs per k-step), NX = 1: about 2^-24
 //         of the row maxima; 128 x 96 tiles.
-//   MID:  4 slices, pairs i + j <= 3 (10 MMAs), NX = 2: about 2^-32; 128 x 80.
-//   HIGH: 5 slices, pairs i + j <= 5 (19 MMAs), NX = 3: about 2^-40; residuals
-//         as accurate as FP64 ones; 128 x 64 tiles fed by 32-deep k-blocks
-//         (64-byte swizzle) so that three stages of five slices fit.
+//   MID:  4 slices, pairs i + j <= 3 (10 MMAs), NX = 3: about 2^-32; 128 x 64.
+//   HIGH: 6 slices, pairs i + j <= 5 (21 MMAs), NX = 4: about 2^-46 of the row
+//         maxima; 128 x 48 tiles fed by 32-deep k-blocks (64-byte swizzle) so
+//         that three stages of six slices fit.
+// The shared accumulator is what limits MID and HIGH: measured at 6400^3, one
+// exact class more (NX 3 -> 4) took HIGH from 5.6e-12 to 1.6e-13 relative
+// error, and these errors set the residual level a phase can reach (the
+// GEMM outputs are ~1e3-1e4 times the residual they cancel down to).
 template <int S_, int QMAX_, int NX_, int BN_, int STAGES_, int KC_, int EPIW_, int BK_ = 64>
 struct Cfg {
     static constexpr int S = S_;                     // integer slices per FP64 operand
@@ -99,8 +103,8 @@ struct Cfg {
     static_assert(128 * (BN_ + 1) * 8 <= STAGES_ * STAGE_BYTES, "output tile staging fits in the TMA ring");
 };
 using Low = Cfg<3, 3, 1, 96, 2, 8, 12>;
-using Mid = Cfg<4, 3, 2, 80, 2, 6, 8>;
-using High = Cfg<5, 5, 3, 64, 3, 8, 8, 32>;
+using Mid = Cfg<4, 3, 3, 64, 2, 5, 8>;
+using High = Cfg<6, 5, 4, 48, 3, 7, 8, 32>;
 constexpr int TMEM_COLS = 512;
 constexpr int BM = 128, KPAD = 64;   // K is padded to KPAD (the slicing tile depth)
 constexpr unsigned long long WAIT_NS = 4000000000ull; // a wait longer than 4 s is declared failed
@@ -608,7 +612,7 @@ struct Engine {
     __nv_bfloat16 *scratch = nullptr;   // slices of the variable operands (shared by groups and modes)
     int *rexp = nullptr;
     int *d_err = nullptr;
-    Mode mode[3];                        // 0 = LOW, 1 = MID, 2 = HIGH (3, 4, 5 slices)
+    Mode mode[3];                        // 0 = LOW, 1 = MID, 2 = HIGH (3, 4, 6 slices)
     std::vector<const Group *> keys;
     bool profile = false;
     int generation = 0;
@@ -941,7 +945,7 @@ void destroy(Engine *e)
 // whose device memory belongs to their own pool allocator, or that must not
 // let a cudaFree synchronise the device. Every GPU that loads the library
 // holds the array until exit; its size bounds the problem: M, N, K <=
-// HX_NOALLOC_MAX_DIM (512), about 5.3 MB.
+// HX_NOALLOC_MAX_DIM (512), about 6.4 MB.
 namespace tc {
 namespace {
 
@@ -1011,7 +1015,7 @@ extern "C" int hx_gemm_noalloc(const double *dA, const double *dB, double *dC, i
         return HX_ERR_ARG;
     }
     if (precision != HX_PRECISION_MIXED && precision != 2) {
-        hx_set_error("hx_gemm_noalloc: precision must be 1 (3 slices) or 2 (5 slices)");
+        hx_set_error("hx_gemm_noalloc: precision must be 1 (3 slices) or 2 (6 slices)");
         return HX_ERR_ARG;
     }
     unsigned char *base = nullptr;

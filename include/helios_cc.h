@@ -98,8 +98,8 @@ typedef struct hx_cc_params {
     int32_t precision;            /* HX_PRECISION_FP64 (default) or HX_PRECISION_MIXED */
     int32_t guess;                /* 0 reference guess (guessCC), 1 learned guess */
     double mixed_switch;          /* mixed precision: residual at which a molecule moves from
-                                     3-slice to 4-slice tensor-core iterations (1e-4); 4-slice
-                                     run to 1e-2 mixed_switch, then 5-slice; any of them hands
+                                     3-slice to 4-slice tensor-core iterations (1e-3); 4-slice
+                                     run to 1e-3 mixed_switch, then 6-slice; any of them hands
                                      over to FP64 iterations below 0.1 eps */
     int32_t mixed_patience;       /* mixed precision: iterations without a new lowest residual
                                      after which a molecule moves on to the next phase (3) */
@@ -191,7 +191,7 @@ int hx_ccsd_get_scf(hx_ccsd *h, int32_t mol, double *C, double *eps, double *fmo
 
 /* Per-iteration record of molecule mol's last solve: for each iteration
  * k < cap, out[5k..5k+4] = max|d1|, max|d2|, E_total, seconds since the start
- * of the solve, phase of the iteration (0 FP64 CUDA cores; 1, 2, 3: five-,
+ * of the solve, phase of the iteration (0 FP64 CUDA cores; 1, 2, 3: six-,
  * four- and three-slice tensor-core contractions). Returns the number of
  * iterations recorded. */
 int hx_ccsd_trace(hx_ccsd *h, int32_t mol, double *out, int32_t cap);
@@ -220,8 +220,8 @@ void hx_ccsd_destroy(hx_ccsd *h);
 /* Engine utility with no counterpart in the reference: C = A B^T for
  * row-major FP64 host matrices (A: M x K, B: N x K, C: M x N) on the engine's
  * FP64 CUDA-core GEMM (precision 0) or its exact-slice tcgen05 GEMM with
- * 3 slices (precision 1, about 2^-24 of the row maxima), 5 slices (precision
- * 2, about 2^-40) or 4 slices (precision 3, about 2^-32); the launch is
+ * 3 slices (precision 1, about 2^-24 of the row maxima), 6 slices (precision
+ * 2, about 2^-46) or 4 slices (precision 3, about 2^-32); the launch is
  * repeated reps times after one warm-up and
  * *ms (if not NULL) receives the mean device time per launch. */
 int hx_gemm(const double *A, const double *B, double *C, int32_t M, int32_t N, int32_t K, int32_t precision,
@@ -234,9 +234,9 @@ int hx_gemm(const double *A, const double *B, double *C, int32_t M, int32_t N, i
  * (cudaFree synchronises the whole device). C = A B^T for row-major FP64
  * matrices already in DEVICE memory
  * (A: M x K, B: N x K, C: M x N), always on the tcgen05 exact-slice GEMM
- * (precision 1: 3 slices, 2: 5 slices; FP64 is rejected). It calls no
+ * (precision 1: 3 slices, 2: 6 slices; FP64 is rejected). It calls no
  * allocator: the operand slices, row exponents, error word and descriptors
- * live in one static device array of about 5.3 MB, whose address is looked
+ * live in one static device array of about 6.4 MB, whose address is looked
  * up once per device (cudaGetSymbolAddress) on the first call; make that
  * first call before any stream capture. Dimensions above
  * HX_NOALLOC_MAX_DIM return HX_ERR_ARG. C is zeroed and accumulated on

@@ -133,7 +133,10 @@ def test_mixed_trace_starts_on_tensor_cores(api):
     cc.finalizeCC()
     assert r["status"] == 1
     assert tr[0, 4] == 3.0 and tr[-1, 4] == 0.0          # 3-slice tensor cores first, FP64 last
-    assert np.all(np.diff(tr[:, 4]) <= 0)                 # phases only move towards FP64
+    d = np.diff(tr[:, 4])
+    # phases only move towards FP64, except that an FP64 check which does not
+    # confirm convergence sends the molecule back to 6-slice iterations
+    assert np.all((d <= 0) | ((d == 1) & (tr[:-1, 4] == 0)))
     assert np.all(np.diff(tr[:, 3]) >= 0)
 
 
@@ -148,7 +151,7 @@ def test_tensor_core_gemm_accuracy(api):
         C, _ = api.gemm(A, B, "mid")
         assert np.abs(C - ref).max() / np.abs(ref).max() < 1e-8
         C, _ = api.gemm(A, B, "high")
-        assert np.abs(C - ref).max() / np.abs(ref).max() < 1e-10
+        assert np.abs(C - ref).max() / np.abs(ref).max() < 1e-12
         C64, _ = api.gemm(A, B, "fp64")
         assert np.abs(C64 - ref).max() / np.abs(ref).max() < 1e-13
 
