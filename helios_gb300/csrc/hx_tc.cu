@@ -63,14 +63,15 @@ namespace tc {
 // for a chunk of depth K) is scaled down by 2^-8NX.
 //   LOW:  3 slices, pairs i + j <= 3 (8 MMAs per k-step), NX = 1: about 2^-24
 //         of the row maxima; 128 x 96 tiles.
-//   MID:  4 slices, pairs i + j <= 3 (10 MMAs), NX = 3: about 2^-32; 128 x 64.
+//   MID:  4 slices, pairs i + j <= 3 (10 MMAs), NX = 2: about 2^-32; 128 x 80.
 //   HIGH: 6 slices, pairs i + j <= 5 (21 MMAs), NX = 4: about 2^-46 of the row
 //         maxima; 128 x 48 tiles fed by 32-deep k-blocks (64-byte swizzle) so
 //         that three stages of six slices fit.
-// The shared accumulator is what limits MID and HIGH: measured at 6400^3, one
-// exact class more (NX 3 -> 4) took HIGH from 5.6e-12 to 1.6e-13 relative
-// error, and these errors set the residual level a phase can reach (the
-// GEMM outputs are ~1e3-1e4 times the residual they cancel down to).
+// The shared accumulator is what limits HIGH: measured at 6400^3, one exact
+// class more (NX 3 -> 4) took it from 5.6e-12 to 1.6e-13 relative error,
+// while a sixth slice alone changed nothing; LOW and MID are limited by their
+// slices. These errors set the residual level a phase can reach (the GEMM
+// outputs are ~1e3-1e4 times the residual they cancel down to).
 template <int S_, int QMAX_, int NX_, int BN_, int STAGES_, int KC_, int EPIW_, int BK_ = 64>
 struct Cfg {
     static constexpr int S = S_;                     // integer slices per FP64 operand
@@ -103,7 +104,7 @@ struct Cfg {
     static_assert(128 * (BN_ + 1) * 8 <= STAGES_ * STAGE_BYTES, "output tile staging fits in the TMA ring");
 };
 using Low = Cfg<3, 3, 1, 96, 2, 8, 12>;
-using Mid = Cfg<4, 3, 3, 64, 2, 5, 8>;
+using Mid = Cfg<4, 3, 2, 80, 2, 6, 8>;
 using High = Cfg<6, 5, 4, 48, 3, 7, 8, 32>;
 constexpr int TMEM_COLS = 512;
 constexpr int BM = 128, KPAD = 64;   // K is padded to KPAD (the slicing tile depth)
@@ -301,6 +302,7 @@ __device__ __forceinline__ bool load_tile(const PrepDesc *__restrict__ pd, int n
     }
     __syncthreads();
     const int rlim = d.R - r0, klim = d.K - k0;
+#pragma unroll
     for (int e = threadIdx.x; e < PT_R * PT_K; e += PT_THREADS) {
         int rr, kk;
         if (d.rfast) { rr = e % PT_R; kk = e / PT_R; } else { kk = e % PT_K; rr = e / PT_K; }
