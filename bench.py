@@ -270,6 +270,27 @@ def run_gb300(args):
                 "tensor_issued_frac_while_in_tc_gemm": tw["gemm_hw_flops"] / (tw["gemm_ms"] * 1e-3 * peak_t)
                 if tw["gemm_ms"] > 0 else None,
                 "tc_gemm_share_of_batch_time": tw["gemm_ms"] * 1e-3 / wsecs if wsecs > 0 else None}
+    # --- finite-field alpha_xx of the 2 x 32 ladder: five field points solved as one batch
+    if args.polariz:
+        from helios_gb300 import polariz
+        lad = molecules.ladder(64)
+        step = 1e-4 * polariz.AU_FIELD        # 1e-4 a.u.: 1e-3 a.u. stalls the reference SCF on this molecule
+        res = {}
+        for label, kwp, seed in (("mixed", api.Keywords(bond_alternation=0.1, accuracy=10, precision="mixed",
+                                                        guess=guess), True),
+                                 ("fp64", api.Keywords(bond_alternation=0.1, accuracy=10, precision="fp64"), False)):
+            t0p = time.perf_counter()
+            pr = polariz.polarizability(lad, kwp, points=5, step=step, seed=seed)
+            res[label] = {"alpha_xx": float(pr["alpha"]), "seconds": time.perf_counter() - t0p,
+                          "iterations": [int(x) for x in pr["iterations"]], "status": [int(x) for x in pr["status"]]}
+        gp = os.path.join(ROOT, "tests", "golden", "polariz64.json")
+        a_or = json.load(open(gp))["alpha_xx"] if os.path.exists(gp) else None
+        extra["polarizability"] = {"molecule": "ladder-64 (2 x 32)", "field_au": 1e-4, "points": 5, **res,
+                                   "alpha_fp64_oracle": a_or,
+                                   "rel_diff_mixed_vs_fp64": abs(res["mixed"]["alpha_xx"] - res["fp64"]["alpha_xx"])
+                                   / abs(res["fp64"]["alpha_xx"]),
+                                   "rel_diff_mixed_vs_oracle": None if a_or is None
+                                   else abs(res["mixed"]["alpha_xx"] - a_or) / abs(a_or)}
     # --- end to end through the C ABI with host buffers
     e2e = run_e2e(api, mol, kw, max(1, min(args.steps, 3)))
     # --- roofline of the tcgen05 GEMM, live over the timed steps
@@ -446,6 +467,7 @@ def main():
     ap.add_argument("--batch", type=int, default=512, help="molecules of the ensemble leg (0 = skip)")
     ap.add_argument("--no-fp64-compare", dest="fp64_compare", action="store_false")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-polariz", dest="polariz", action="store_false", help="skip the polarizability leg")
     ap.add_argument("--ref-pairs", type=int, default=48, help="doubles pairs per reference-arm step")
     args = ap.parse_args()
     if args.warmup < 3:
