@@ -290,28 +290,28 @@ class CoupledCluster:
         rows = np.ascontiguousarray(rows, dtype=np.int64)
         X = np.zeros((rows.size, 8), dtype=np.float32)
         T = np.zeros(rows.size, dtype=np.float32)
-        _check(library().hx_ccsd_training_rows(self._h, mol, rows.size, rows.ctypes.data_as(_c_l),
+        _check(library().hx_ccsd_training_rows(self._h, int(mol), rows.size, rows.ctypes.data_as(_c_l),
                                                X.ctypes.data_as(_c_f), T.ctypes.data_as(_c_f)))
         return X, T
 
     def set_guess(self, mol: int, t1, t2):
         t1 = np.asfortranarray(t1, dtype=np.float64)
         t2 = np.asfortranarray(t2, dtype=np.float64)
-        _check(library().hx_ccsd_set_guess(self._h, mol, t1.ctypes.data_as(_c_d), t2.ctypes.data_as(_c_d)))
+        _check(library().hx_ccsd_set_guess(self._h, int(mol), t1.ctypes.data_as(_c_d), t2.ctypes.data_as(_c_d)))
 
     def amplitudes(self, mol: int = 0):
         """t1 (o, v) and t2 (o, o, v, v) as numpy arrays indexed like the reference."""
         N, o, v, _ = self.dims[mol]
         t1 = np.zeros((o, v), order="F")
         t2 = np.zeros((o, o, v, v), order="F")
-        _check(library().hx_ccsd_get_amplitudes(self._h, mol, t1.ctypes.data_as(_c_d), t2.ctypes.data_as(_c_d)))
+        _check(library().hx_ccsd_get_amplitudes(self._h, int(mol), t1.ctypes.data_as(_c_d), t2.ctypes.data_as(_c_d)))
         return t1, t2
 
     def scf(self, mol: int = 0):
         N = self.dims[mol][0]
         C = np.zeros((N, N)); eps = np.zeros(N); fmo = np.zeros((N, N)); out = np.zeros(4)
         st = np.zeros(2, dtype=np.int32)
-        _check(library().hx_ccsd_get_scf(self._h, mol, C.ctypes.data_as(_c_d), eps.ctypes.data_as(_c_d),
+        _check(library().hx_ccsd_get_scf(self._h, int(mol), C.ctypes.data_as(_c_d), eps.ctypes.data_as(_c_d),
                                          fmo.ctypes.data_as(_c_d), out.ctypes.data_as(_c_d), st.ctypes.data_as(_c_i)))
         return {"C": C, "eps": eps, "F": fmo, "energy": out[0], "eel": out[1], "enuc": out[2],
                 "accuracy": out[3], "status": int(st[0]), "iterations": int(st[1])}
@@ -319,9 +319,9 @@ class CoupledCluster:
     def trace(self, mol: int = 0) -> np.ndarray:
         """Per-iteration (max|d1|, max|d2|, E_total, seconds, phase) of the last solve;
         phase 3, 2, 1 = 3-, 4-, 6-slice tensor cores, 0 = FP64."""
-        n = _check(library().hx_ccsd_trace(self._h, mol, None, 0))
+        n = _check(library().hx_ccsd_trace(self._h, int(mol), None, 0))
         out = np.zeros((max(n, 1), 5))
-        library().hx_ccsd_trace(self._h, mol, out.ctypes.data_as(_c_d), n)
+        library().hx_ccsd_trace(self._h, int(mol), out.ctypes.data_as(_c_d), n)
         return out[:n]
 
     def timing(self, profile: int = -1) -> dict:

@@ -232,16 +232,20 @@ __global__ void k_step_finish(const CCMol *mols, const int *active, const double
 }
 
 // ---------------------------------------------------------------- DIIS
+// gate[mol]: the DIIS step runs while max(|d1|,|d2|) >= gate[mol]. The
+// reference stops mixing once the residual is below the convergence target
+// (there the iteration ends); FP64 iterations use that target, tensor-core
+// iterations (which hand over rather than converge) their hand-over target.
 // Weighted dots of the newest error vector with every stored one. The doubles
 // part is a symmetric pair matrix; the reference's vectors hold only the pairs
 // (ia) <= (jb), so off-diagonal products count 1/2 and diagonal ones 1.
-__global__ void k_diis_dots(const CCMol *mols, const DiisMol *diis, const int *active, double eps,
+__global__ void k_diis_dots(const CCMol *mols, const DiisMol *diis, const int *active, const double *gate,
                             double *part, int nblk)
 {
     if (skip(active)) return;
     const CCMol &m = mols[blockIdx.y];
     const DiisMol &h = diis[blockIdx.y];
-    if (!(fmax(m.res[0], m.res[1]) >= eps)) return;      // converged: the reference skips DIIS
+    if (!(fmax(m.res[0], m.res[1]) >= gate[blockIdx.y])) return;      // converged: the reference skips DIIS
     const long long ov = (long long)m.o * m.v;
     const int cnt = h.count[0] + 1, n = cnt < h.nd ? cnt : h.nd;
     const int k = blockIdx.z;                             // stored vector of this block
@@ -265,14 +269,14 @@ __global__ void k_diis_dots(const CCMol *mols, const DiisMol *diis, const int *a
 // Ordered sum of the partial dots into the Gram matrix (slot indexing), then
 // the bordered DIIS system solved by Gaussian elimination with partial
 // pivoting (one thread per molecule). Coefficients go to h.coef[slot].
-__global__ void k_diis_solve(const CCMol *mols, const DiisMol *diis, const int *active, double eps,
+__global__ void k_diis_solve(const CCMol *mols, const DiisMol *diis, const int *active, const double *gate,
                              const double *part, int nblk)
 {
     const int mol = blockIdx.x;
     if (active && !active[mol]) return;
     const CCMol &m = mols[mol];
     const DiisMol &h = diis[mol];
-    if (!(fmax(m.res[0], m.res[1]) >= eps)) return;
+    if (!(fmax(m.res[0], m.res[1]) >= gate[mol])) return;
     const int cnt = h.count[0] + 1, n = cnt < h.nd ? cnt : h.nd;
     const int slot = h.count[0] % h.nd;
     __shared__ double g[HX_MAX_DIIS];
@@ -328,12 +332,12 @@ __global__ void k_diis_solve(const CCMol *mols, const DiisMol *diis, const int *
 }
 
 // t = sum_k c_k Ht[k]
-__global__ void k_diis_extrapolate(const CCMol *mols, const DiisMol *diis, const int *active, double eps)
+__global__ void k_diis_extrapolate(const CCMol *mols, const DiisMol *diis, const int *active, const double *gate)
 {
     if (skip(active)) return;
     const CCMol &m = mols[blockIdx.y];
     const DiisMol &h = diis[blockIdx.y];
-    if (!(fmax(m.res[0], m.res[1]) >= eps)) return;
+    if (!(fmax(m.res[0], m.res[1]) >= gate[blockIdx.y])) return;
     const int n = (int)h.coef[HX_MAX_DIIS];
     if (n < 2) return;
     const long long ov = (long long)m.o * m.v;
@@ -501,17 +505,17 @@ cudaError_t hx_step(const CCMol *m, const DiisMol *h, const int *act, int nmol, 
     return cudaGetLastError();
 }
 
-cudaError_t hx_diis(const CCMol *m, const DiisMol *h, const int *act, int nmol, double eps, double *part,
+cudaError_t hx_diis(const CCMol *m, const DiisMol *h, const int *act, int nmol, const double *gate, double *part,
                     int nblk, int nd_max, cudaStream_t s)
 {
-    k_diis_dots<<<dim3(nblk, nmol, nd_max), NT, 0, s>>>(m, h, act, eps, part, nblk);
+    k_diis_dots<<<dim3(nblk, nmol, nd_max), NT, 0, s>>>(m, h, act, gate, part, nblk);
     hx_count_launches(3);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_diis_solve<<<nmol, 32, 0, s>>>(m, h, act, eps, part, nblk);
+    k_diis_solve<<<nmol, 32, 0, s>>>(m, h, act, gate, part, nblk);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_diis_extrapolate<<<dim3(nblk, nmol), NT, 0, s>>>(m, h, act, eps);
+    k_diis_extrapolate<<<dim3(nblk, nmol), NT, 0, s>>>(m, h, act, gate);
     return cudaGetLastError();
 }
 

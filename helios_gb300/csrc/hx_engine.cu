@@ -188,6 +188,9 @@ struct hx_ccsd {
     DiisMol *d_diis = nullptr;
     int *d_active = nullptr;
     std::vector<int> active;
+    double *d_gate = nullptr;            // per molecule: residual below which the DIIS step is skipped
+    std::vector<double> gate;
+    double gate_eps = 0.0;               // convergence target the gates were made for
     double *d_part = nullptr;
     double *d_res = nullptr;             // nmol x 8 iteration results (inside the arena)
     int nblk = 64;                       // blocks per molecule of the reductions (set at allocation)
@@ -290,8 +293,23 @@ static int run_group(hx_ccsd *h, Group &g)
     return HX_OK;
 }
 
+// Mixed precision: a tensor-core phase hands over to FP64 once its residual
+// is below kHighMargin * eps (times the molecule's fin_scale).
+static const double kHighMargin = 0.1;
+// A tensor-core phase keeps the DIIS extrapolation down to its hand-over
+// target: below eps, plain steps (the reference's converged case) throw the
+// residual back up by several times and the phase wanders for tens of
+// iterations before it reaches kHighMargin * eps.
+static double diis_gate(const hx_ccsd *h, int mi)
+{
+    if (h->tce && h->phase[mi] != PH_FP64) return kHighMargin * h->fin_scale[mi] * h->gate_eps;
+    return h->gate_eps;
+}
+
 static int upload_masks(hx_ccsd *h)
 {
+    for (int mi = 0; mi < h->nmol; ++mi) h->gate[mi] = diis_gate(h, mi);
+    HX_CU(cudaMemcpyAsync(h->d_gate, h->gate.data(), sizeof(double) * h->nmol, cudaMemcpyHostToDevice, h->st));
     std::vector<int> m((size_t)PH_COUNT * h->nmol);
     for (int ph = 0; ph < PH_COUNT; ++ph)
         for (int mi = 0; mi < h->nmol; ++mi) m[(size_t)ph * h->nmol + mi] = h->active[mi] && h->phase[mi] == ph;
@@ -300,7 +318,7 @@ static int upload_masks(hx_ccsd *h)
         for (int ph = 0; ph < PH_COUNT; ++ph)
             HX_CU(cudaMemcpyAsync(h->d_act_ph[ph], &m[(size_t)ph * h->nmol], sizeof(int) * h->nmol,
                                   cudaMemcpyHostToDevice, h->st));
-    // the masks are pageable host vectors: wait so they may go out of scope
+    // the masks and gates are pageable host vectors: wait so they may change
     HX_CU(cudaStreamSynchronize(h->st));
     return HX_OK;
 }
@@ -455,6 +473,8 @@ static int allocate(hx_ccsd *h)
     h->nblk = (int)std::max<long long>(1, std::min<long long>(std::max(1, 1216 / h->nmol), (maxpair + 4095) / 4096));
     HX_CU(cudaMalloc(&h->d_part, sizeof(double) * std::max<size_t>((size_t)h->nmol * h->nblk * HX_MAX_DIIS, 2 * HX_SCF_GRID_MAX)));
     for (int ph = 0; ph < PH_COUNT; ++ph) HX_CU(cudaMalloc(&h->d_act_ph[ph], sizeof(int) * h->nmol));
+    HX_CU(cudaMalloc(&h->d_gate, sizeof(double) * h->nmol));
+    h->gate.assign(h->nmol, 0.0);
     h->active.assign(h->nmol, 1);
     h->scf_failed.assign(h->nmol, 0);
     h->phase.assign(h->nmol, PH_FP64);
@@ -673,6 +693,7 @@ int hx_ccsd_init(hx_ccsd *h)
 // One iterationCC for every active molecule (no host synchronisation).
 static int iteration_body(hx_ccsd *h, double eps)
 {
+    if (eps != h->gate_eps) { h->gate_eps = eps; HX_TRY(upload_masks(h)); }
     const int nm = h->nmol;
     auto &P = h->plan;
     int k = 0;
@@ -715,7 +736,7 @@ static int iteration_body(hx_ccsd *h, double eps)
     HX_TRY(run_group(h, P[k++]));                                    // r1 -= Boo UG
     const int use_diis = h->p.diis_enabled ? 1 : 0;
     HX_CU(hx_step(h->d_cc, h->d_diis, h->d_active, nm, h->p.t1_step, h->p.t2_step, use_diis, h->d_part, h->nblk, h->st));
-    if (use_diis) HX_CU(hx_diis(h->d_cc, h->d_diis, h->d_active, nm, eps, h->d_part, h->nblk, h->p.diis_steps, h->st));
+    if (use_diis) HX_CU(hx_diis(h->d_cc, h->d_diis, h->d_active, nm, h->d_gate, h->d_part, h->nblk, h->p.diis_steps, h->st));
     HX_CU(hx_energy(h->d_cc, h->d_active, nm, h->d_part, h->nblk, h->st));
     return HX_OK;
 }
@@ -811,7 +832,6 @@ static int diis_purge(hx_ccsd *h, int mi, double a)
 // that stops improving for mixed_patience iterations hands over early and
 // the DIIS history restarts (its error vectors are then too noisy to mix
 // with more accurate ones).
-static const double kHighMargin = 0.1;
 static const double kMidSpan = 1e-3;
 static const int kMaxFp64Returns = 3;
 
@@ -829,6 +849,7 @@ static int solve_all(hx_ccsd *h, int maxiter, double eps)
         h->fp_returns[mi] = 0;
         h->trace[mi].clear();
     }
+    h->gate_eps = eps;
     HX_TRY(upload_masks(h));
     const auto t0 = std::chrono::steady_clock::now();
     HX_CU(cudaEventRecord(h->ev[2], h->st));
@@ -849,7 +870,7 @@ static int solve_all(hx_ccsd *h, int maxiter, double eps)
             const double a = std::max(r[0], r[1]);
             const int ph = h->phase[mi];
             h->trace[mi].push_back({r[0], r[1], r[2], secs, (double)ph});
-            if (h->p.diis_enabled && a >= eps) {          // the step pushed (t, error) into the ring
+            if (h->p.diis_enabled && a >= h->gate[mi]) {  // the step pushed (t, error) into the ring
                 const int nd = h->diis[mi].nd;
                 h->slot_phase[mi][(size_t)(h->dcount[mi] % nd)] = ph;
                 ++h->dcount[mi];
@@ -1084,6 +1105,7 @@ void hx_ccsd_destroy(hx_ccsd *h)
     cudaFree(h->d_diis);
     cudaFree(h->d_active);
     for (int ph = 0; ph < PH_COUNT; ++ph) cudaFree(h->d_act_ph[ph]);
+    cudaFree(h->d_gate);
     cudaFree(h->d_part);
     if (h->st) cudaStreamDestroy(h->st);
     delete h;
