@@ -101,7 +101,8 @@ struct Cfg {
     static_assert(2 * NQ * BN_ <= 512, "two TMEM buffers must fit in 512 columns");
     static_assert(STAGES_ * S_ * (128 * BK_ * 2 + BN_ * BK_ * 2) + 1280 <= 232448, "shared memory");
     static_assert(EPIW_ % 4 == 0 && EPI_COLS % 8 == 0, "epilogue split");
-    static_assert(128 * (BN_ + 1) * 8 <= STAGES_ * STAGE_BYTES, "output tile staging fits in the TMA ring");
+    static_assert(128 * (BN_ + 1) * 8 + 128 * 12 <= STAGES_ * STAGE_BYTES, "output tile staging fits in the TMA ring");
+    static_assert(EPIW_ * 32 >= 128 && EPIW_ * 32 >= BN_, "epilogue threads cover the tile's rows and columns");
 };
 using Low = Cfg<3, 3, 1, 96, 2, 8, 12>;
 using Mid = Cfg<4, 3, 2, 80, 2, 6, 8>;
@@ -244,6 +245,17 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v)
 __device__ __forceinline__ long long split_off(int x, int xi, long long s0, long long s1)
 {
     return (long long)(x / xi) * s0 + (long long)(x % xi) * s1;
+}
+
+// x 2^(ea + eb - 14) for row exponent ea of A and column exponent eb of B:
+// the value ldexp gives (one rounding; exact for normal results); zero when
+// the row or the column is all zero (exponent INT_MIN: every product is zero)
+__device__ __forceinline__ double scale_pow2(double x, int ea, int eb)
+{
+    if (ea == INT_MIN || eb == INT_MIN) return 0.0;
+    const int e = ea + eb - 14;
+    if (e >= -1022 && e <= 1023) return x * __longlong_as_double((long long)(e + 1023) << 52);
+    return ldexp(x, e);
 }
 
 // ------------------------------------------------------------------ split + gather
@@ -561,23 +573,46 @@ __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restri
             mbar_arrive(&acc_empty[buf]);
         }
         // every chunk is drained, so the TMA ring is idle: stage the tile in its
-        // shared memory and write C with consecutive threads on consecutive n
+        // shared memory with the row offsets and exponents of C, then write the
+        // valid part of the tile: one fixed column per thread (consecutive
+        // threads on consecutive n), rows RSTEP apart, U rows of C read ahead
         constexpr int LD = C::BN + 1;
         double *stile = (double *)smem;                      // [BM][BN + 1]
+        long long *srow = (long long *)(stile + BM * LD);    // [BM] row offsets into C
+        int *sexp = (int *)(srow + BM);                      // [BM] row exponents of A
 #pragma unroll
         for (int e = 0; e < C::EPI_COLS; ++e) stile[row * LD + col0 + e] = (double)hi[e] + (double)lo[e];
+        const int mv = min(BM, d.M - tm * BM), nv = min(C::BN, d.N - tn * C::BN);
+        if (threadIdx.x < mv) {
+            const int m = tm * BM + threadIdx.x;
+            srow[threadIdx.x] = split_off(m, d.Mi, d.c[0], d.c[1]);
+            sexp[threadIdx.x] = d.expA[(long long)bt * d.Mp + m];
+        }
         asm volatile("bar.sync 1, %0;" ::"r"(C::EPI_THREADS) : "memory");
-        double *Cp = d.C + (long long)bt * d.c[4];
-        for (int idx = threadIdx.x; idx < BM * C::BN && ok; idx += C::EPI_THREADS) {
-            const int mm = idx / C::BN, nn = idx - mm * C::BN;
-            const int m = tm * BM + mm, n = tn * C::BN + nn;
-            if (m >= d.M || n >= d.N) continue;
-            const int ea = d.expA[(long long)bt * d.Mp + m], eb = d.expB[(long long)bt * d.Np + n];
-            double *p = Cp + split_off(m, d.Mi, d.c[0], d.c[1]) + split_off(n, d.Ni, d.c[2], d.c[3]);
-            double r = d.alpha * ldexp(stile[mm * LD + nn], ea + eb - 14);
-            if (d.ksplit > 1) { atomicAdd(p, r); continue; }
-            if (d.beta != 0.0) r += d.beta * *p;
-            *p = r;
+        constexpr int RSTEP = C::EPI_THREADS / C::BN, U = 8;
+        const int nn = threadIdx.x % C::BN, rr = threadIdx.x / C::BN;
+        if (ok && rr < RSTEP && nn < nv) {
+            const int n = tn * C::BN + nn;
+            const int eb = d.expB[(long long)bt * d.Np + n];
+            double *Cn = d.C + (long long)bt * d.c[4] + split_off(n, d.Ni, d.c[2], d.c[3]);
+            const bool load_c = d.ksplit == 1 && d.beta != 0.0;
+            for (int m0 = rr; m0 < mv; m0 += RSTEP * U) {
+                double old[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int mm = m0 + u * RSTEP;
+                    old[u] = (load_c && mm < mv) ? Cn[srow[mm]] : 0.0;
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int mm = m0 + u * RSTEP;
+                    if (mm >= mv) break;
+                    const double r = d.alpha * scale_pow2(stile[mm * LD + nn], sexp[mm], eb);
+                    double *p = Cn + srow[mm];
+                    if (d.ksplit > 1) atomicAdd(p, r);
+                    else *p = load_c ? r + d.beta * old[u] : r;
+                }
+            }
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -709,7 +744,10 @@ static cudaError_t prep_launch(const PrepDesc *d, int n, long long tiles, long l
 }
 
 // Problems below this many multiply-adds stay on the FP64 CUDA-core kernel.
-static const double kMinTcWork = 4.0e6;
+// GB300's FP64 rate is about a thousandth of its BF16 tensor rate, so even
+// the small contractions of 8..64-site molecules (padded to 128-row tiles)
+// are faster on the tensor cores; only the tiniest stay on FP64.
+static const double kMinTcWork = 1.0e4;
 
 static bool on_tc(const TgemmDesc &t) { return (double)t.batch * t.M * t.N * t.K >= kMinTcWork; }
 

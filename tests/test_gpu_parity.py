@@ -142,7 +142,8 @@ def test_mixed_trace_starts_on_tensor_cores(api):
 
 def test_tensor_core_gemm_accuracy(api):
     rng = np.random.default_rng(3)
-    for (M, N, K) in ((130, 70, 200), (512, 384, 1000)):
+    # partial tiles, one-row / one-column problems and K far below the k-block
+    for (M, N, K) in ((130, 70, 200), (512, 384, 1000), (5, 1, 3), (1, 7, 64), (200, 3, 17), (37, 250, 9)):
         A = rng.normal(size=(M, K))
         B = rng.normal(size=(N, K))
         ref = A @ B.T
