@@ -4,9 +4,11 @@
 
 Runs the reference SCF (oracle/rhf.py) and the factorised FP64 restatement of
 the reference's r-ccsd (oracle/ccsd_fact.py, "2-1" projection, DIIS 20,
-residual threshold 1e-10) on polyene(160) with bond-alternation 0.1 and
+residual threshold 1e-8) on polyene(160) with bond-alternation 0.1 and
 records E_ref, E_corr and the per-iteration trace (max|d1|, max|d2|, E).
-Takes about an hour on 8 cores.
+Takes about two hours on 8 cores (27 iterations of about 4 minutes). At a
+1e-8 residual the energy is settled well below 1e-6 eV: the last five
+iterations of the trace move it by at most 3e-7 eV.
 """
 from __future__ import annotations
 
@@ -24,7 +26,7 @@ from oracle.ppp import build_model                 # noqa: E402
 from oracle.rhf import mo_fock, rhf                # noqa: E402
 
 
-def main(n=160, eps=1e-10):
+def main(n=160, eps=1e-8):
     mol = molecules.polyene(n)
     model = build_model(mol, alternation=0.1)
     scf = rhf(model)

@@ -228,3 +228,19 @@ def test_full_size_polyene_properties(api):
     I = ccsd_fact.Integrals(s["C"], build_model(mol, alternation=0.1)["G"], o)
     e = ccsd_fact.energy(s["F"], I, t1, t2, r["energy"][1])
     assert abs(e[0] - r["energy"][0]) < 1e-8
+
+
+def test_full_size_polyene_mixed_energy_matches_oracle(api):
+    # N = 160 (o = v = 80): the mixed-precision solve, learned guess and the
+    # FP64 check included, must land within 1e-6 eV of the FP64 oracle's
+    # converged energy (tests/golden/polyene160.json, residual 1e-8), and its
+    # SCF must reproduce the oracle's reference energy.
+    gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "polyene160.json")))
+    cc = api.CoupledCluster(molecules.polyene(160), _kw(api, accuracy=7, precision="mixed", guess="learned"))
+    cc.initCC()
+    r = cc.iterate()
+    tr = cc.trace(0)
+    cc.finalizeCC()
+    assert r["status"] == 1 and tr[-1, 4] == 0.0
+    assert abs(r["energy"][1] - gold["eref"]) < 1e-9
+    assert abs(r["energy"][0] - gold["energy"][0]) < 1e-6
