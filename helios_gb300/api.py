@@ -49,7 +49,8 @@ class CCParams(ctypes.Structure):
                 ("check_divergence", ctypes.c_int32), ("divergence_threshold", ctypes.c_double),
                 ("check_stagnation", ctypes.c_int32), ("stagnation_threshold", ctypes.c_double),
                 ("stagnation_after", ctypes.c_int32), ("precision", ctypes.c_int32), ("guess", ctypes.c_int32),
-                ("mixed_switch", ctypes.c_double), ("mixed_patience", ctypes.c_int32)]
+                ("mixed_switch", ctypes.c_double), ("mixed_patience", ctypes.c_int32),
+                ("mixed_check", ctypes.c_int32)]
 
 
 class HxError(RuntimeError):
@@ -84,7 +85,7 @@ def library():
 
 def gemm(A, B, precision="fp64", reps=1):
     """C = A @ B.T on the engine's FP64 ("fp64") or tensor-core GEMM ("mixed": 3 slices,
-    "mid": 4 slices, "high": 6 slices); returns (C, ms per launch)."""
+    "mid": 4 slices, "high": 6 slices, "exact": 7 slices, FP64 emulated); returns (C, ms per launch)."""
     A = np.ascontiguousarray(A, dtype=np.float64)
     B = np.ascontiguousarray(B, dtype=np.float64)
     M, K = A.shape
@@ -92,7 +93,7 @@ def gemm(A, B, precision="fp64", reps=1):
     C = np.zeros((M, N))
     ms = ctypes.c_double()
     _check(library().hx_gemm(A.ctypes.data_as(_c_d), B.ctypes.data_as(_c_d), C.ctypes.data_as(_c_d), M, N, K,
-                             {"fp64": 0, "mixed": 1, "high": 2, "mid": 3}[precision], reps, ctypes.byref(ms)))
+                             {"fp64": 0, "mixed": 1, "high": 2, "mid": 3, "exact": 4}[precision], reps, ctypes.byref(ms)))
     return C, ms.value
 
 
@@ -172,6 +173,7 @@ class Keywords:
     model: object = None                         # engine: learned-guess parameters (None = the shipped model)
     mixed_switch: float = 1e-3                   # engine: residual where 3-slice hands over to 4-slice
     mixed_patience: int = 3                      # engine: non-improving iterations before the next phase
+    mixed_check: str = "emulated"                # engine: convergence checks on "emulated" (7-slice) or "fp64"
 
     def to_c(self) -> CCParams:
         p = CCParams()
@@ -198,6 +200,7 @@ class Keywords:
         p.guess = {"reference": 0, "learned": 1}[self.guess]
         p.mixed_switch = self.mixed_switch
         p.mixed_patience = self.mixed_patience
+        p.mixed_check = {"emulated": 0, "fp64": 1}[self.mixed_check]
         return p
 
 
@@ -318,7 +321,7 @@ class CoupledCluster:
 
     def trace(self, mol: int = 0) -> np.ndarray:
         """Per-iteration (max|d1|, max|d2|, E_total, seconds, phase) of the last solve;
-        phase 3, 2, 1 = 3-, 4-, 6-slice tensor cores, 0 = FP64."""
+        phase 4, 3, 2 = 3-, 4-, 6-slice tensor cores, 1 = 7-slice (FP64 emulated), 0 = FP64."""
         n = _check(library().hx_ccsd_trace(self._h, int(mol), None, 0))
         out = np.zeros((max(n, 1), 5))
         library().hx_ccsd_trace(self._h, int(mol), out.ctypes.data_as(_c_d), n)

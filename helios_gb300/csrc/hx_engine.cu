@@ -167,8 +167,8 @@ struct Rules {   // gIterator.f90:88-210
     }
 };
 
-enum { PH_FP64 = 0, PH_HIGH = 1, PH_MID = 2, PH_LOW = 3, PH_COUNT = 4 };
-// tensor-core mode (tc::run_group) of a phase: LOW 0, MID 1, HIGH 2
+enum { PH_FP64 = 0, PH_EXACT = 1, PH_HIGH = 2, PH_MID = 3, PH_LOW = 4, PH_COUNT = 5 };
+// tensor-core mode (tc::run_group) of a phase: LOW 0, MID 1, HIGH 2, EXACT 3
 static inline int tc_mode(int ph) { return PH_LOW - ph; }
 
 struct hx_ccsd {
@@ -206,7 +206,7 @@ struct hx_ccsd {
     std::vector<int> scf_failed;         // batches: molecules whose SCF did not converge are left out
     tc::Engine *tce = nullptr;           // tensor-core backend (mixed precision)
     mlp::Model *model = nullptr;         // learned T2 guess (guess = 1)
-    // mixed precision: per-molecule phase (PH_LOW / PH_MID / PH_HIGH
+    // mixed precision: per-molecule phase (PH_LOW / PH_MID / PH_HIGH / PH_EXACT
     // tensor-core iterations, PH_FP64 CUDA-core FP64) and one launch mask per phase
     std::vector<int> phase, stall;
     std::vector<double> best;
@@ -217,8 +217,8 @@ struct hx_ccsd {
     // phase ended (0 = not ended, -1 = its vectors purged)
     std::vector<long long> dcount;
     std::vector<std::vector<int>> slot_phase;
-    std::vector<std::array<double, 4>> ph_end;
-    int *d_act_ph[PH_COUNT] = {nullptr, nullptr, nullptr, nullptr};
+    std::vector<std::array<double, PH_COUNT>> ph_end;
+    int *d_act_ph[PH_COUNT] = {};
     std::vector<std::vector<std::array<double, 5>>> trace;
     // device time of the last hx_ccsd_init and solve (events on st)
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -278,10 +278,10 @@ static int run_group(hx_ccsd *h, Group &g)
 {
     if (g.tiles == 0) return HX_OK;
     if (h->tce) {
-        int n[PH_COUNT] = {0, 0, 0, 0};
+        int n[PH_COUNT] = {};
         for (int mi = 0; mi < h->nmol; ++mi)
             if (h->active[mi]) ++n[h->phase[mi]];
-        for (int ph = PH_LOW; ph >= PH_HIGH; --ph) {
+        for (int ph = PH_LOW; ph >= PH_EXACT; --ph) {
             if (!n[ph]) continue;
             cudaError_t e = tc::run_group(h->tce, g.h.data(), (int)g.h.size(), h->d_act_ph[ph], h->st, tc_mode(ph));
             if (e != cudaSuccess) { hx_set_error("tensor-core group: %s", cudaGetErrorString(e)); return HX_ERR_CUDA; }
@@ -302,7 +302,7 @@ static const double kHighMargin = 0.1;
 // iterations before it reaches kHighMargin * eps.
 static double diis_gate(const hx_ccsd *h, int mi)
 {
-    if (h->tce && h->phase[mi] != PH_FP64) return kHighMargin * h->fin_scale[mi] * h->gate_eps;
+    if (h->tce && h->phase[mi] >= PH_HIGH) return kHighMargin * h->fin_scale[mi] * h->gate_eps;
     return h->gate_eps;
 }
 
@@ -480,7 +480,7 @@ static int allocate(hx_ccsd *h)
     h->phase.assign(h->nmol, PH_FP64);
     h->dcount.assign(h->nmol, 0);
     h->slot_phase.assign(h->nmol, {});
-    h->ph_end.assign(h->nmol, {0.0, 0.0, 0.0, 0.0});
+    h->ph_end.assign(h->nmol, {});
     h->stall.assign(h->nmol, 0);
     h->best.assign(h->nmol, 1e300);
     h->fin_scale.assign(h->nmol, 1.0);
@@ -528,6 +528,7 @@ void hx_cc_params_default(hx_cc_params *p)
     p->guess = 0;
     p->mixed_switch = 1e-3;
     p->mixed_patience = 3;
+    p->mixed_check = 0;
 }
 
 int hx_ccsd_create_batch(const hx_ppp_model *ms, int32_t n, const hx_cc_params *p, hx_ccsd **out)
@@ -537,6 +538,7 @@ int hx_ccsd_create_batch(const hx_ppp_model *ms, int32_t n, const hx_cc_params *
     if (p->projection_type != 1 && p->projection_type != 2) { hx_set_error("projection-type must be 1 or 2"); return HX_ERR_ARG; }
     if (p->diis_enabled && (p->diis_steps < 2 || p->diis_steps > HX_MAX_DIIS)) { hx_set_error("diis-steps outside 2..%d", HX_MAX_DIIS); return HX_ERR_ARG; }
     if (p->precision != HX_PRECISION_FP64 && p->precision != HX_PRECISION_MIXED) { hx_set_error("unknown precision mode"); return HX_ERR_ARG; }
+    if (p->mixed_check != 0 && p->mixed_check != 1) { hx_set_error("mixed_check must be 0 (7-slice emulated FP64) or 1 (FP64)"); return HX_ERR_ARG; }
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) { hx_set_error("no CUDA device"); return HX_ERR_CUDA; }
     hx_ccsd *h = new hx_ccsd();
@@ -775,7 +777,7 @@ static void diis_mirror_reset(hx_ccsd *h, int mi)
 {
     h->dcount[mi] = 0;
     h->slot_phase[mi].assign((size_t)h->diis[mi].nd, -1);
-    h->ph_end[mi] = {0.0, 0.0, 0.0, 0.0};
+    h->ph_end[mi] = {};
 }
 
 // Mixed precision keeps the DIIS history across a precision switch (a plain
@@ -792,7 +794,7 @@ static int diis_purge(hx_ccsd *h, int mi, double a)
     const int nd = h->diis[mi].nd;
     const int valid = (int)std::min<long long>(h->dcount[mi], nd);
     std::vector<int> drop;
-    for (int ph = 1; ph < PH_COUNT; ++ph) {
+    for (int ph = PH_HIGH; ph < PH_COUNT; ++ph) {        // EXACT and FP64 vectors are never purged
         if (!(h->ph_end[mi][ph] > 0.0) || !(a < kPurge * h->ph_end[mi][ph])) continue;
         for (int k = 0; k < valid; ++k)
             if (h->slot_phase[mi][k] == ph) drop.push_back(k);
@@ -817,20 +819,22 @@ static int diis_purge(hx_ccsd *h, int mi, double a)
 //   LOW   3-slice tensor-core contractions (about 2^-24 of the operands' row
 //         maxima) until the residual falls below mixed_switch;
 //   MID   4-slice (about 2^-32) until it falls below kMidSpan * mixed_switch;
-//   HIGH  6-slice (about 2^-46: residuals as accurate as FP64 ones);
-//   FP64  CUDA-core FP64 iterations: convergence is declared only here, so the
-//         final residual and energy are plain FP64 (the defect correction). An
-//         FP64 residual that does not confirm convergence sends the molecule
-//         back to 6-slice iterations with a 10x tighter hand-over target (at
-//         most kMaxFp64Returns times): an FP64 iteration costs as much as
-//         tens of 6-slice ones.
-// Every tensor-core phase hands over to FP64 once the residual is below
-// kHighMargin * eps (the iteration is not monotone, and one more
-// tensor-core iteration costs far less than an FP64 iteration whose
-// residual lands just above eps). A phase switches while its own error is
-// still about 1 % of the residual, so the DIIS history is kept; a phase
-// that stops improving for mixed_patience iterations hands over early and
-// the DIIS history restarts (its error vectors are then too noisy to mix
+//   HIGH  6-slice (about 2^-46) until it falls below kHighMargin * eps;
+//   check the iteration that may declare convergence: EXACT, 7-slice
+//         contractions that emulate FP64 ones (mixed_check = 0), or plain
+//         CUDA-core FP64 (mixed_check = 1). Convergence is declared only
+//         here, so the final residual and energy carry FP64 accuracy (the
+//         defect correction). A check that does not confirm convergence
+//         sends the molecule back to 6-slice iterations with a 10x tighter
+//         hand-over target (at most kMaxFp64Returns times); after that the
+//         check phase iterates on, and EXACT iterations that stop improving
+//         for mixed_patience iterations hand over to CUDA-core FP64.
+// A tensor-core phase hands over to the check below kHighMargin * eps (the
+// iteration is not monotone, and one more 6-slice iteration costs less than
+// a check whose residual lands just above eps). A phase switches while its
+// own error is still about 1 % of the residual, so the DIIS history is kept;
+// a phase that stops improving for mixed_patience iterations hands over early
+// and the DIIS history restarts (its error vectors are then too noisy to mix
 // with more accurate ones).
 static const double kMidSpan = 1e-3;
 static const int kMaxFp64Returns = 3;
@@ -839,6 +843,7 @@ static int solve_all(hx_ccsd *h, int maxiter, double eps)
 {
     if (h->p.projection_type != 2) { hx_set_error("projection-type 1 is not built on the GPU path"); return HX_ERR_UNSUPPORTED; }
     const bool mixed = h->tce != nullptr;
+    const int check_ph = h->p.mixed_check == 1 ? PH_FP64 : PH_EXACT;
     int remaining = 0;
     for (int mi = 0; mi < h->nmol; ++mi) {
         remaining += h->active[mi];
@@ -876,15 +881,15 @@ static int solve_all(hx_ccsd *h, int maxiter, double eps)
                 ++h->dcount[mi];
             }
             if (mixed) HX_TRY(diis_purge(h, mi, a));
-            if (ph != PH_FP64 && !cancel) {
+            if (ph >= PH_HIGH && !cancel) {
                 // tensor-core phases never claim convergence: they hand over
                 if (a < h->best[mi]) { h->best[mi] = a; h->stall[mi] = 0; } else ++h->stall[mi];
                 const double fin = kHighMargin * h->fin_scale[mi] * eps;
                 const double below = ph == PH_LOW ? h->p.mixed_switch : ph == PH_MID ? kMidSpan * h->p.mixed_switch : 0.0;
                 const bool stalled = h->stall[mi] >= h->p.mixed_patience;
                 int next = ph;
-                if (a < fin) next = PH_FP64;
-                else if (a < below || stalled) next = ph - 1;
+                if (a < fin) next = check_ph;
+                else if (a < below || stalled) next = ph == PH_HIGH ? check_ph : ph - 1;
                 Rules &R = h->rules[mi];
                 int s = R.update(next != ph ? std::max(a, eps * 2) : a, h->p, maxiter, eps, false);
                 if (s == HX_DIVERGED || s == HX_STAGNATED || s == HX_FAILED_MAXITER) {
@@ -895,7 +900,7 @@ static int solve_all(hx_ccsd *h, int maxiter, double eps)
                     h->best[mi] = 1e300;
                     changed = true;
                     h->ph_end[mi][ph] = a;
-                    if (stalled && a >= fin && ph != PH_HIGH) {
+                    if (stalled && a >= fin && ph != PH_HIGH) {          // LOW or MID
                         HX_CU(cudaMemsetAsync(h->diis[mi].count, 0, sizeof(int), h->st));
                         diis_mirror_reset(h, mi);
                     }
@@ -909,7 +914,7 @@ static int solve_all(hx_ccsd *h, int maxiter, double eps)
                 --remaining;
                 changed = true;
             } else if (mixed && h->fp_returns[mi] < kMaxFp64Returns) {
-                // the FP64 check did not confirm convergence: more 6-slice
+                // the check did not confirm convergence: more 6-slice
                 // iterations to a 10x tighter target, then check again
                 h->phase[mi] = PH_HIGH;
                 h->fin_scale[mi] *= 0.1;
@@ -917,6 +922,13 @@ static int solve_all(hx_ccsd *h, int maxiter, double eps)
                 h->stall[mi] = 0;
                 h->best[mi] = 1e300;
                 changed = true;
+            } else if (mixed && ph == PH_EXACT) {
+                if (a < h->best[mi]) { h->best[mi] = a; h->stall[mi] = 0; }
+                else if (++h->stall[mi] >= h->p.mixed_patience) {
+                    h->phase[mi] = PH_FP64;
+                    h->stall[mi] = 0;
+                    changed = true;
+                }
             }
         }
         if (changed) HX_TRY(upload_masks(h));
@@ -1116,7 +1128,7 @@ void hx_ccsd_destroy(hx_ccsd *h)
 int hx_gemm(const double *A, const double *B, double *C, int32_t M, int32_t N, int32_t K, int32_t precision,
             int32_t reps, double *ms)
 {
-    if (!A || !B || !C || M <= 0 || N <= 0 || K <= 0 || reps < 1 || precision < 0 || precision > 3) {
+    if (!A || !B || !C || M <= 0 || N <= 0 || K <= 0 || reps < 1 || precision < 0 || precision > 4) {
         hx_set_error("hx_gemm: bad arguments");
         return HX_ERR_ARG;
     }
@@ -1150,7 +1162,8 @@ int hx_gemm(const double *A, const double *B, double *C, int32_t M, int32_t N, i
     if (rc == HX_OK && precision != HX_PRECISION_FP64) rc = tc::create(&te, plan, st);
     if (rc == HX_OK) {
         auto launch = [&]() -> cudaError_t {
-            if (te) return tc::run_group(te, plan[0].h.data(), 1, dact, st, precision == 2 ? 2 : precision == 3 ? 1 : 0);
+            if (te) return tc::run_group(te, plan[0].h.data(), 1, dact, st,
+                                         precision == 2 ? 2 : precision == 3 ? 1 : precision == 4 ? 3 : 0);
             return hx_tgemm_f64_launch(plan[0].d, 1, plan[0].tiles, dact, st);
         };
         cudaError_t ce = launch();               // warm-up

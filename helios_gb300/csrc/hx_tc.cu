@@ -67,6 +67,10 @@ namespace tc {
 //   HIGH: 6 slices, pairs i + j <= 5 (21 MMAs), NX = 4: about 2^-46 of the row
 //         maxima; 128 x 48 tiles fed by 32-deep k-blocks (64-byte swizzle) so
 //         that three stages of six slices fit.
+//   EXACT: 7 slices (48 fraction bits below the leading digit, past FP64's
+//         53-bit mantissa), pairs i + j <= 6 (28 MMAs), NX = 5: an emulation
+//         of an FP64 GEMM, its error that of the FP64 product itself; 128 x 32
+//         tiles, so that two buffers of six accumulators fit in TMEM.
 // The shared accumulator is what limits HIGH: measured at 6400^3, one exact
 // class more (NX 3 -> 4) took it from 5.6e-12 to 1.6e-13 relative error,
 // while a sixth slice alone changed nothing; LOW and MID are limited by their
@@ -91,6 +95,10 @@ struct Cfg {
     static constexpr int STAGE_BYTES = S * (ATILE + BTILE);
     static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
     static constexpr int EPI_COLS = BN / (EPIW_ / 4); // columns drained per epilogue thread
+    // 7-slice mode: the exact classes are drained into an int64 per element
+    // (units of 2^-8(NX-1)); the other modes use an FP32 (hi, lo) pair
+    static constexpr bool INT_DRAIN = S_ >= 7;
+    static constexpr float DRAIN_SCALE = (float)(1ull << (8 * (NX_ - 1)));
     static constexpr int PRODUCTS = [] { int n = 0; for (int i = 0; i < S_; ++i) for (int j = 0; j < S_; ++j) n += (i + j <= QMAX_); return n; }();
     __host__ __device__ static constexpr int cls(int q) { return q < NX_ ? q : NX_; }
     // pairs in the largest exact class
@@ -103,10 +111,13 @@ struct Cfg {
     static_assert(EPIW_ % 4 == 0 && EPI_COLS % 8 == 0, "epilogue split");
     static_assert(128 * (BN_ + 1) * 8 + 128 * 12 <= STAGES_ * STAGE_BYTES, "output tile staging fits in the TMA ring");
     static_assert(EPIW_ * 32 >= 128 && EPIW_ * 32 >= BN_, "epilogue threads cover the tile's rows and columns");
+    // int64 drain: a chunk adds below 2^(24 + 8(NX-1) + 1); 32 chunks stay below 2^63
+    static_assert(!INT_DRAIN || 24 + 8 * (NX_ - 1) + 1 + 5 < 63, "int64 drain headroom");
 };
 using Low = Cfg<3, 3, 1, 96, 2, 8, 12>;
 using Mid = Cfg<4, 3, 2, 80, 2, 6, 8>;
 using High = Cfg<6, 5, 4, 48, 3, 7, 8, 32>;
+using Exact = Cfg<7, 6, 5, 32, 3, 6, 8, 32>;
 constexpr int TMEM_COLS = 512;
 constexpr int BM = 128, KPAD = 64;   // K is padded to KPAD (the slicing tile depth)
 constexpr unsigned long long WAIT_NS = 4000000000ull; // a wait longer than 4 s is declared failed
@@ -538,8 +549,16 @@ __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restri
         const int col0 = (warp >> 2) * C::EPI_COLS;
         const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
         float hi[C::EPI_COLS], lo[C::EPI_COLS];
+        // INT_DRAIN: each exact class of a chunk is an integer count of
+        // 2^-8q below 2^24, so a[q] 2^8(NX-1) is an integer below 2^56 and
+        // one int64 sums every exact class of up to 32 chunks without
+        // rounding; every 32 chunks it moves into an FP64 sum. The merged
+        // class (about 2^-8NX of the value) is summed in FP32.
+        long long iacc[C::EPI_COLS];
+        double dacc[C::EPI_COLS];
+        float macc[C::EPI_COLS];
 #pragma unroll
-        for (int e = 0; e < C::EPI_COLS; ++e) { hi[e] = 0.f; lo[e] = 0.f; }
+        for (int e = 0; e < C::EPI_COLS; ++e) { hi[e] = 0.f; lo[e] = 0.f; iacc[e] = 0; dacc[e] = 0.0; macc[e] = 0.f; }
         for (int c = 0; c < nchunk; ++c) {
             const int buf = c & 1;
             const uint32_t use = (uint32_t)(c >> 1);
@@ -553,24 +572,41 @@ __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restri
 #pragma unroll
                 for (int q = 0; q < C::NQ; ++q)
                     tmem_ld8(tmem + lane_base + (uint32_t)(buf * C::NQ * C::BN + q * C::BN + col0 + c0), a[q]);
+                if constexpr (C::INT_DRAIN) {
 #pragma unroll
-                for (int e = 0; e < 8; ++e) {
-                    float x = a[0][e], err = 0.f;
+                    for (int e = 0; e < 8; ++e) {
+                        long long v = 0;
 #pragma unroll
-                    for (int q = 1; q < C::NQ; ++q) {
-                        const float sq = x + a[q][e];
-                        const float bq = sq - x;
-                        err += (x - (sq - bq)) + (a[q][e] - bq);
-                        x = sq;
+                        for (int q = 0; q < C::NX; ++q) v += __float2ll_rn(a[q][e] * C::DRAIN_SCALE);
+                        iacc[c0 + e] += v;
+                        if constexpr (C::NQ > C::NX) macc[c0 + e] += a[C::NX][e];
                     }
-                    const float sh = hi[c0 + e] + x;
-                    const float bh = sh - hi[c0 + e];
-                    lo[c0 + e] += ((hi[c0 + e] - (sh - bh)) + (x - bh)) + err;
-                    hi[c0 + e] = sh;
+                } else {
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) {
+                        float x = a[0][e], err = 0.f;
+#pragma unroll
+                        for (int q = 1; q < C::NQ; ++q) {
+                            const float sq = x + a[q][e];
+                            const float bq = sq - x;
+                            err += (x - (sq - bq)) + (a[q][e] - bq);
+                            x = sq;
+                        }
+                        const float sh = hi[c0 + e] + x;
+                        const float bh = sh - hi[c0 + e];
+                        lo[c0 + e] += ((hi[c0 + e] - (sh - bh)) + (x - bh)) + err;
+                        hi[c0 + e] = sh;
+                    }
                 }
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             mbar_arrive(&acc_empty[buf]);
+            if constexpr (C::INT_DRAIN) {
+                if ((c & 31) == 31) {
+#pragma unroll
+                    for (int e = 0; e < C::EPI_COLS; ++e) { dacc[e] += (double)iacc[e]; iacc[e] = 0; }
+                }
+            }
         }
         // every chunk is drained, so the TMA ring is idle: stage the tile in its
         // shared memory with the row offsets and exponents of C, then write the
@@ -581,7 +617,9 @@ __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restri
         long long *srow = (long long *)(stile + BM * LD);    // [BM] row offsets into C
         int *sexp = (int *)(srow + BM);                      // [BM] row exponents of A
 #pragma unroll
-        for (int e = 0; e < C::EPI_COLS; ++e) stile[row * LD + col0 + e] = (double)hi[e] + (double)lo[e];
+        for (int e = 0; e < C::EPI_COLS; ++e)
+            stile[row * LD + col0 + e] = C::INT_DRAIN ? (dacc[e] + (double)iacc[e]) / (double)C::DRAIN_SCALE + (double)macc[e]
+                                                      : (double)hi[e] + (double)lo[e];
         const int mv = min(BM, d.M - tm * BM), nv = min(C::BN, d.N - tn * C::BN);
         if (threadIdx.x < mv) {
             const int m = tm * BM + threadIdx.x;
@@ -649,7 +687,7 @@ struct Engine {
     __nv_bfloat16 *scratch = nullptr;   // slices of the variable operands (shared by groups and modes)
     int *rexp = nullptr;
     int *d_err = nullptr;
-    Mode mode[3];                        // 0 = LOW, 1 = MID, 2 = HIGH (3, 4, 6 slices)
+    Mode mode[4];                        // 0 = LOW, 1 = MID, 2 = HIGH, 3 = EXACT (3, 4, 6, 7 slices)
     std::vector<const Group *> keys;
     bool profile = false;
     int generation = 0;
@@ -738,7 +776,8 @@ static cudaError_t prep_launch(const PrepDesc *d, int n, long long tiles, long l
     row_scale<<<tb, PT_THREADS, 0, s>>>(d, n, tiles, active);
     if (S == Low::S) split_gather<Low::S><<<tb, PT_THREADS, 0, s>>>(d, n, tiles, active);
     else if (S == Mid::S) split_gather<Mid::S><<<tb, PT_THREADS, 0, s>>>(d, n, tiles, active);
-    else split_gather<High::S><<<tb, PT_THREADS, 0, s>>>(d, n, tiles, active);
+    else if (S == High::S) split_gather<High::S><<<tb, PT_THREADS, 0, s>>>(d, n, tiles, active);
+    else split_gather<Exact::S><<<tb, PT_THREADS, 0, s>>>(d, n, tiles, active);
     hx_count_launches(3);
     return cudaGetLastError();
 }
@@ -861,10 +900,11 @@ int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s)
 {
     *out = nullptr;
     Engine *e = new Engine();
-    e->mode[0].BK = Low::BK; e->mode[1].BK = Mid::BK; e->mode[2].BK = High::BK;
+    e->mode[0].BK = Low::BK; e->mode[1].BK = Mid::BK; e->mode[2].BK = High::BK; e->mode[3].BK = Exact::BK;
     e->mode[0].S = Low::S; e->mode[0].BN = Low::BN; e->mode[0].products = Low::PRODUCTS; e->mode[0].smem = Low::SMEM_BYTES;
     e->mode[1].S = Mid::S; e->mode[1].BN = Mid::BN; e->mode[1].products = Mid::PRODUCTS; e->mode[1].smem = Mid::SMEM_BYTES;
     e->mode[2].S = High::S; e->mode[2].BN = High::BN; e->mode[2].products = High::PRODUCTS; e->mode[2].smem = High::SMEM_BYTES;
+    e->mode[3].S = Exact::S; e->mode[3].BN = Exact::BN; e->mode[3].products = Exact::PRODUCTS; e->mode[3].smem = Exact::SMEM_BYTES;
     // variable operands share one scratch: the largest group of either mode
     size_t need = 0, need_rows = 0;
     for (const Mode &md : e->mode)
@@ -894,7 +934,8 @@ int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s)
     for (const Group &g : plan) e->keys.push_back(&g);
     if (cudaFuncSetAttribute(tc_gemm<Low>, cudaFuncAttributeMaxDynamicSharedMemorySize, Low::SMEM_BYTES) != cudaSuccess ||
         cudaFuncSetAttribute(tc_gemm<Mid>, cudaFuncAttributeMaxDynamicSharedMemorySize, Mid::SMEM_BYTES) != cudaSuccess ||
-        cudaFuncSetAttribute(tc_gemm<High>, cudaFuncAttributeMaxDynamicSharedMemorySize, High::SMEM_BYTES) != cudaSuccess) {
+        cudaFuncSetAttribute(tc_gemm<High>, cudaFuncAttributeMaxDynamicSharedMemorySize, High::SMEM_BYTES) != cudaSuccess ||
+        cudaFuncSetAttribute(tc_gemm<Exact>, cudaFuncAttributeMaxDynamicSharedMemorySize, Exact::SMEM_BYTES) != cudaSuccess) {
         destroy(e);
         hx_set_error("cannot reserve shared memory for tc_gemm");
         return HX_ERR_CUDA;
@@ -908,7 +949,7 @@ cudaError_t run_group(Engine *e, const TgemmDesc *descs, int n, const int *d_act
     int gi = -1;
     for (size_t k = 0; k < e->keys.size(); ++k)
         if (e->keys[k]->h.data() == descs) { gi = (int)k; break; }
-    if (gi < 0 || mode < 0 || mode > 2) return cudaErrorInvalidValue;
+    if (gi < 0 || mode < 0 || mode > 3) return cudaErrorInvalidValue;
     Mode &md = e->mode[mode];
     SubGroup &sg = md.groups[gi];
     if (sg.fp64.tiles > 0) {
@@ -939,7 +980,8 @@ cudaError_t run_group(Engine *e, const TgemmDesc *descs, int n, const int *d_act
     }
     if (mode == 0) tc_gemm<Low><<<(unsigned)sg.tiles, Low::NTHREADS, Low::SMEM_BYTES, s>>>(sg.d_tcd, (int)sg.tcd.size(), d_active, e->d_err);
     else if (mode == 1) tc_gemm<Mid><<<(unsigned)sg.tiles, Mid::NTHREADS, Mid::SMEM_BYTES, s>>>(sg.d_tcd, (int)sg.tcd.size(), d_active, e->d_err);
-    else tc_gemm<High><<<(unsigned)sg.tiles, High::NTHREADS, High::SMEM_BYTES, s>>>(sg.d_tcd, (int)sg.tcd.size(), d_active, e->d_err);
+    else if (mode == 2) tc_gemm<High><<<(unsigned)sg.tiles, High::NTHREADS, High::SMEM_BYTES, s>>>(sg.d_tcd, (int)sg.tcd.size(), d_active, e->d_err);
+    else tc_gemm<Exact><<<(unsigned)sg.tiles, Exact::NTHREADS, Exact::SMEM_BYTES, s>>>(sg.d_tcd, (int)sg.tcd.size(), d_active, e->d_err);
     r = cudaGetLastError();
     if (e->profile) {
         cudaEventRecord(pend.b, s);

@@ -100,9 +100,12 @@ typedef struct hx_cc_params {
     double mixed_switch;          /* mixed precision: residual at which a molecule moves from
                                      3-slice to 4-slice tensor-core iterations (1e-3); 4-slice
                                      run to 1e-3 mixed_switch, then 6-slice; any of them hands
-                                     over to FP64 iterations below 0.1 eps */
+                                     over to the check iterations below 0.1 eps */
     int32_t mixed_patience;       /* mixed precision: iterations without a new lowest residual
                                      after which a molecule moves on to the next phase (3) */
+    int32_t mixed_check;          /* mixed precision: the iterations that may declare
+                                     convergence: 0 = 7-slice tensor-core contractions that
+                                     emulate FP64 (default), 1 = FP64 on the CUDA cores */
 } hx_cc_params;
 
 typedef struct hx_ccsd hx_ccsd;
@@ -191,9 +194,9 @@ int hx_ccsd_get_scf(hx_ccsd *h, int32_t mol, double *C, double *eps, double *fmo
 
 /* Per-iteration record of molecule mol's last solve: for each iteration
  * k < cap, out[5k..5k+4] = max|d1|, max|d2|, E_total, seconds since the start
- * of the solve, phase of the iteration (0 FP64 CUDA cores; 1, 2, 3: six-,
- * four- and three-slice tensor-core contractions). Returns the number of
- * iterations recorded. */
+ * of the solve, phase of the iteration (0 FP64 CUDA cores; 1, 2, 3, 4: seven-
+ * (FP64 emulated), six-, four- and three-slice tensor-core contractions).
+ * Returns the number of iterations recorded. */
 int hx_ccsd_trace(hx_ccsd *h, int32_t mol, double *out, int32_t cap);
 
 /* Engine utility with no counterpart in the reference: device timing.
@@ -221,8 +224,9 @@ void hx_ccsd_destroy(hx_ccsd *h);
  * row-major FP64 host matrices (A: M x K, B: N x K, C: M x N) on the engine's
  * FP64 CUDA-core GEMM (precision 0) or its exact-slice tcgen05 GEMM with
  * 3 slices (precision 1, about 2^-24 of the row maxima), 6 slices (precision
- * 2, about 2^-46) or 4 slices (precision 3, about 2^-32); the launch is
- * repeated reps times after one warm-up and
+ * 2, about 2^-46), 4 slices (precision 3, about 2^-32) or 7 slices
+ * (precision 4: FP64 emulated, as accurate as the FP64 product); the launch
+ * is repeated reps times after one warm-up and
  * *ms (if not NULL) receives the mean device time per launch. */
 int hx_gemm(const double *A, const double *B, double *C, int32_t M, int32_t N, int32_t K, int32_t precision,
             int32_t reps, double *ms);

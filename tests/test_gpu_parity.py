@@ -132,11 +132,13 @@ def test_mixed_trace_starts_on_tensor_cores(api):
     tr = cc.trace(0)
     cc.finalizeCC()
     assert r["status"] == 1
-    assert tr[0, 4] == 3.0 and tr[-1, 4] == 0.0          # 3-slice tensor cores first, FP64 last
+    # 3-slice tensor cores first; the last iteration is a check (7-slice
+    # emulated FP64 by default)
+    assert tr[0, 4] == 4.0 and tr[-1, 4] == 1.0
     d = np.diff(tr[:, 4])
-    # phases only move towards FP64, except that an FP64 check which does not
+    # phases only move down the ladder, except that a check which does not
     # confirm convergence sends the molecule back to 6-slice iterations
-    assert np.all((d <= 0) | ((d == 1) & (tr[:-1, 4] == 0)))
+    assert np.all((d <= 0) | ((tr[1:, 4] == 2) & (tr[:-1, 4] <= 1)))
     assert np.all(np.diff(tr[:, 3]) >= 0)
 
 
@@ -155,6 +157,24 @@ def test_tensor_core_gemm_accuracy(api):
         assert np.abs(C - ref).max() / np.abs(ref).max() < 1e-12
         C64, _ = api.gemm(A, B, "fp64")
         assert np.abs(C64 - ref).max() / np.abs(ref).max() < 1e-13
+        CX, _ = api.gemm(A, B, "exact")
+        assert np.abs(CX - ref).max() / np.abs(ref).max() < 1e-14
+
+
+def test_exact_gemm_is_as_accurate_as_fp64(api):
+    # the 7-slice mode against an extended-precision product: its error is
+    # that of an FP64 GEMM (rows of very different scales included)
+    rng = np.random.default_rng(5)
+    for (M, N, K) in ((130, 70, 200), (64, 48, 3000)):
+        A = rng.normal(size=(M, K)) * np.exp(2 * rng.normal(size=(M, 1)))
+        B = rng.normal(size=(N, K))
+        ref = (A.astype(np.longdouble) @ B.T.astype(np.longdouble))
+        scale = np.abs(ref).max(axis=1, keepdims=True)
+        CX, _ = api.gemm(A, B, "exact")
+        C64, _ = api.gemm(A, B, "fp64")
+        ex = float((np.abs(CX - ref) / scale).max())
+        e64 = float((np.abs(C64 - ref) / scale).max())
+        assert ex < 4 * e64 + 1e-16, (ex, e64)
 
 
 def test_status_codes(api):
@@ -232,15 +252,15 @@ def test_full_size_polyene_properties(api):
 
 def test_full_size_polyene_mixed_energy_matches_oracle(api):
     # N = 160 (o = v = 80): the mixed-precision solve, learned guess and the
-    # FP64 check included, must land within 1e-6 eV of the FP64 oracle's
-    # converged energy (tests/golden/polyene160.json, residual 1e-8), and its
-    # SCF must reproduce the oracle's reference energy.
+    # 7-slice (emulated FP64) check included, must land within 1e-6 eV of the
+    # FP64 oracle's converged energy (tests/golden/polyene160.json, residual
+    # 1e-8), and its SCF must reproduce the oracle's reference energy.
     gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "polyene160.json")))
     cc = api.CoupledCluster(molecules.polyene(160), _kw(api, accuracy=7, precision="mixed", guess="learned"))
     cc.initCC()
     r = cc.iterate()
     tr = cc.trace(0)
     cc.finalizeCC()
-    assert r["status"] == 1 and tr[-1, 4] == 0.0
+    assert r["status"] == 1 and tr[-1, 4] == 1.0
     assert abs(r["energy"][1] - gold["eref"]) < 1e-9
     assert abs(r["energy"][0] - gold["energy"][0]) < 1e-6

@@ -39,6 +39,8 @@ def test_default_parameters_are_helios_defaults(lib):
     assert p.scf_maxiter == 400 and p.scf_eps == 1e-12 and p.scf_step == 0.05
     assert p.projection_type == 2 and p.divergence_threshold == 1e3 and p.stagnation_after == 200
     assert p.stagnation_threshold == 60.0
+    # engine keys after the reference's: mixed-precision ladder defaults
+    assert p.mixed_switch == 1e-3 and p.mixed_patience == 3 and p.mixed_check == 0
 
 
 def test_keywords_potentiate_like_the_reference(lib):
