@@ -271,6 +271,19 @@ def run_gb300(args):
                 "tensor_issued_frac_while_in_tc_gemm": tw["gemm_hw_flops"] / (tw["gemm_ms"] * 1e-3 * peak_t)
                 if tw["gemm_ms"] > 0 else None,
                 "tc_gemm_share_of_batch_time": tw["gemm_ms"] * 1e-3 / wsecs if wsecs > 0 else None}
+        # the same batch on the plain FP64 path (one solve: it has no tensor-core warm-up)
+        if args.fp64_compare:
+            c64 = api.CoupledCluster(mols, api.Keywords(bond_alternation=0.1, accuracy=8, precision="fp64"))
+            c64.initCC()
+            o64 = c64.solve_batch()
+            t64 = c64.timing()
+            c64.finalizeCC()
+            s64 = (t64["init_ms"] + t64["solve_ms"]) / 1e3
+            extra["batch"]["fp64_plain"] = {"seconds": s64, "molecules_per_s": args.batch / s64,
+                                            "converged": int((o64["status"] == 1).sum()),
+                                            "mean_iterations": float(o64["iterations"].mean())}
+            best = extra["batch"].get("learned_guess", extra["batch"].get("reference_guess"))
+            extra["batch"]["speedup_mixed_vs_fp64"] = s64 / best["seconds"]
     # --- finite-field alpha_xx of the 2 x 32 ladder: five field points solved as one batch
     if args.polariz:
         from helios_gb300 import polariz
