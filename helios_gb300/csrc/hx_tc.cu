@@ -515,7 +515,11 @@ __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restri
                     const uint32_t sa = smem_u32(smem + st * C::STAGE_BYTES);
                     const uint32_t sb = sa + C::S * C::ATILE;
                     const bool chunk_start = kb == c * C::KC;
-#pragma unroll 1
+                    // descriptors of the stage's first slices; the others differ
+                    // only in the start-address field (address / 16, 14 bits:
+                    // shared memory stays below 256 KB, so adding never carries)
+                    const uint64_t a0 = smem_desc<C>(sa), b0 = smem_desc<C>(sb);
+#pragma unroll
                     for (int kk = 0; kk < C::BK / 16; ++kk) {
 #pragma unroll
                         for (int i = 0; i < C::S; ++i) {
@@ -531,8 +535,8 @@ __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restri
                                                                : (C::NX < C::S ? 0 : C::NX - (C::S - 1));
                                 const bool first = chunk_start && kk == 0 && i == i_first &&
                                                    (cl < C::NX || j == C::NX - i_first);
-                                const uint64_t ad = smem_desc<C>(sa + i * C::ATILE + kk * 32);
-                                const uint64_t bd = smem_desc<C>(sb + j * C::BTILE + kk * 32);
+                                const uint64_t ad = a0 + (uint64_t)((i * C::ATILE + kk * 32) >> 4);
+                                const uint64_t bd = b0 + (uint64_t)((j * C::BTILE + kk * 32) >> 4);
                                 mma_bf16(dbase + cl * C::BN, ad, bd, idesc, first ? 0u : 1u);
                             }
                         }
