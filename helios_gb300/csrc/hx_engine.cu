@@ -376,7 +376,8 @@ static void build_plan(hx_ccsd *h)
         P[G_FVOO].h.push_back(tg(m.gov, m.u, m.Foo2, 1, o, o, v * ov, o, o, ov, {0, (long long)v * ov, ov, 1, 0}, {0, (long long)v * ov, ov, 1, 0}, {0, o, 0, 1, 0}, 1.0, 1.0, mi));
         //    E_ij^ab = sum_c t_ij^ac F'_bc - sum_k t_ik^ab F'_kj
         P[G_E1].h.push_back(tg(m.t2, m.Fvv2, m.X2, 1, o * v * o, v, v, o * v * o, v, v, {0, v, 0, 1, 0}, {0, v, 0, 1, 0}, {0, v, 0, 1, 0}, 1.0, 1.0, mi));
-        P[G_E2].h.push_back(tg(m.Foo2, m.t2, m.X2, ov, o, v, o, o, v, o, {0, 1, 0, o, 0}, {0, 1, 0, v, ov}, {0, v, 0, 1, ov}, -1.0, 1.0, mi));
+        //    (one GEMM per molecule: N runs over (ia, b), so C rows are contiguous in b)
+        P[G_E2].h.push_back(tg(m.Foo2, m.t2, m.X2, 1, o, ov * v, o, o, v, o, {0, 1, 0, o, 0}, {ov, 1, 0, v, 0}, {0, v, ov, 1, 0}, -1.0, 1.0, mi));
         // singles: r1 = F~_ai + sum_kc u_ik^ac F~_kc + sum_kcd u_ki^cd (ad|kc)~ - sum_klc u_kl^ac (ki|lc)~
         P[G_S1].h.push_back(tg(m.u, m.Fd + o, m.r1, 1, ov, 1, ov, ov, 1, v, {0, ov, v, 1, 0}, {0, 0, N, 1, 0}, {0, 1, 0, 0, 0}, 1.0, 1.0, mi));
         P[G_S1].h.push_back(tg(m.u, m.Bov0, m.U, 1, ov, N, ov, ov, N, ov, {0, ov, 0, 1, 0}, {0, ov, 0, 1, 0}, {0, N, 0, 1, 0}, 1.0, 0.0, mi));

@@ -76,7 +76,7 @@ namespace tc {
 // while a sixth slice alone changed nothing; LOW and MID are limited by their
 // slices. These errors set the residual level a phase can reach (the GEMM
 // outputs are ~1e3-1e4 times the residual they cancel down to).
-template <int S_, int QMAX_, int NX_, int BN_, int STAGES_, int KC_, int EPIW_, int BK_ = 64>
+template <int S_, int QMAX_, int NX_, int BN_, int STAGES_, int KC_, int EPIW_, int BK_, int STG_>
 struct Cfg {
     static constexpr int S = S_;                     // integer slices per FP64 operand
     static constexpr int QMAX = QMAX_;               // slice pairs with i + j <= QMAX are multiplied
@@ -93,7 +93,9 @@ struct Cfg {
     static constexpr int ATILE = BM * BK * 2;        // bytes per A slice tile
     static constexpr int BTILE = BN * BK * 2;        // bytes per B slice tile
     static constexpr int STAGE_BYTES = S * (ATILE + BTILE);
-    static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+    static constexpr int STG_ROWS = STG_;            // output rows staged at a time
+    static constexpr int STG_BYTES = STG_ * (BN_ + 1) * 8 + 128 * 12;   // strip + row offsets and exponents
+    static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + STG_BYTES + 1024 + 256;
     static constexpr int EPI_COLS = BN / (EPIW_ / 4); // columns drained per epilogue thread
     // 7-slice mode: the exact classes are drained into an int64 per element
     // (units of 2^-8(NX-1)); the other modes use an FP32 (hi, lo) pair
@@ -107,17 +109,19 @@ struct Cfg {
     static_assert((long long)XPAIRS * KC_ * BK_ * 16384LL < (1LL << 24), "chunk too deep for exact sums");
     static_assert(BK_ == 64 || BK_ == 32, "k-block depth");
     static_assert(2 * NQ * BN_ <= 512, "two TMEM buffers must fit in 512 columns");
-    static_assert(STAGES_ * S_ * (128 * BK_ * 2 + BN_ * BK_ * 2) + 1280 <= 232448, "shared memory");
+    static_assert(STAGES_ * S_ * (128 * BK_ * 2 + BN_ * BK_ * 2) + STG_ * (BN_ + 1) * 8 + 128 * 12 + 1280 <= 232448,
+                  "shared memory");
+    static_assert(128 % STG_ == 0 && STG_ >= 8, "staging strip");
     static_assert(EPIW_ % 4 == 0 && EPI_COLS % 8 == 0, "epilogue split");
-    static_assert(128 * (BN_ + 1) * 8 + 128 * 12 <= STAGES_ * STAGE_BYTES, "output tile staging fits in the TMA ring");
     static_assert(EPIW_ * 32 >= 128 && EPIW_ * 32 >= BN_, "epilogue threads cover the tile's rows and columns");
     // int64 drain: a chunk adds below 2^(24 + 8(NX-1) + 1); 32 chunks stay below 2^63
     static_assert(!INT_DRAIN || 24 + 8 * (NX_ - 1) + 1 + 5 < 63, "int64 drain headroom");
 };
-using Low = Cfg<3, 3, 1, 96, 2, 8, 12>;
-using Mid = Cfg<4, 3, 2, 80, 2, 6, 8>;
-using High = Cfg<6, 5, 4, 48, 3, 7, 8, 32>;
-using Exact = Cfg<7, 6, 5, 32, 3, 6, 8, 32>;
+// (the strip heights are what each ring leaves of the 227 KB per CTA)
+using Low = Cfg<3, 3, 1, 96, 2, 8, 12, 64, 64>;
+using Mid = Cfg<4, 3, 2, 80, 2, 6, 8, 64, 16>;
+using High = Cfg<6, 5, 4, 48, 3, 7, 8, 32, 64>;
+using Exact = Cfg<7, 6, 5, 32, 3, 6, 8, 32, 32>;
 constexpr int TMEM_COLS = 512;
 constexpr int BM = 128, KPAD = 64;   // K is padded to KPAD (the slicing tile depth)
 constexpr unsigned long long WAIT_NS = 4000000000ull; // a wait longer than 4 s is declared failed
@@ -417,49 +421,75 @@ __global__ void __launch_bounds__(PT_THREADS) split_gather(const PrepDesc *__res
 }
 
 // ------------------------------------------------------------------ the GEMM
+// Work of one output tile: its problem, batch entry, tile row and column,
+// k-block range and chunks (grouped rasterisation: 16 tile-rows per group
+// keep A and B blocks L2-resident).
+struct TileWork {
+    int di, bt, tm, tn, kb0, nkb, nchunk;
+};
 template <class C>
-__global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restrict__ descs, int ndesc,
-                                                        const int *__restrict__ active, int *err)
+__device__ __forceinline__ TileWork tile_work(const TcDesc *__restrict__ descs, int ndesc, long long tile)
 {
-    extern __shared__ __align__(1024) uint8_t smem_raw[];
-    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t *full = (uint64_t *)(smem + C::STAGES * C::STAGE_BYTES);
-    uint64_t *empty = full + C::STAGES;
-    uint64_t *acc_full = empty + C::STAGES;      // [2] MMA -> epilogue: chunk done in buffer b
-    uint64_t *acc_empty = acc_full + 2;       // [2] epilogue -> MMA: buffer b drained
-    uint32_t *tmem_slot = (uint32_t *)(acc_empty + 2);
-    __shared__ int s_d;
-
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const long long tile = blockIdx.x;
-    if (threadIdx.x == 0) {
-        int lo = 0, hi = ndesc - 1;
-        while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (descs[mid].tile_start <= tile) lo = mid; else hi = mid - 1;
-        }
-        s_d = lo;
+    TileWork w;
+    int lo = 0, hi = ndesc - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (descs[mid].tile_start <= tile) lo = mid; else hi = mid - 1;
     }
-    __syncthreads();
-    const TcDesc &d = descs[s_d];
-    if (active && !active[d.mol]) return;
+    w.di = lo;
+    const TcDesc &d = descs[lo];
     long long local = tile - d.tile_start;
     const int ks = (int)(local % d.ksplit);
     local /= d.ksplit;
     const long long per_batch = (long long)d.tiles_m * d.tiles_n;
-    const int bt = (int)(local / per_batch);
-    local -= bt * per_batch;
-    // grouped rasterisation: 16 tile-rows per group keep A and B blocks L2-resident
+    w.bt = (int)(local / per_batch);
+    local -= w.bt * per_batch;
     const int GM = 16;
     const int group = (int)(local / (GM * d.tiles_n));
     const int first_m = group * GM;
     const int gsz = min(d.tiles_m - first_m, GM);
     const int in_g = (int)(local % (GM * d.tiles_n));
-    const int tm = first_m + in_g % gsz, tn = in_g / gsz;
-    const int kb0 = ks * d.kb_per;
-    const int nkb = min(d.Kp / C::BK - kb0, d.kb_per);  // >= 1 by construction
-    const int nchunk = (nkb + C::KC - 1) / C::KC;
+    w.tm = first_m + in_g % gsz;
+    w.tn = in_g / gsz;
+    w.kb0 = ks * d.kb_per;
+    w.nkb = min(d.Kp / C::BK - w.kb0, d.kb_per);  // >= 1 by construction
+    w.nchunk = (w.nkb + C::KC - 1) / C::KC;
+    return w;
+}
 
+// AND of v over the epilogue threads (named barrier 1), so that they leave
+// the tile loop together and never wait at a named barrier for one another
+template <int NT>
+__device__ __forceinline__ bool epilogue_all(bool v)
+{
+    uint32_t r;
+    asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.and.pred q, 1, %2, p;\n\t"
+                 "selp.u32 %0, 1, 0, q;\n\t}" : "=r"(r) : "r"((uint32_t)v), "n"(NT) : "memory");
+    return r != 0;
+}
+
+// Persistent: CTA b computes tiles b, b + gridDim.x, ... The producer warp
+// streams k-blocks through the TMA ring and the MMA warp fills the two TMEM
+// buffers with one running count each across tiles, so loads and MMAs of the
+// next tile overlap the epilogue of the previous one; the epilogue stages the
+// output in its own shared-memory strip, STG_ROWS rows at a time.
+template <class C>
+__global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restrict__ descs, int ndesc, long long ntiles,
+                                                        const int *__restrict__ active, int *err)
+{
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    constexpr int LD = C::BN + 1;
+    double *strip = (double *)(smem + C::STAGES * C::STAGE_BYTES);   // [STG_ROWS][BN + 1] output staging
+    long long *srow = (long long *)(strip + C::STG_ROWS * LD);       // [BM] row offsets into C
+    int *sexp = (int *)(srow + BM);                                   // [BM] row exponents of A
+    uint64_t *full = (uint64_t *)(sexp + BM);
+    uint64_t *empty = full + C::STAGES;
+    uint64_t *acc_full = empty + C::STAGES;      // [2] MMA -> epilogue: chunk done in buffer b
+    uint64_t *acc_empty = acc_full + 2;       // [2] epilogue -> MMA: buffer b drained
+    uint32_t *tmem_slot = (uint32_t *)(acc_empty + 2);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
         for (int s = 0; s < C::STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
         for (int b = 0; b < 2; ++b) { mbar_init(&acc_full[b], 1); mbar_init(&acc_empty[b], C::EPI_THREADS); }
@@ -479,71 +509,82 @@ __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restri
 
     if (warp == WP) {
         if (lane == 0) {
-            const int arow0 = bt * d.Mp + tm * BM, brow0 = bt * d.Np + tn * C::BN;
-            const int aplane = d.batch * d.Mp, bplane = d.batch * d.Np;
-            for (int kb = 0; kb < nkb && ok; ++kb) {
-                const int st = kb % C::STAGES;
-                const uint32_t ph = (kb / C::STAGES) & 1;
-                ok = mbar_wait(&empty[st], ph ^ 1, err, 1);
-                if (!ok) break;
-                uint8_t *sa = smem + st * C::STAGE_BYTES;
-                uint8_t *sb = sa + C::S * C::ATILE;
-                mbar_expect_tx(&full[st], C::STAGE_BYTES);
-                for (int p = 0; p < C::S; ++p) {
-                    tma_load_2d(sa + p * C::ATILE, &d.mapA, &full[st], (kb0 + kb) * C::BK, p * aplane + arow0);
-                    tma_load_2d(sb + p * C::BTILE, &d.mapB, &full[st], (kb0 + kb) * C::BK, p * bplane + brow0);
+            long long g = 0;                                  // k-blocks loaded so far
+            for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+                const TileWork w = tile_work<C>(descs, ndesc, tile);
+                const TcDesc &d = descs[w.di];
+                if (active && !active[d.mol]) continue;
+                const int arow0 = w.bt * d.Mp + w.tm * BM, brow0 = w.bt * d.Np + w.tn * C::BN;
+                const int aplane = d.batch * d.Mp, bplane = d.batch * d.Np;
+                for (int kb = 0; kb < w.nkb && ok; ++kb, ++g) {
+                    const int st = (int)(g % C::STAGES);
+                    const uint32_t ph = (uint32_t)((g / C::STAGES) & 1);
+                    ok = mbar_wait(&empty[st], ph ^ 1, err, 1);
+                    if (!ok) break;
+                    uint8_t *sa = smem + st * C::STAGE_BYTES;
+                    uint8_t *sb = sa + C::S * C::ATILE;
+                    mbar_expect_tx(&full[st], C::STAGE_BYTES);
+                    for (int p = 0; p < C::S; ++p) {
+                        tma_load_2d(sa + p * C::ATILE, &d.mapA, &full[st], (w.kb0 + kb) * C::BK, p * aplane + arow0);
+                        tma_load_2d(sb + p * C::BTILE, &d.mapB, &full[st], (w.kb0 + kb) * C::BK, p * bplane + brow0);
+                    }
                 }
             }
         }
     } else if (warp == WM) {
         if (lane == 0) {
             const uint32_t idesc = idesc_bf16(BM, C::BN);
-            for (int c = 0; c < nchunk && ok; ++c) {
-                const int buf = c & 1;
-                const uint32_t use = (uint32_t)(c >> 1);
-                ok = mbar_wait(&acc_empty[buf], (use & 1) ^ 1, err, 4);
-                if (!ok) break;
-                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const uint32_t dbase = tmem + (uint32_t)(buf * C::NQ * C::BN);
-                const int kend = min(nkb, (c + 1) * C::KC);
-                for (int kb = c * C::KC; kb < kend && ok; ++kb) {
-                    const int st = kb % C::STAGES;
-                    const uint32_t ph = (kb / C::STAGES) & 1;
-                    ok = mbar_wait(&full[st], ph, err, 2);
+            long long g = 0, gc = 0;                          // k-blocks and chunks consumed so far
+            for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+                const TileWork w = tile_work<C>(descs, ndesc, tile);
+                if (active && !active[descs[w.di].mol]) continue;
+                for (int c = 0; c < w.nchunk && ok; ++c, ++gc) {
+                    const int buf = (int)(gc & 1);
+                    const uint32_t use = (uint32_t)(gc >> 1);
+                    ok = mbar_wait(&acc_empty[buf], (use & 1) ^ 1, err, 4);
                     if (!ok) break;
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                    const uint32_t sa = smem_u32(smem + st * C::STAGE_BYTES);
-                    const uint32_t sb = sa + C::S * C::ATILE;
-                    const bool chunk_start = kb == c * C::KC;
-                    // descriptors of the stage's first slices; the others differ
-                    // only in the start-address field (address / 16, 14 bits:
-                    // shared memory stays below 256 KB, so adding never carries)
-                    const uint64_t a0 = smem_desc<C>(sa), b0 = smem_desc<C>(sb);
+                    const uint32_t dbase = tmem + (uint32_t)(buf * C::NQ * C::BN);
+                    const int kend = min(w.nkb, (c + 1) * C::KC);
+                    for (int kb = c * C::KC; kb < kend && ok; ++kb, ++g) {
+                        const int st = (int)(g % C::STAGES);
+                        const uint32_t ph = (uint32_t)((g / C::STAGES) & 1);
+                        ok = mbar_wait(&full[st], ph, err, 2);
+                        if (!ok) break;
+                        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                        const uint32_t sa = smem_u32(smem + st * C::STAGE_BYTES);
+                        const uint32_t sb = sa + C::S * C::ATILE;
+                        const bool chunk_start = kb == c * C::KC;
+                        // descriptors of the stage's first slices; the others differ
+                        // only in the start-address field (address / 16, 14 bits:
+                        // shared memory stays below 256 KB, so adding never carries)
+                        const uint64_t a0 = smem_desc<C>(sa), b0 = smem_desc<C>(sb);
 #pragma unroll
-                    for (int kk = 0; kk < C::BK / 16; ++kk) {
+                        for (int kk = 0; kk < C::BK / 16; ++kk) {
 #pragma unroll
-                        for (int i = 0; i < C::S; ++i) {
+                            for (int i = 0; i < C::S; ++i) {
 #pragma unroll
-                            for (int j = 0; j < C::S; ++j) {
-                                const int q = i + j;
-                                if (q > C::QMAX) continue;
-                                const int cl = C::cls(q);
-                                // the first product of a class in the chunk overwrites its
-                                // accumulator: issue order is kk, i, j, so that is the pair
-                                // with the smallest i of the class at kk = 0
-                                const int i_first = cl < C::NX ? (cl < C::S ? 0 : cl - (C::S - 1))
-                                                               : (C::NX < C::S ? 0 : C::NX - (C::S - 1));
-                                const bool first = chunk_start && kk == 0 && i == i_first &&
-                                                   (cl < C::NX || j == C::NX - i_first);
-                                const uint64_t ad = a0 + (uint64_t)((i * C::ATILE + kk * 32) >> 4);
-                                const uint64_t bd = b0 + (uint64_t)((j * C::BTILE + kk * 32) >> 4);
-                                mma_bf16(dbase + cl * C::BN, ad, bd, idesc, first ? 0u : 1u);
+                                for (int j = 0; j < C::S; ++j) {
+                                    const int q = i + j;
+                                    if (q > C::QMAX) continue;
+                                    const int cl = C::cls(q);
+                                    // the first product of a class in the chunk overwrites its
+                                    // accumulator: issue order is kk, i, j, so that is the pair
+                                    // with the smallest i of the class at kk = 0
+                                    const int i_first = cl < C::NX ? (cl < C::S ? 0 : cl - (C::S - 1))
+                                                                   : (C::NX < C::S ? 0 : C::NX - (C::S - 1));
+                                    const bool first = chunk_start && kk == 0 && i == i_first &&
+                                                       (cl < C::NX || j == C::NX - i_first);
+                                    const uint64_t ad = a0 + (uint64_t)((i * C::ATILE + kk * 32) >> 4);
+                                    const uint64_t bd = b0 + (uint64_t)((j * C::BTILE + kk * 32) >> 4);
+                                    mma_bf16(dbase + cl * C::BN, ad, bd, idesc, first ? 0u : 1u);
+                                }
                             }
                         }
+                        mma_commit(&empty[st]);
                     }
-                    mma_commit(&empty[st]);
+                    mma_commit(&acc_full[buf]);
                 }
-                mma_commit(&acc_full[buf]);
             }
         }
     } else {
@@ -552,109 +593,124 @@ __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restri
         const int row = (warp & 3) * 32 + lane;
         const int col0 = (warp >> 2) * C::EPI_COLS;
         const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
-        float hi[C::EPI_COLS], lo[C::EPI_COLS];
-        // INT_DRAIN: each exact class of a chunk is an integer count of
-        // 2^-8q below 2^24, so a[q] 2^8(NX-1) is an integer below 2^56 and
-        // one int64 sums every exact class of up to 32 chunks without
-        // rounding; every 32 chunks it moves into an FP64 sum. The merged
-        // class (about 2^-8NX of the value) is summed in FP32.
-        long long iacc[C::EPI_COLS];
-        double dacc[C::EPI_COLS];
-        float macc[C::EPI_COLS];
-#pragma unroll
-        for (int e = 0; e < C::EPI_COLS; ++e) { hi[e] = 0.f; lo[e] = 0.f; iacc[e] = 0; dacc[e] = 0.0; macc[e] = 0.f; }
-        for (int c = 0; c < nchunk; ++c) {
-            const int buf = c & 1;
-            const uint32_t use = (uint32_t)(c >> 1);
-            if (ok) ok = mbar_wait(&acc_full[buf], use & 1, err, 3);
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll
-            for (int c0 = 0; c0 < C::EPI_COLS; c0 += 8) {
-                // chunk value of 8 columns: the classes (exact ones first) summed
-                // by TwoSum, then added into (hi, lo); rounding errors go to lo
-                float a[C::NQ][8];
-#pragma unroll
-                for (int q = 0; q < C::NQ; ++q)
-                    tmem_ld8(tmem + lane_base + (uint32_t)(buf * C::NQ * C::BN + q * C::BN + col0 + c0), a[q]);
-                if constexpr (C::INT_DRAIN) {
-#pragma unroll
-                    for (int e = 0; e < 8; ++e) {
-                        long long v = 0;
-#pragma unroll
-                        for (int q = 0; q < C::NX; ++q) v += __float2ll_rn(a[q][e] * C::DRAIN_SCALE);
-                        iacc[c0 + e] += v;
-                        if constexpr (C::NQ > C::NX) macc[c0 + e] += a[C::NX][e];
-                    }
-                } else {
-#pragma unroll
-                    for (int e = 0; e < 8; ++e) {
-                        float x = a[0][e], err = 0.f;
-#pragma unroll
-                        for (int q = 1; q < C::NQ; ++q) {
-                            const float sq = x + a[q][e];
-                            const float bq = sq - x;
-                            err += (x - (sq - bq)) + (a[q][e] - bq);
-                            x = sq;
-                        }
-                        const float sh = hi[c0 + e] + x;
-                        const float bh = sh - hi[c0 + e];
-                        lo[c0 + e] += ((hi[c0 + e] - (sh - bh)) + (x - bh)) + err;
-                        hi[c0 + e] = sh;
-                    }
-                }
-            }
-            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-            mbar_arrive(&acc_empty[buf]);
-            if constexpr (C::INT_DRAIN) {
-                if ((c & 31) == 31) {
-#pragma unroll
-                    for (int e = 0; e < C::EPI_COLS; ++e) { dacc[e] += (double)iacc[e]; iacc[e] = 0; }
-                }
-            }
-        }
-        // every chunk is drained, so the TMA ring is idle: stage the tile in its
-        // shared memory with the row offsets and exponents of C, then write the
-        // valid part of the tile: one fixed column per thread (consecutive
-        // threads on consecutive n), rows RSTEP apart, U rows of C read ahead
-        constexpr int LD = C::BN + 1;
-        double *stile = (double *)smem;                      // [BM][BN + 1]
-        long long *srow = (long long *)(stile + BM * LD);    // [BM] row offsets into C
-        int *sexp = (int *)(srow + BM);                      // [BM] row exponents of A
-#pragma unroll
-        for (int e = 0; e < C::EPI_COLS; ++e)
-            stile[row * LD + col0 + e] = C::INT_DRAIN ? (dacc[e] + (double)iacc[e]) / (double)C::DRAIN_SCALE + (double)macc[e]
-                                                      : (double)hi[e] + (double)lo[e];
-        const int mv = min(BM, d.M - tm * BM), nv = min(C::BN, d.N - tn * C::BN);
-        if (threadIdx.x < mv) {
-            const int m = tm * BM + threadIdx.x;
-            srow[threadIdx.x] = split_off(m, d.Mi, d.c[0], d.c[1]);
-            sexp[threadIdx.x] = d.expA[(long long)bt * d.Mp + m];
-        }
-        asm volatile("bar.sync 1, %0;" ::"r"(C::EPI_THREADS) : "memory");
-        constexpr int RSTEP = C::EPI_THREADS / C::BN, U = 8;
+        // store: one fixed column per thread (consecutive threads on
+        // consecutive n), rows RSTEP apart, U rows of C read ahead
+        constexpr int RSTEP = C::EPI_THREADS / C::BN, U = 4;
         const int nn = threadIdx.x % C::BN, rr = threadIdx.x / C::BN;
-        if (ok && rr < RSTEP && nn < nv) {
-            const int n = tn * C::BN + nn;
-            const int eb = d.expB[(long long)bt * d.Np + n];
-            double *Cn = d.C + (long long)bt * d.c[4] + split_off(n, d.Ni, d.c[2], d.c[3]);
-            const bool load_c = d.ksplit == 1 && d.beta != 0.0;
-            for (int m0 = rr; m0 < mv; m0 += RSTEP * U) {
-                double old[U];
+        long long gc = 0;                                     // chunks drained so far
+        for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+            const TileWork w = tile_work<C>(descs, ndesc, tile);
+            const TcDesc &d = descs[w.di];
+            if (active && !active[d.mol]) continue;
+            float hi[C::EPI_COLS], lo[C::EPI_COLS];
+            // INT_DRAIN: each exact class of a chunk is an integer count of
+            // 2^-8q below 2^24, so a[q] 2^8(NX-1) is an integer below 2^56 and
+            // one int64 sums every exact class of up to 32 chunks without
+            // rounding; every 32 chunks it moves into an FP64 sum. The merged
+            // class (about 2^-8NX of the value) is summed in FP32.
+            long long iacc[C::EPI_COLS];
+            double dacc[C::EPI_COLS];
+            float macc[C::EPI_COLS];
 #pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    const int mm = m0 + u * RSTEP;
-                    old[u] = (load_c && mm < mv) ? Cn[srow[mm]] : 0.0;
+            for (int e = 0; e < C::EPI_COLS; ++e) { hi[e] = 0.f; lo[e] = 0.f; iacc[e] = 0; dacc[e] = 0.0; macc[e] = 0.f; }
+            for (int c = 0; c < w.nchunk; ++c, ++gc) {
+                const int buf = (int)(gc & 1);
+                const uint32_t use = (uint32_t)(gc >> 1);
+                if (ok) ok = mbar_wait(&acc_full[buf], use & 1, err, 3);
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+                for (int c0 = 0; c0 < C::EPI_COLS; c0 += 8) {
+                    // chunk value of 8 columns: the classes (exact ones first) summed
+                    // by TwoSum, then added into (hi, lo); rounding errors go to lo
+                    float a[C::NQ][8];
+#pragma unroll
+                    for (int q = 0; q < C::NQ; ++q)
+                        tmem_ld8(tmem + lane_base + (uint32_t)(buf * C::NQ * C::BN + q * C::BN + col0 + c0), a[q]);
+                    if constexpr (C::INT_DRAIN) {
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) {
+                            long long v = 0;
+#pragma unroll
+                            for (int q = 0; q < C::NX; ++q) v += __float2ll_rn(a[q][e] * C::DRAIN_SCALE);
+                            iacc[c0 + e] += v;
+                            if constexpr (C::NQ > C::NX) macc[c0 + e] += a[C::NX][e];
+                        }
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) {
+                            float x = a[0][e], err = 0.f;
+#pragma unroll
+                            for (int q = 1; q < C::NQ; ++q) {
+                                const float sq = x + a[q][e];
+                                const float bq = sq - x;
+                                err += (x - (sq - bq)) + (a[q][e] - bq);
+                                x = sq;
+                            }
+                            const float sh = hi[c0 + e] + x;
+                            const float bh = sh - hi[c0 + e];
+                            lo[c0 + e] += ((hi[c0 + e] - (sh - bh)) + (x - bh)) + err;
+                            hi[c0 + e] = sh;
+                        }
+                    }
                 }
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                mbar_arrive(&acc_empty[buf]);
+                if constexpr (C::INT_DRAIN) {
+                    if ((c & 31) == 31) {
 #pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    const int mm = m0 + u * RSTEP;
-                    if (mm >= mv) break;
-                    const double r = d.alpha * scale_pow2(stile[mm * LD + nn], sexp[mm], eb);
-                    double *p = Cn + srow[mm];
-                    if (d.ksplit > 1) atomicAdd(p, r);
-                    else *p = load_c ? r + d.beta * old[u] : r;
+                        for (int e = 0; e < C::EPI_COLS; ++e) { dacc[e] += (double)iacc[e]; iacc[e] = 0; }
+                    }
                 }
             }
+            // the tile is drained: row offsets and exponents of C, then the
+            // valid rows STG_ROWS at a time through the strip
+            const int mv = min(BM, d.M - w.tm * BM), nv = min(C::BN, d.N - w.tn * C::BN);
+            if (threadIdx.x < mv) {
+                const int m = w.tm * BM + threadIdx.x;
+                srow[threadIdx.x] = split_off(m, d.Mi, d.c[0], d.c[1]);
+                sexp[threadIdx.x] = d.expA[(long long)w.bt * d.Mp + m];
+            }
+            int eb = 0;
+            double *Cn = nullptr;
+            if (rr < RSTEP && nn < nv) {
+                const int n = w.tn * C::BN + nn;
+                eb = d.expB[(long long)w.bt * d.Np + n];
+                Cn = d.C + (long long)w.bt * d.c[4] + split_off(n, d.Ni, d.c[2], d.c[3]);
+            }
+            const bool load_c = d.ksplit == 1 && d.beta != 0.0;
+            for (int r0 = 0; r0 < mv; r0 += C::STG_ROWS) {
+                if (row >= r0 && row < r0 + C::STG_ROWS) {
+#pragma unroll
+                    for (int e = 0; e < C::EPI_COLS; ++e)
+                        strip[(row - r0) * LD + col0 + e] =
+                            C::INT_DRAIN ? (dacc[e] + (double)iacc[e]) / (double)C::DRAIN_SCALE + (double)macc[e]
+                                         : (double)hi[e] + (double)lo[e];
+                }
+                asm volatile("bar.sync 1, %0;" ::"r"(C::EPI_THREADS) : "memory");
+                const int rend = min(r0 + C::STG_ROWS, mv);
+                if (ok && Cn) {
+                    for (int m0 = r0 + rr; m0 < rend; m0 += RSTEP * U) {
+                        double old[U];
+#pragma unroll
+                        for (int u = 0; u < U; ++u) {
+                            const int mm = m0 + u * RSTEP;
+                            old[u] = (load_c && mm < rend) ? Cn[srow[mm]] : 0.0;
+                        }
+#pragma unroll
+                        for (int u = 0; u < U; ++u) {
+                            const int mm = m0 + u * RSTEP;
+                            if (mm >= rend) break;
+                            const double r = d.alpha * scale_pow2(strip[(mm - r0) * LD + nn], sexp[mm], eb);
+                            double *p = Cn + srow[mm];
+                            if (d.ksplit > 1) atomicAdd(p, r);
+                            else *p = load_c ? r + d.beta * old[u] : r;
+                        }
+                    }
+                }
+                asm volatile("bar.sync 1, %0;" ::"r"(C::EPI_THREADS) : "memory");
+            }
+            ok = epilogue_all<C::EPI_THREADS>(ok);
+            if (!ok) break;
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -699,6 +755,7 @@ struct Engine {
     std::vector<Pending> pending;
     std::vector<cudaEvent_t> pool;
     double tot[4] = {0, 0, 0, 0};
+    int nsm = 152;                       // SMs of the device: CTAs of a persistent launch
 };
 
 static cudaEvent_t take_event(Engine *e)
@@ -904,6 +961,13 @@ int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s)
 {
     *out = nullptr;
     Engine *e = new Engine();
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&e->nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || e->nsm < 1) {
+        delete e;
+        hx_set_error("cannot query the device's multiprocessor count");
+        return HX_ERR_CUDA;
+    }
     e->mode[0].BK = Low::BK; e->mode[1].BK = Mid::BK; e->mode[2].BK = High::BK; e->mode[3].BK = Exact::BK;
     e->mode[0].S = Low::S; e->mode[0].BN = Low::BN; e->mode[0].products = Low::PRODUCTS; e->mode[0].smem = Low::SMEM_BYTES;
     e->mode[1].S = Mid::S; e->mode[1].BN = Mid::BN; e->mode[1].products = Mid::PRODUCTS; e->mode[1].smem = Mid::SMEM_BYTES;
@@ -982,10 +1046,13 @@ cudaError_t run_group(Engine *e, const TgemmDesc *descs, int n, const int *d_act
         }
         cudaEventRecord(pend.a, s);
     }
-    if (mode == 0) tc_gemm<Low><<<(unsigned)sg.tiles, Low::NTHREADS, Low::SMEM_BYTES, s>>>(sg.d_tcd, (int)sg.tcd.size(), d_active, e->d_err);
-    else if (mode == 1) tc_gemm<Mid><<<(unsigned)sg.tiles, Mid::NTHREADS, Mid::SMEM_BYTES, s>>>(sg.d_tcd, (int)sg.tcd.size(), d_active, e->d_err);
-    else if (mode == 2) tc_gemm<High><<<(unsigned)sg.tiles, High::NTHREADS, High::SMEM_BYTES, s>>>(sg.d_tcd, (int)sg.tcd.size(), d_active, e->d_err);
-    else tc_gemm<Exact><<<(unsigned)sg.tiles, Exact::NTHREADS, Exact::SMEM_BYTES, s>>>(sg.d_tcd, (int)sg.tcd.size(), d_active, e->d_err);
+    // persistent: one CTA per SM (shared memory allows one), each looping over tiles
+    const unsigned grid = (unsigned)std::min<long long>(sg.tiles, e->nsm);
+    const int nd = (int)sg.tcd.size();
+    if (mode == 0) tc_gemm<Low><<<grid, Low::NTHREADS, Low::SMEM_BYTES, s>>>(sg.d_tcd, nd, sg.tiles, d_active, e->d_err);
+    else if (mode == 1) tc_gemm<Mid><<<grid, Mid::NTHREADS, Mid::SMEM_BYTES, s>>>(sg.d_tcd, nd, sg.tiles, d_active, e->d_err);
+    else if (mode == 2) tc_gemm<High><<<grid, High::NTHREADS, High::SMEM_BYTES, s>>>(sg.d_tcd, nd, sg.tiles, d_active, e->d_err);
+    else tc_gemm<Exact><<<grid, Exact::NTHREADS, Exact::SMEM_BYTES, s>>>(sg.d_tcd, nd, sg.tiles, d_active, e->d_err);
     r = cudaGetLastError();
     if (e->profile) {
         cudaEventRecord(pend.b, s);
@@ -1157,8 +1224,9 @@ extern "C" int hx_gemm_noalloc(const double *dA, const double *dB, double *dC, i
     if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_prep, p, sizeof(p), cudaMemcpyHostToDevice, s);
     if (ce == cudaSuccess) {
         ce = prep_launch(d_prep, 2, work, rows, S, nullptr, s);
-        if (ce == cudaSuccess && high) tc_gemm<High><<<(unsigned)tiles, High::NTHREADS, High::SMEM_BYTES, s>>>(d_tcd, 1, nullptr, err);
-        else if (ce == cudaSuccess) tc_gemm<Low><<<(unsigned)tiles, Low::NTHREADS, Low::SMEM_BYTES, s>>>(d_tcd, 1, nullptr, err);
+        // one CTA per tile (the kernel's tile loop then runs once per CTA)
+        if (ce == cudaSuccess && high) tc_gemm<High><<<(unsigned)tiles, High::NTHREADS, High::SMEM_BYTES, s>>>(d_tcd, 1, tiles, nullptr, err);
+        else if (ce == cudaSuccess) tc_gemm<Low><<<(unsigned)tiles, Low::NTHREADS, Low::SMEM_BYTES, s>>>(d_tcd, 1, tiles, nullptr, err);
         hx_count_launches(1);
         if (ce == cudaSuccess) ce = cudaGetLastError();
     }
