@@ -355,11 +355,14 @@ static void build_plan(hx_ccsd *h)
         //   sum_cd (ac|bd)~ t_ij^cd = sum_mu,nu X_mu,a X_nu,b G_mu,nu [sum_cd C_mu,c C_nu,d t_ij^cd]
         P[G_LAD_A].h.push_back(tg(m.t2, Cmo + o, m.T1s, 1, o * v * o, N, v, o * v * o, N, v, {0, v, 0, 1, 0}, {0, N, 0, 1, 0}, {0, N, 0, 1, 0}, 1.0, 0.0, mi));
         P[G_LAD_B].h.push_back(tg(Cmo + o, m.T1s, m.Ts, o, N, o * N, v, N, o * N, v, {0, N, 0, 1, 0}, {0, 1, 0, (long long)o * N, (long long)v * o * N}, {0, (long long)o * N, 0, 1, (long long)N * o * N}, 1.0, 0.0, mi));
-        P[G_LAD_D].h.push_back(tg(m.Ts, m.X + o, m.Z1, 1, o * N * o, v, N, o * N * o, v, N, {0, N, 0, 1, 0}, {0, 1, 0, N, 0}, {0, v, 0, 1, 0}, 1.0, 0.0, mi));
-        P[G_LAD_E].h.push_back(tg(m.X + o, m.Z1, m.r2, o, v, ov, N, v, ov, N, {0, 1, 0, N, 0}, {0, 1, 0, ov, (long long)N * ov}, {0, ov, 0, 1, (long long)v * ov}, 1.0, 1.0, mi));
+        //   Z = Ts X: its virtual columns (X_v = Cv - Co t1) close the ladder, its
+        //   occupied ones (X_o = Co exactly: the dressing leaves them) feed the
+        //   hole-hole intermediate below -- one product, one slicing of Ts
+        P[G_LAD_D].h.push_back(tg(m.Ts, m.X, m.Z, 1, o * N * o, N, N, o * N * o, N, N, {0, N, 0, 1, 0}, {0, 1, 0, N, 0}, {0, N, 0, 1, 0}, 1.0, 0.0, mi));
+        P[G_LAD_E].h.push_back(tg(m.X + o, m.Z + o, m.r2, o, v, ov, N, v, v, N, {0, 1, 0, N, 0}, {N, 1, 0, (long long)o * N, (long long)N * o * N}, {0, ov, v, 1, (long long)v * ov}, 1.0, 1.0, mi));
         // hole-hole ladder: W_klij = (ki|lj)~ + sum_cd t_ij^cd (kc|ld), the latter through the site basis
-        P[G_W_D].h.push_back(tg(m.Ts, Cmo, m.Zo, 1, o * N * o, o, N, o * N * o, o, N, {0, N, 0, 1, 0}, {0, 1, 0, N, 0}, {0, o, 0, 1, 0}, 1.0, 0.0, mi));
-        P[G_W_E].h.push_back(tg(Cmo, m.Zo, m.Woo, o, o, o * o, N, o, o * o, N, {0, 1, 0, N, 0}, {0, 1, 0, o * o, (long long)N * o * o}, {0, o * o, 0, 1, (long long)o * o * o}, 1.0, 0.0, mi));
+        //   (G_W_D stays empty: Z's occupied columns are the former Zo = Ts Co)
+        P[G_W_E].h.push_back(tg(Cmo, m.Z, m.Woo, o, o, o * o, N, o, o, N, {0, 1, 0, N, 0}, {N, 1, 0, (long long)o * N, (long long)N * o * N}, {0, o * o, o, 1, (long long)o * o * o}, 1.0, 0.0, mi));
         P[G_W_INT].h.push_back(tg(m.Boo, m.GBoo, m.Woo, 1, o * o, o * o, N, o, o, N, {o, 1, 0, o * o, 0}, {o, 1, 0, o * o, 0}, {(long long)o * o, (long long)o * o * o, 1, o, 0}, 1.0, 1.0, mi));
         P[G_HH].h.push_back(tg(m.Woo, m.t2, m.r2, 1, o * o, v * v, o * o, o, v, o, {(long long)o * o * o, o, (long long)o * o, 1, 0}, {ov, 1, (long long)v * ov, v, 0}, {(long long)v * ov, v, ov, 1, 0}, 1.0, 1.0, mi));
         // C: Cint_kiac = (ki|ac)~ - 1/2 sum_ld t_li^ad (kd|lc);  C_ij^ab = -sum_kc t_kj^bc Cint_kiac
@@ -431,7 +434,7 @@ static int allocate(hx_ccsd *h)
             m.Boo = A.take<double>((size_t)N * o * o); m.GBoo = A.take<double>((size_t)N * o * o);
             m.Bvv = A.take<double>((size_t)N * v * v); m.GBvv = A.take<double>((size_t)N * v * v);
             m.T1s = A.take<double>((size_t)o * v * o * N); m.Ts = A.take<double>((size_t)o * N * o * N);
-            m.Z1 = A.take<double>((size_t)o * N * o * v); m.Zo = A.take<double>((size_t)o * N * o * o);
+            m.Z = A.take<double>((size_t)o * N * o * N);
             m.Woo = A.take<double>((size_t)o * o * o * o);
             m.Cint = A.take<double>(pr); m.Cp = A.take<double>(pr); m.Dint = A.take<double>(pr); m.X2 = A.take<double>(pr);
             m.Fvv2 = A.take<double>((size_t)v * v); m.Foo2 = A.take<double>((size_t)o * o);

@@ -41,7 +41,7 @@ struct CCMol {
     double *Boo, *GBoo;                   // [N][o*o]  X_mu,k Y_mu,i (index k*o+i)
     double *Bvv, *GBvv;                   // [N][v*v]  X_mu,a Y_mu,c (index a*v+c)
     // contraction scratch
-    double *T1s, *Ts, *Z1, *Zo, *Woo;     // ladder: o*v*o*N, o*N*o*N, o*N*o*v, o*N*o*o, o^4
+    double *T1s, *Ts, *Z, *Woo;           // ladder: o*v*o*N, o*N*o*N, Ts X: o*N*o*N, o^4
     double *Cint, *Cp, *Dint, *X2;        // o^2 v^2 each
     double *Fvv2, *Foo2;                  // v*v, o*o
     double *U, *UG, *Vs;                  // [o*v][N], [o*v][N], [o][N]
