@@ -311,12 +311,13 @@ struct PrepTile {
 // Stage tile `u` of the launch in shared memory (zero outside R x K); returns
 // false (uniformly) when its molecule is inactive.
 __device__ __forceinline__ bool load_tile(const PrepDesc *__restrict__ pd, int n, long long u, const int *active,
-                                          PrepTile &t, int &b, int &r0, int &k0)
+                                          PrepTile &t, int &b, int &r0, int &k0, bool skip_single = false)
 {
     if (threadIdx.x == 0) t.desc = find_desc(pd, n, u);
     __syncthreads();
     const PrepDesc &d = pd[t.desc];
     if (active && !active[d.mol]) return false;
+    if (skip_single && d.Kp == PT_K) return false;      // split_gather scales these rows itself
     long long local = u - d.work_start;
     const int tk = d.Kp / PT_K, tr = (d.Rp + PT_R - 1) / PT_R;
     k0 = (int)(local % tk) * PT_K;
@@ -356,7 +357,8 @@ __global__ void rexp_init(const PrepDesc *__restrict__ pd, int n, long long rows
 
 // Row exponents: e with max|row| < 2^e (frexp), combined over the k tiles of a row by
 // atomicMax (the list's exponents start at INT_MIN; a row that stays there is
-// all zero and is treated as e = 0).
+// all zero and is treated as e = 0). Operands with one k tile per row are left
+// to split_gather, which scales them from the tile it slices.
 __global__ void __launch_bounds__(PT_THREADS) row_scale(const PrepDesc *__restrict__ pd, int n, long long units,
                                                         const int *__restrict__ active)
 {
@@ -364,7 +366,7 @@ __global__ void __launch_bounds__(PT_THREADS) row_scale(const PrepDesc *__restri
     const int rr = threadIdx.x >> 3, part = threadIdx.x & 7;
     for (long long u = blockIdx.x; u < units; u += gridDim.x) {
         int b, r0, k0;
-        if (load_tile(pd, n, u, active, t, b, r0, k0)) {
+        if (load_tile(pd, n, u, active, t, b, r0, k0, true)) {
             const PrepDesc &d = pd[t.desc];
             // magnitudes compare as their bit patterns with the sign cleared
             unsigned long long mb = 0;
@@ -396,25 +398,47 @@ __global__ void __launch_bounds__(PT_THREADS) split_gather(const PrepDesc *__res
     const int rr = threadIdx.x >> 3, c8 = (threadIdx.x & 7) * 8;
     for (long long u = blockIdx.x; u < units; u += gridDim.x) {
         int b, r0, k0;
-        // (a partial last row tile has rows beyond Rp: they write nothing)
-        if (load_tile(pd, n, u, active, t, b, r0, k0) && r0 + rr < pd[t.desc].Rp) {
+        if (load_tile(pd, n, u, active, t, b, r0, k0)) {
             const PrepDesc &d = pd[t.desc];
-            int e = d.rexp[(long long)b * d.Rp + r0 + rr];
-            if (e == INT_MIN) e = 0;
-            __align__(16) __nv_bfloat16 out[S][8];
+            const bool in_rows = r0 + rr < d.Rp;  // a partial last row tile has rows beyond Rp: they write nothing
+            int e;
+            if (d.Kp == PT_K) {
+                // one k tile per row (K <= 64): the row's scale from this tile,
+                // so these operands skip row_scale (all lanes join the shuffle)
+                unsigned long long mb = 0;
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                int dg[S];
-                slice_digits<S>(t.x[rr][c8 + q], e, dg);
+                for (int q = 0; q < 8; ++q) {
+                    const unsigned long long v = dbits(t.x[rr][c8 + q]) & 0x7FFFFFFFFFFFFFFFull;
+                    mb = v > mb ? v : mb;
+                }
 #pragma unroll
-                for (int p = 0; p < S; ++p)                     // s_p 2^-8p, exact in bf16
-                    out[p][q] = __float2bfloat16_rn((float)dg[p] * (p == 0 ? 1.f : __int_as_float((127 - 8 * p) << 23)));
+                for (int o = 1; o < 8; o <<= 1) {
+                    const unsigned long long v = __shfl_xor_sync(0xffffffffu, mb, o);
+                    mb = v > mb ? v : mb;
+                }
+                if ((threadIdx.x & 7) == 0 && mb != 0 && r0 + rr < d.R)
+                    d.rexp[(long long)b * d.Rp + r0 + rr] = exp_of_bits(mb);
+                e = mb != 0 ? exp_of_bits(mb) : 0;
+            } else {
+                e = in_rows ? d.rexp[(long long)b * d.Rp + r0 + rr] : 0;
+                if (e == INT_MIN) e = 0;
             }
-            const long long plane = (long long)d.batch * d.Rp * d.Kp;
-            const long long off = ((long long)b * d.Rp + r0 + rr) * d.Kp + k0 + c8;
+            if (in_rows) {
+                __align__(16) __nv_bfloat16 out[S][8];
 #pragma unroll
-            for (int p = 0; p < S; ++p)
-                *reinterpret_cast<uint4 *>(d.dst + p * plane + off) = *reinterpret_cast<const uint4 *>(out[p]);
+                for (int q = 0; q < 8; ++q) {
+                    int dg[S];
+                    slice_digits<S>(t.x[rr][c8 + q], e, dg);
+#pragma unroll
+                    for (int p = 0; p < S; ++p)                     // s_p 2^-8p, exact in bf16
+                        out[p][q] = __float2bfloat16_rn((float)dg[p] * (p == 0 ? 1.f : __int_as_float((127 - 8 * p) << 23)));
+                }
+                const long long plane = (long long)d.batch * d.Rp * d.Kp;
+                const long long off = ((long long)b * d.Rp + r0 + rr) * d.Kp + k0 + c8;
+#pragma unroll
+                for (int p = 0; p < S; ++p)
+                    *reinterpret_cast<uint4 *>(d.dst + p * plane + off) = *reinterpret_cast<const uint4 *>(out[p]);
+            }
         }
         __syncthreads();
     }
