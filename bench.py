@@ -218,7 +218,7 @@ def run_gb300(args):
     t_mixed = time_to_tolerance(tr, e_ref) if e_ref is not None else None
     mixed = {"status": int(last["status"]), "iterations": int(last["iterations"]),
              "iterations_3slice": int((tr[:, 4] == 4).sum()), "iterations_4slice": int((tr[:, 4] == 3).sum()),
-             "iterations_6slice": int((tr[:, 4] == 2).sum()),
+             "iterations_5slice": int((tr[:, 4] == 2).sum()),
              "iterations_7slice_fp64_emulated": int((tr[:, 4] == 1).sum()),
              "fp64_iterations": int((tr[:, 4] == 0).sum()),
              "E_total": e_final,

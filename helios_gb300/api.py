@@ -85,7 +85,7 @@ def library():
 
 def gemm(A, B, precision="fp64", reps=1):
     """C = A @ B.T on the engine's FP64 ("fp64") or tensor-core GEMM ("mixed": 3 slices,
-    "mid": 4 slices, "high": 6 slices, "exact": 7 slices, FP64 emulated); returns (C, ms per launch)."""
+    "mid": 4 slices, "high": 5 slices, "exact": 7 slices, FP64 emulated); returns (C, ms per launch)."""
     A = np.ascontiguousarray(A, dtype=np.float64)
     B = np.ascontiguousarray(B, dtype=np.float64)
     M, K = A.shape
@@ -321,7 +321,7 @@ class CoupledCluster:
 
     def trace(self, mol: int = 0) -> np.ndarray:
         """Per-iteration (max|d1|, max|d2|, E_total, seconds, phase) of the last solve;
-        phase 4, 3, 2 = 3-, 4-, 6-slice tensor cores, 1 = 7-slice (FP64 emulated), 0 = FP64."""
+        phase 4, 3, 2 = 3-, 4-, 5-slice tensor cores, 1 = 7-slice (FP64 emulated), 0 = FP64."""
         n = _check(library().hx_ccsd_trace(self._h, int(mol), None, 0))
         out = np.zeros((max(n, 1), 5))
         library().hx_ccsd_trace(self._h, int(mol), out.ctypes.data_as(_c_d), n)

@@ -211,7 +211,7 @@ struct hx_ccsd {
     std::vector<int> phase, stall;
     std::vector<double> best;
     std::vector<double> fin_scale;       // mixed: tightening of the hand-over target after a failed FP64 check
-    std::vector<int> fp_returns;          // mixed: FP64 checks that sent a molecule back to 6-slice iterations
+    std::vector<int> fp_returns;          // mixed: checks that sent a molecule back to 5-slice iterations
     // host mirror of each molecule's DIIS ring: pushes so far and the phase
     // that produced each slot (-1 empty or purged); residual at which each
     // phase ended (0 = not ended, -1 = its vectors purged)
@@ -823,18 +823,18 @@ static int diis_purge(hx_ccsd *h, int mi, double a)
 //   LOW   3-slice tensor-core contractions (about 2^-24 of the operands' row
 //         maxima) until the residual falls below mixed_switch;
 //   MID   4-slice (about 2^-32) until it falls below kMidSpan * mixed_switch;
-//   HIGH  6-slice (about 2^-46) until it falls below kHighMargin * eps;
+//   HIGH  5-slice (about 2^-35) until it falls below kHighMargin * eps;
 //   check the iteration that may declare convergence: EXACT, 7-slice
 //         contractions that emulate FP64 ones (mixed_check = 0), or plain
 //         CUDA-core FP64 (mixed_check = 1). Convergence is declared only
 //         here, so the final residual and energy carry FP64 accuracy (the
 //         defect correction). A check that does not confirm convergence
-//         sends the molecule back to 6-slice iterations with a 10x tighter
+//         sends the molecule back to 5-slice iterations with a 10x tighter
 //         hand-over target (at most kMaxFp64Returns times); after that the
 //         check phase iterates on, and EXACT iterations that stop improving
 //         for mixed_patience iterations hand over to CUDA-core FP64.
 // A tensor-core phase hands over to the check below kHighMargin * eps (the
-// iteration is not monotone, and one more 6-slice iteration costs less than
+// iteration is not monotone, and one more 5-slice iteration costs less than
 // a check whose residual lands just above eps). A phase switches while its
 // own error is still about 1 % of the residual, so the DIIS history is kept;
 // a phase that stops improving for mixed_patience iterations hands over early
@@ -904,6 +904,10 @@ static int solve_all(hx_ccsd *h, int maxiter, double eps)
                     h->best[mi] = 1e300;
                     changed = true;
                     h->ph_end[mi][ph] = a;
+                    // HIGH stalled above its hand-over target: its floor is above
+                    // it, so the check phase iterates on instead of sending the
+                    // molecule back
+                    if (ph == PH_HIGH && a >= fin) h->fp_returns[mi] = kMaxFp64Returns;
                     if (stalled && a >= fin && ph != PH_HIGH) {          // LOW or MID
                         HX_CU(cudaMemsetAsync(h->diis[mi].count, 0, sizeof(int), h->st));
                         diis_mirror_reset(h, mi);
@@ -918,7 +922,7 @@ static int solve_all(hx_ccsd *h, int maxiter, double eps)
                 --remaining;
                 changed = true;
             } else if (mixed && h->fp_returns[mi] < kMaxFp64Returns) {
-                // the check did not confirm convergence: more 6-slice
+                // the check did not confirm convergence: more 5-slice
                 // iterations to a 10x tighter target, then check again
                 h->phase[mi] = PH_HIGH;
                 h->fin_scale[mi] *= 0.1;

@@ -64,18 +64,19 @@ namespace tc {
 //   LOW:  3 slices, pairs i + j <= 3 (8 MMAs per k-step), NX = 1: about 2^-24
 //         of the row maxima; 128 x 96 tiles.
 //   MID:  4 slices, pairs i + j <= 3 (10 MMAs), NX = 2: about 2^-32; 128 x 80.
-//   HIGH: 6 slices, pairs i + j <= 5 (21 MMAs), NX = 4: about 2^-46 of the row
-//         maxima; 128 x 48 tiles fed by 32-deep k-blocks (64-byte swizzle) so
-//         that three stages of six slices fit.
+//   HIGH: 5 slices, pairs i + j <= 4 (15 MMAs), NX = 3: about 2^-35 of the row
+//         maxima (3.3e-11 measured at 6400^3); 128 x 64 tiles fed by 32-deep
+//         k-blocks (64-byte swizzle). Six slices with pairs i + j <= 5 and
+//         NX = 4 reached 1.5e-13 but took 1.7x longer (21 MMAs on 128 x 48
+//         tiles), far more accuracy than the phase needs: it hands over to
+//         the 7-slice check at 0.1 eps, and the ladder sends any molecule
+//         whose residual stalls above that to 7-slice iterations.
 //   EXACT: 7 slices (48 fraction bits below the leading digit, past FP64's
 //         53-bit mantissa), pairs i + j <= 6 (28 MMAs), NX = 5: an emulation
 //         of an FP64 GEMM, its error that of the FP64 product itself; 128 x 32
 //         tiles, so that two buffers of six accumulators fit in TMEM.
-// The shared accumulator is what limits HIGH: measured at 6400^3, one exact
-// class more (NX 3 -> 4) took it from 5.6e-12 to 1.6e-13 relative error,
-// while a sixth slice alone changed nothing; LOW and MID are limited by their
-// slices. These errors set the residual level a phase can reach (the GEMM
-// outputs are ~1e3-1e4 times the residual they cancel down to).
+// These errors set the residual level a phase can reach (the GEMM outputs
+// are ~1e3-1e4 times the residual they cancel down to).
 template <int S_, int QMAX_, int NX_, int BN_, int STAGES_, int KC_, int EPIW_, int BK_, int STG_>
 struct Cfg {
     static constexpr int S = S_;                     // integer slices per FP64 operand
@@ -120,7 +121,7 @@ struct Cfg {
 // (the strip heights are what each ring leaves of the 227 KB per CTA)
 using Low = Cfg<3, 3, 1, 96, 2, 8, 12, 64, 64>;
 using Mid = Cfg<4, 3, 2, 80, 2, 6, 8, 64, 16>;
-using High = Cfg<6, 5, 4, 48, 3, 7, 8, 32, 64>;
+using High = Cfg<5, 4, 3, 64, 3, 8, 8, 32, 64>;
 using Exact = Cfg<7, 6, 5, 32, 3, 6, 8, 32, 32>;
 constexpr int TMEM_COLS = 512;
 constexpr int BM = 128, KPAD = 64;   // K is padded to KPAD (the slicing tile depth)
@@ -1192,7 +1193,7 @@ extern "C" int hx_gemm_noalloc(const double *dA, const double *dB, double *dC, i
         return HX_ERR_ARG;
     }
     if (precision != HX_PRECISION_MIXED && precision != 2) {
-        hx_set_error("hx_gemm_noalloc: precision must be 1 (3 slices) or 2 (6 slices)");
+        hx_set_error("hx_gemm_noalloc: precision must be 1 (3 slices) or 2 (5 slices)");
         return HX_ERR_ARG;
     }
     unsigned char *base = nullptr;

@@ -9,7 +9,7 @@ struct Engine;
 int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s);
 // Run one plan group on the tensor cores: slice the operands, tcgen05 GEMM,
 // FP64 epilogue. mode 0 = LOW (3 slices, about 2^-24 of the row maxima),
-// 1 = MID (4 slices, about 2^-32), 2 = HIGH (6 slices, about 2^-46), 3 =
+// 1 = MID (4 slices, about 2^-32), 2 = HIGH (5 slices, about 2^-35), 3 =
 // EXACT (7 slices: an FP64 GEMM emulated, as accurate as the FP64 product).
 cudaError_t run_group(Engine *e, const TgemmDesc *descs, int n, const int *d_active, cudaStream_t s, int mode);
 void destroy(Engine *e);

@@ -99,7 +99,7 @@ typedef struct hx_cc_params {
     int32_t guess;                /* 0 reference guess (guessCC), 1 learned guess */
     double mixed_switch;          /* mixed precision: residual at which a molecule moves from
                                      3-slice to 4-slice tensor-core iterations (1e-3); 4-slice
-                                     run to 1e-3 mixed_switch, then 6-slice; any of them hands
+                                     run to 1e-3 mixed_switch, then 5-slice; any of them hands
                                      over to the check iterations below 0.1 eps */
     int32_t mixed_patience;       /* mixed precision: iterations without a new lowest residual
                                      after which a molecule moves on to the next phase (3) */
@@ -195,7 +195,7 @@ int hx_ccsd_get_scf(hx_ccsd *h, int32_t mol, double *C, double *eps, double *fmo
 /* Per-iteration record of molecule mol's last solve: for each iteration
  * k < cap, out[5k..5k+4] = max|d1|, max|d2|, E_total, seconds since the start
  * of the solve, phase of the iteration (0 FP64 CUDA cores; 1, 2, 3, 4: seven-
- * (FP64 emulated), six-, four- and three-slice tensor-core contractions).
+ * (FP64 emulated), five-, four- and three-slice tensor-core contractions).
  * Returns the number of iterations recorded. */
 int hx_ccsd_trace(hx_ccsd *h, int32_t mol, double *out, int32_t cap);
 
@@ -223,8 +223,8 @@ void hx_ccsd_destroy(hx_ccsd *h);
 /* Engine utility with no counterpart in the reference: C = A B^T for
  * row-major FP64 host matrices (A: M x K, B: N x K, C: M x N) on the engine's
  * FP64 CUDA-core GEMM (precision 0) or its exact-slice tcgen05 GEMM with
- * 3 slices (precision 1, about 2^-24 of the row maxima), 6 slices (precision
- * 2, about 2^-46), 4 slices (precision 3, about 2^-32) or 7 slices
+ * 3 slices (precision 1, about 2^-24 of the row maxima), 5 slices (precision
+ * 2, about 2^-35), 4 slices (precision 3, about 2^-32) or 7 slices
  * (precision 4: FP64 emulated, as accurate as the FP64 product); the launch
  * is repeated reps times after one warm-up and
  * *ms (if not NULL) receives the mean device time per launch. */
@@ -238,7 +238,7 @@ int hx_gemm(const double *A, const double *B, double *C, int32_t M, int32_t N, i
  * (cudaFree synchronises the whole device). C = A B^T for row-major FP64
  * matrices already in DEVICE memory
  * (A: M x K, B: N x K, C: M x N), always on the tcgen05 exact-slice GEMM
- * (precision 1: 3 slices, 2: 6 slices; FP64 is rejected). It calls no
+ * (precision 1: 3 slices, 2: 5 slices; FP64 is rejected). It calls no
  * allocator: the operand slices, row exponents, error word and descriptors
  * live in one static device array of about 6.4 MB, whose address is looked
  * up once per device (cudaGetSymbolAddress) on the first call; make that

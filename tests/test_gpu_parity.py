@@ -117,10 +117,13 @@ def test_larger_molecule_against_factorised_oracle(api):
     assert abs(out["ecorr"] - f["ecorr"]) < 1e-8
 
 
-def test_mixed_precision_reaches_fp64_energy(api):
+@pytest.mark.parametrize("accuracy", [10, 12])
+def test_mixed_precision_reaches_fp64_energy(api, accuracy):
+    # 12 is the reference's default threshold: below the 5-slice floor, so the
+    # molecule finishes with 7-slice (emulated FP64) iterations
     for mol in (molecules.polyene(20), molecules.ladder(24)):
-        e64 = api.get_energy(mol, _kw(api))
-        mx = api.get_energy(mol, _kw(api, precision="mixed"))
+        e64 = api.get_energy(mol, _kw(api, accuracy=accuracy))
+        mx = api.get_energy(mol, _kw(api, precision="mixed", accuracy=accuracy))
         assert mx["status"] == 1
         assert abs(mx["energy"][0] - e64["energy"][0]) < 1e-6
 
@@ -137,7 +140,7 @@ def test_mixed_trace_starts_on_tensor_cores(api):
     assert tr[0, 4] == 4.0 and tr[-1, 4] == 1.0
     d = np.diff(tr[:, 4])
     # phases only move down the ladder, except that a check which does not
-    # confirm convergence sends the molecule back to 6-slice iterations
+    # confirm convergence sends the molecule back to 5-slice iterations
     assert np.all((d <= 0) | ((tr[1:, 4] == 2) & (tr[:-1, 4] <= 1)))
     assert np.all(np.diff(tr[:, 3]) >= 0)
 
@@ -154,7 +157,7 @@ def test_tensor_core_gemm_accuracy(api):
         C, _ = api.gemm(A, B, "mid")
         assert np.abs(C - ref).max() / np.abs(ref).max() < 1e-8
         C, _ = api.gemm(A, B, "high")
-        assert np.abs(C - ref).max() / np.abs(ref).max() < 1e-12
+        assert np.abs(C - ref).max() / np.abs(ref).max() < 1e-10
         C64, _ = api.gemm(A, B, "fp64")
         assert np.abs(C64 - ref).max() / np.abs(ref).max() < 1e-13
         CX, _ = api.gemm(A, B, "exact")
