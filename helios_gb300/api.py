@@ -77,7 +77,7 @@ def library():
                      "hx_ccsd_iterate", "hx_ccsd_energy", "hx_ccsd_solve", "hx_ccsd_solve_batch",
                      "hx_ccsd_get_amplitudes", "hx_ccsd_get_scf", "hx_ccsd_dims", "hx_ccsd_trace",
                      "hx_gemm", "hx_ccsd_timing", "hx_last_error", "hx_ccsd_set_model", "hx_ccsd_training_rows",
-                     "hx_mlp_nparam", "hx_mlp_predict", "hx_mlp_grad", "hx_mlp_train"):
+                     "hx_mlp_nparam", "hx_mlp_predict", "hx_mlp_grad", "hx_mlp_train", "hx_ccsd_triples"):
             getattr(lib, name).restype = ctypes.c_int
         _lib = lib
     return _lib
@@ -318,6 +318,13 @@ class CoupledCluster:
                                          fmo.ctypes.data_as(_c_d), out.ctypes.data_as(_c_d), st.ctypes.data_as(_c_i)))
         return {"C": C, "eps": eps, "F": fmo, "energy": out[0], "eel": out[1], "enuc": out[2],
                 "accuracy": out[3], "status": int(st[0]), "iterations": int(st[1])}
+
+    def triples(self, mol: int = 0) -> dict:
+        """(T) of molecule mol after a solve: textbook (T) = E[4] + E[5], its parts, and the
+        reference's r-ccsd(t) triples term (= -(T), see hx_ccsd_triples)."""
+        e = np.zeros(4)
+        _check(library().hx_ccsd_triples(self._h, int(mol), e.ctypes.data_as(_c_d)))
+        return {"T": e[0], "E4": e[1], "E5": e[2], "reference_term": e[3]}
 
     def trace(self, mol: int = 0) -> np.ndarray:
         """Per-iteration (max|d1|, max|d2|, E_total, seconds, phase) of the last solve;

@@ -1131,6 +1131,65 @@ void hx_ccsd_destroy(hx_ccsd *h)
     delete h;
 }
 
+// (T) of molecule mol from its current amplitudes (hx_triples.cu has the
+// formulas). The integrals come from the site basis: (ck|jl) = C_ck^T G C_jl
+// and (bd|ai) = (G C_ai)^T C_bd as GEMMs; X = (bd|ai) t_kj^cd - (ck|jl) t_il^ab
+// as two GEMMs over [(i a b)][(k c j)] on the FP64 CUDA-core kernel; X and
+// W take o^3 v^3 doubles each, allocated for the call.
+int hx_ccsd_triples(hx_ccsd *h, int32_t mol, double e[4])
+{
+    if (!h || !h->initialized) { hx_set_error("hx_ccsd_triples before hx_ccsd_init"); return HX_ERR_STATE; }
+    if (mol < 0 || mol >= h->nmol) { hx_set_error("hx_ccsd_triples: molecule %d of %d", mol, h->nmol); return HX_ERR_ARG; }
+    if (h->scf_failed[mol]) { hx_set_error("hx_ccsd_triples: the SCF of molecule %d did not converge", mol); return HX_ERR_SCF; }
+    const CCMol &m = h->cc[mol];
+    const int N = m.N, o = m.o, v = m.v;
+    const long long ov = (long long)o * v, o3 = (long long)o * o * o, n3 = o3 * v * v * v;
+    const size_t nX = (size_t)n3, nI1 = (size_t)ov * v * v, nJ = (size_t)ov * o * o;
+    const size_t nBvv = (size_t)N * v * v, nBoo = (size_t)N * o * o, npart = 2 * (size_t)o3;
+    const size_t elems = 2 * nX + nI1 + nJ + nBvv + 2 * nBoo + npart + 2;
+    size_t fre = 0, tot = 0;
+    HX_CU(cudaMemGetInfo(&fre, &tot));
+    if ((double)elems * sizeof(double) > 0.9 * (double)fre) {
+        hx_set_error("hx_ccsd_triples: N = %d needs %.1f GB of device memory for X and W (o^3 v^3 doubles each), "
+                     "%.1f GB are free", N, elems * 8.0 / 1e9, fre / 1e9);
+        return HX_ERR_NOMEM;
+    }
+    double *buf = nullptr;
+    HX_CU(cudaMalloc(&buf, elems * sizeof(double)));
+    double *X = buf, *W = X + nX, *I1 = W + nX, *J = I1 + nI1, *Bvv0 = J + nJ, *Boo0 = Bvv0 + nBvv,
+           *GBoo0 = Boo0 + nBoo, *part = GBoo0 + nBoo, *out = part + npart;
+    std::vector<Group> gs(5);
+    const long long oo = (long long)o * o, vv = (long long)v * v;
+    gs[0].h.push_back(tg(m.G, Boo0, GBoo0, 1, N, (int)oo, N, N, (int)oo, N, {0, N, 0, 1, 0}, {0, 1, 0, oo, 0}, {0, oo, 0, 1, 0}, 1.0, 0.0, mol));
+    gs[1].h.push_back(tg(m.Bov0, GBoo0, J, 1, (int)ov, (int)oo, N, (int)ov, (int)oo, N, {0, 1, 0, ov, 0}, {0, 1, 0, oo, 0}, {0, oo, 0, 1, 0}, 1.0, 0.0, mol));
+    gs[2].h.push_back(tg(m.GBov0, Bvv0, I1, 1, (int)ov, (int)vv, N, (int)ov, (int)vv, N, {0, 1, 0, ov, 0}, {0, 1, 0, vv, 0}, {0, vv, 0, 1, 0}, 1.0, 0.0, mol));
+    const long long ncol = (long long)o * v * o;
+    gs[3].h.push_back(tg(I1, m.t2, X, 1, (int)(ov * v), (int)ncol, v, v, o, v, {vv, v, 0, 1, 0}, {ov, v, 0, 1, 0}, {v * ncol, ncol, o, 1, 0}, 1.0, 0.0, mol));
+    gs[4].h.push_back(tg(m.t2, J, X, 1, (int)(ov * v), (int)ncol, o, v, o, o, {ov, 1, 0, v, 0}, {oo, o, 0, 1, 0}, {v * ncol, ncol, o, 1, 0}, -1.0, 1.0, mol));
+    int rc = HX_OK;
+    cudaError_t ce = hx_triples_pairs(m.Cmo, N, o, Bvv0, Boo0, h->st);
+    for (auto &g : gs) {
+        if (ce != cudaSuccess || rc != HX_OK) break;
+        rc = upload_group(g);
+        if (rc == HX_OK) ce = hx_tgemm_f64_launch(g.d, (int)g.h.size(), g.tiles, nullptr, h->st);
+    }
+    if (ce == cudaSuccess && rc == HX_OK) ce = hx_triples_energy(X, W, m.t1, m.gov, m.Fmo, N, o, part, out, h->st);
+    double r[2] = {0.0, 0.0};
+    if (ce == cudaSuccess && rc == HX_OK) ce = cudaMemcpyAsync(r, out, sizeof(r), cudaMemcpyDeviceToHost, h->st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(h->st);
+    for (auto &g : gs) if (g.d) cudaFree(g.d);
+    cudaFree(buf);
+    if (rc != HX_OK) return rc;
+    if (ce != cudaSuccess) { hx_set_error("hx_ccsd_triples: %s", cudaGetErrorString(ce)); return HX_ERR_CUDA; }
+    if (e) {
+        e[0] = r[0] + r[1];      // (T) = E[4] + E[5] (spin-orbital textbook sign)
+        e[1] = r[0];
+        e[2] = r[1];
+        e[3] = -(r[0] + r[1]);   // the reference's triples term c1 + c2 (+ c3 = 0 for canonical RHF)
+    }
+    return HX_OK;
+}
+
 // C = A B^T for row-major FP64 host matrices, on the engine's FP64 or
 // tensor-core GEMM; reps > 1 repeats the launch and reports the mean time.
 int hx_gemm(const double *A, const double *B, double *C, int32_t M, int32_t N, int32_t K, int32_t precision,

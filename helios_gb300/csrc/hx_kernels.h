@@ -24,3 +24,10 @@ cudaError_t hx_step(const CCMol *m, const DiisMol *h, const int *act, int nmol, 
 cudaError_t hx_diis(const CCMol *m, const DiisMol *h, const int *act, int nmol, const double *gate, double *part,
                     int nblk, int nd_max, cudaStream_t s);
 cudaError_t hx_energy(const CCMol *m, const int *act, int nmol, double *part, int nblk, cudaStream_t s);
+
+// (T) triples (hx_triples.cu): ZDO pair products of the occupied and virtual
+// orbitals, then W, the energy partials and their ordered sum (out[0] = E[4],
+// out[1] = E[5]) from X = [(i a b)][(k c j)].
+cudaError_t hx_triples_pairs(const double *C, int N, int o, double *Bvv0, double *Boo0, cudaStream_t s);
+cudaError_t hx_triples_energy(const double *X, double *W, const double *t1, const double *gov, const double *Fmo,
+                              int N, int o, double *part, double *out, cudaStream_t s);

@@ -199,6 +199,17 @@ int hx_ccsd_get_scf(hx_ccsd *h, int32_t mol, double *C, double *eps, double *fmo
  * Returns the number of iterations recorded. */
 int hx_ccsd_trace(hx_ccsd *h, int32_t mol, double *out, int32_t cap);
 
+/* r-ccsd(t): the (T) triples correction of molecule mol from its amplitudes
+ * after a solve (the reference computes it in the spin-orbital basis,
+ * mod_cc.f90:2028-2111; this is the same quantity in spatial orbitals).
+ * e[0] = (T) = E[4] + E[5] in the textbook sign convention, e[1] = E[4]
+ * (connected triples), e[2] = E[5] (disconnected), e[3] = the reference's
+ * triples term c1 + c2 + c3, which is -(T): its c1 multiplies amp^2 by
+ * D = F_aa + F_bb + F_cc - F_ii - F_jj - F_kk > 0, and c3 (a term in F_kc)
+ * vanishes for canonical RHF orbitals. Needs 2 o^3 v^3 doubles of device
+ * memory for the call (HX_ERR_NOMEM when they are not free). */
+int hx_ccsd_triples(hx_ccsd *h, int32_t mol, double e[4]);
+
 /* Engine utility with no counterpart in the reference: device timing.
  * out[0] = ms of the last hx_ccsd_init (SCF, integrals, guess), out[1] = ms
  * of the last solve, both from CUDA events on the handle's stream;
