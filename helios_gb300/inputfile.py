@@ -12,7 +12,8 @@ per bond ``i j beta kind`` (1-based sites, kind single / double / nonset).
 definebd.f90 that the r-ccsd path reads, with their defaults and their
 power-of-ten ("potentiate") conventions) and the job (method, jobtype,
 polarizability grid, harvest); ``write_input`` writes the same format;
-``run_input`` runs an energy or polarizability job of method r-ccsd. Engine
+``run_input`` runs an energy job of method r-ccsd or r-ccsd(t), or a
+polarizability job of r-ccsd. Engine
 options the reference has no key for (precision, guess, mixed_check) go in a
 ``%engine{ }`` block, which the reference's reader never looks for.
 """
@@ -189,13 +190,25 @@ def write_input(mol: Molecule, kw: api.Keywords | None = None, job: Job | None =
 
 
 def run_input(source: str, harvest_file: str | None = None) -> dict:
-    """Run the job of an input file on the engine (method r-ccsd)."""
+    """Run the job of an input file on the engine (methods r-ccsd and r-ccsd(t))."""
     mol, kw, job = read_input(source)
-    if job.methods != ["r-ccsd"]:
-        raise ValueError(f"methods {job.methods}: the engine runs r-ccsd")
+    if job.methods not in (["r-ccsd"], ["r-ccsd(t)"]):
+        raise ValueError(f"methods {job.methods}: the engine runs r-ccsd and r-ccsd(t)")
     if job.jobtype == "energy":
-        out = api.get_energy(mol, kw)
-        return {"job": job, "energy": out["energy"], "status": out["status"], "iterations": out["iterations"]}
+        cc = api.CoupledCluster(mol, kw)
+        cc.initCC()
+        out = cc.iterate()
+        res = {"job": job, "energy": out["energy"], "status": out["status"], "iterations": out["iterations"]}
+        if job.methods == ["r-ccsd(t)"] and out["status"] == 1:
+            t = cc.triples(0)
+            # the reference adds its triples term to the CCSD energy (energy(1), mod_cc.f90:2104)
+            res["triples"] = t
+            res["energy_ccsd_t"] = float(out["energy"][0] + t["reference_term"])
+            res["energy_ccsd_t_textbook"] = float(out["energy"][0] + t["T"])
+        cc.finalizeCC()
+        return res
+    if job.methods != ["r-ccsd"]:
+        raise ValueError("polarizability jobs run r-ccsd")
     if job.jobtype == "polarizability":
         from . import properties
         res, report = properties.polarizability_job(mol, kw, scales=job.components, npoints=job.points,
@@ -217,3 +230,6 @@ if __name__ == "__main__":
         e = r["energy"]
         print(f"status {r['status']} iterations {r['iterations']}")
         print(f"E_total {e[0]:.12f} eV  E_ref {e[1]:.12f} eV  E_corr {e[0] - e[1]:.12f} eV")
+        if "triples" in r:
+            print(f"(T) {r['triples']['T']:.12f} eV  E_CCSD(T) {r['energy_ccsd_t_textbook']:.12f} eV  "
+                  f"(reference convention: {r['energy_ccsd_t']:.12f} eV)")

@@ -42,3 +42,11 @@ def test_polarizability_job_with_harvest(api, tmp_path):
     assert rec["scales"] == "x" and rec["points"] == 5
     assert rec["a"][0] == pytest.approx(want["stencils"][5]["alpha"]["xx"], rel=1e-9)
     assert "Polarizability results for r-ccsd" in r["report"]
+
+
+def test_ccsd_t_energy_job(api):
+    text = _dodecahexaene_text().replace("precision = mixed", "precision = fp64").replace("method = r-ccsd", "method = r-ccsd(t)")
+    r = inputfile.run_input(text)
+    t = r["triples"]
+    assert t["T"] < 0 and r["energy_ccsd_t_textbook"] == pytest.approx(r["energy"][0] + t["T"])
+    assert r["energy_ccsd_t"] == pytest.approx(r["energy"][0] - t["T"])
