@@ -305,6 +305,21 @@ def run_gb300(args):
                                    / abs(res["fp64"]["alpha_xx"]),
                                    "rel_diff_mixed_vs_oracle": None if a_or is None
                                    else abs(res["mixed"]["alpha_xx"] - a_or) / abs(a_or)}
+    # --- the (T) correction of the ensemble's largest molecule size (ladder, 64 sites)
+    if args.triples:
+        ct = api.CoupledCluster(molecules.ladder(64), api.Keywords(bond_alternation=0.1, accuracy=8,
+                                                                   precision="mixed", guess=guess))
+        ct.initCC()
+        rt = ct.iterate()
+        torch.cuda.synchronize()
+        t0t = time.perf_counter()
+        tt = ct.triples(0)
+        secs_t = time.perf_counter() - t0t
+        tmt = ct.timing()
+        ct.finalizeCC()
+        extra["triples"] = {"molecule": "ladder-64 (o = v = 32)", "ccsd_status": int(rt["status"]),
+                            "ccsd_solve_s": tmt["solve_ms"] / 1e3, "T_eV": tt["T"], "E4_eV": tt["E4"],
+                            "E5_eV": tt["E5"], "reference_term_eV": tt["reference_term"], "triples_s": secs_t}
     # --- end to end through the C ABI with host buffers
     e2e = run_e2e(api, mol, kw, max(1, min(args.steps, 3)))
     # --- roofline of the tcgen05 GEMM, live over the timed steps
@@ -482,6 +497,7 @@ def main():
     ap.add_argument("--no-fp64-compare", dest="fp64_compare", action="store_false")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-polariz", dest="polariz", action="store_false", help="skip the polarizability leg")
+    ap.add_argument("--no-triples", dest="triples", action="store_false", help="skip the (T) leg")
     ap.add_argument("--ref-pairs", type=int, default=48, help="doubles pairs per reference-arm step")
     args = ap.parse_args()
     if args.warmup < 3:
