@@ -323,6 +323,20 @@ static int upload_masks(hx_ccsd *h)
     return HX_OK;
 }
 
+// The particle-particle ladder and the t2 part of the hole-hole intermediate
+// go through the site basis (four and two GEMMs of K = v or N: o^2 (v^2 N +
+// v N^2) flops instead of o^2 v^4). For small molecules on the tensor cores
+// those GEMMs are single k-block tiles that the MMAs barely use, so up to
+// kMoLadderMaxV virtual orbitals the mixed path builds (ac|bd)~ (v^2 x v^2 x
+// N) and does both terms as two deep GEMMs in the MO basis (o^2 x v^2 x v^2
+// and o^2 x o^2 x v^2): more flops, far fewer and fuller tiles. FP64
+// iterations keep the site basis, which has the fewest flops.
+static const int kMoLadderMaxV = 32;
+static bool mo_ladder(const hx_ccsd *h, int mi)
+{
+    return h->p.precision == HX_PRECISION_MIXED && h->v[mi] <= kMoLadderMaxV;
+}
+
 // Descriptors of every contraction of one iteration, for every molecule.
 // Index conventions are spelled out in hx_plan.h; each block cites the term
 // of the T1-dressed closed-shell CCSD equations it evaluates.
@@ -353,16 +367,25 @@ static void build_plan(hx_ccsd *h)
         P[G_LEAD].h.push_back(tg(m.Bia, m.GBia, m.r2, 1, ov, ov, N, ov, ov, N, {0, 1, 0, ov, 0}, {0, 1, 0, ov, 0}, {0, ov, 0, 1, 0}, 1.0, 0.0, mi));
         // particle-particle ladder through the site basis:
         //   sum_cd (ac|bd)~ t_ij^cd = sum_mu,nu X_mu,a X_nu,b G_mu,nu [sum_cd C_mu,c C_nu,d t_ij^cd]
-        P[G_LAD_A].h.push_back(tg(m.t2, Cmo + o, m.T1s, 1, o * v * o, N, v, o * v * o, N, v, {0, v, 0, 1, 0}, {0, N, 0, 1, 0}, {0, N, 0, 1, 0}, 1.0, 0.0, mi));
-        P[G_LAD_B].h.push_back(tg(Cmo + o, m.T1s, m.Ts, o, N, o * N, v, N, o * N, v, {0, N, 0, 1, 0}, {0, 1, 0, (long long)o * N, (long long)v * o * N}, {0, (long long)o * N, 0, 1, (long long)N * o * N}, 1.0, 0.0, mi));
-        //   Z = Ts X: its virtual columns (X_v = Cv - Co t1) close the ladder, its
-        //   occupied ones (X_o = Co exactly: the dressing leaves them) feed the
-        //   hole-hole intermediate below -- one product, one slicing of Ts
-        P[G_LAD_D].h.push_back(tg(m.Ts, m.X, m.Z, 1, o * N * o, N, N, o * N * o, N, N, {0, N, 0, 1, 0}, {0, 1, 0, N, 0}, {0, N, 0, 1, 0}, 1.0, 0.0, mi));
-        P[G_LAD_E].h.push_back(tg(m.X + o, m.Z + o, m.r2, o, v, ov, N, v, v, N, {0, 1, 0, N, 0}, {N, 1, 0, (long long)o * N, (long long)N * o * N}, {0, ov, v, 1, (long long)v * ov}, 1.0, 1.0, mi));
-        // hole-hole ladder: W_klij = (ki|lj)~ + sum_cd t_ij^cd (kc|ld), the latter through the site basis
-        //   (G_W_D stays empty: Z's occupied columns are the former Zo = Ts Co)
-        P[G_W_E].h.push_back(tg(Cmo, m.Z, m.Woo, o, o, o * o, N, o, o, N, {0, 1, 0, N, 0}, {N, 1, 0, (long long)o * N, (long long)N * o * N}, {0, o * o, o, 1, (long long)o * o * o}, 1.0, 0.0, mi));
+        const long long vv = (long long)v * v, vov = (long long)v * ov;
+        if (mo_ladder(h, mi)) {
+            // (ac|bd)~ = sum_mu Bvv[mu][ac] GBvv[mu][bd]; r2_ij^ab += sum_cd (ac|bd)~ t_ij^cd
+            P[G_LAD_A].h.push_back(tg(m.Bvv, m.GBvv, m.Vvv, 1, (int)vv, (int)vv, N, (int)vv, (int)vv, N, {0, 1, 0, vv, 0}, {0, 1, 0, vv, 0}, {0, vv, 0, 1, 0}, 1.0, 0.0, mi));
+            P[G_LAD_E].h.push_back(tg(m.t2, m.Vvv, m.r2, 1, o * o, (int)vv, (int)vv, o, v, v, {vov, v, ov, 1, 0}, {vv * v, v, vv, 1, 0}, {vov, v, ov, 1, 0}, 1.0, 1.0, mi));
+            // W_klij = sum_cd (kc|ld) t_ij^cd into Woo[i][k][j][l] ((ki|lj)~ is added below)
+            P[G_W_E].h.push_back(tg(m.gov, m.t2, m.Woo, 1, o * o, o * o, (int)vv, o, o, v, {(long long)v * ov, v, ov, 1, 0}, {vov, v, ov, 1, 0}, {(long long)o * o, 1, (long long)o * o * o, o, 0}, 1.0, 0.0, mi));
+        } else {
+            P[G_LAD_A].h.push_back(tg(m.t2, Cmo + o, m.T1s, 1, o * v * o, N, v, o * v * o, N, v, {0, v, 0, 1, 0}, {0, N, 0, 1, 0}, {0, N, 0, 1, 0}, 1.0, 0.0, mi));
+            P[G_LAD_B].h.push_back(tg(Cmo + o, m.T1s, m.Ts, o, N, o * N, v, N, o * N, v, {0, N, 0, 1, 0}, {0, 1, 0, (long long)o * N, (long long)v * o * N}, {0, (long long)o * N, 0, 1, (long long)N * o * N}, 1.0, 0.0, mi));
+            //   Z = Ts X: its virtual columns (X_v = Cv - Co t1) close the ladder, its
+            //   occupied ones (X_o = Co exactly: the dressing leaves them) feed the
+            //   hole-hole intermediate below -- one product, one slicing of Ts
+            P[G_LAD_D].h.push_back(tg(m.Ts, m.X, m.Z, 1, o * N * o, N, N, o * N * o, N, N, {0, N, 0, 1, 0}, {0, 1, 0, N, 0}, {0, N, 0, 1, 0}, 1.0, 0.0, mi));
+            P[G_LAD_E].h.push_back(tg(m.X + o, m.Z + o, m.r2, o, v, ov, N, v, v, N, {0, 1, 0, N, 0}, {N, 1, 0, (long long)o * N, (long long)N * o * N}, {0, ov, v, 1, (long long)v * ov}, 1.0, 1.0, mi));
+            // hole-hole ladder: W_klij = (ki|lj)~ + sum_cd t_ij^cd (kc|ld), the latter through the site basis
+            //   (G_W_D stays empty: Z's occupied columns are the former Zo = Ts Co)
+            P[G_W_E].h.push_back(tg(Cmo, m.Z, m.Woo, o, o, o * o, N, o, o, N, {0, 1, 0, N, 0}, {N, 1, 0, (long long)o * N, (long long)N * o * N}, {0, o * o, o, 1, (long long)o * o * o}, 1.0, 0.0, mi));
+        }
         P[G_W_INT].h.push_back(tg(m.Boo, m.GBoo, m.Woo, 1, o * o, o * o, N, o, o, N, {o, 1, 0, o * o, 0}, {o, 1, 0, o * o, 0}, {(long long)o * o, (long long)o * o * o, 1, o, 0}, 1.0, 1.0, mi));
         P[G_HH].h.push_back(tg(m.Woo, m.t2, m.r2, 1, o * o, v * v, o * o, o, v, o, {(long long)o * o * o, o, (long long)o * o, 1, 0}, {ov, 1, (long long)v * ov, v, 0}, {(long long)v * ov, v, ov, 1, 0}, 1.0, 1.0, mi));
         // C: Cint_kiac = (ki|ac)~ - 1/2 sum_ld t_li^ad (kd|lc);  C_ij^ab = -sum_kc t_kj^bc Cint_kiac
@@ -436,6 +459,7 @@ static int allocate(hx_ccsd *h)
             m.T1s = A.take<double>((size_t)o * v * o * N); m.Ts = A.take<double>((size_t)o * N * o * N);
             m.Z = A.take<double>((size_t)o * N * o * N);
             m.Woo = A.take<double>((size_t)o * o * o * o);
+            m.Vvv = mo_ladder(h, mi) ? A.take<double>((size_t)v * v * v * v) : nullptr;
             m.Cint = A.take<double>(pr); m.Cp = A.take<double>(pr); m.Dint = A.take<double>(pr); m.X2 = A.take<double>(pr);
             m.Fvv2 = A.take<double>((size_t)v * v); m.Foo2 = A.take<double>((size_t)o * o);
             m.U = A.take<double>(ov * N); m.UG = A.take<double>(ov * N); m.Vs = A.take<double>((size_t)o * N);

@@ -42,6 +42,8 @@ struct CCMol {
     double *Bvv, *GBvv;                   // [N][v*v]  X_mu,a Y_mu,c (index a*v+c)
     // contraction scratch
     double *T1s, *Ts, *Z, *Woo;           // ladder: o*v*o*N, o*N*o*N, Ts X: o*N*o*N, o^4
+    double *Vvv;                          // MO-basis ladder integrals (ac|bd)~ [(a c)][(b d)], v^4
+                                          // (small molecules in mixed precision; else null)
     double *Cint, *Cp, *Dint, *X2;        // o^2 v^2 each
     double *Fvv2, *Foo2;                  // v*v, o*o
     double *U, *UG, *Vs;                  // [o*v][N], [o*v][N], [o][N]
