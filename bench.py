@@ -6,11 +6,13 @@ Workload (N = 1 per GPU): the 160-site polyene (o = v = 80), the single-GPU
 configuration the headline metric is quoted on. One step = one full solve
 through the engine: RHF SCF, integrals, guess and the CCSD iteration to
 |dE_corr| <= 1e-6 eV, in mixed precision (exact-slice BF16 tcgen05
-contractions, FP64 finishing iterations; stop rule: FP64 residual < 1e-7).
+contractions of 3, 4 and 5 slices, then a 7-slice check that emulates FP64;
+stop rule: that residual < 1e-7).
 value = polyene solves per second over all ranks (replicas: every rank solves
 its own polyene, no device collective). The same line carries the plain FP64
 GPU path's time to 1e-6 eV on the same molecule, the 512-molecule ensemble
-throughput, the roofline of the dominant kernel (the tcgen05 GEMM, timed live
+throughput (mixed and plain FP64), the 64-site ladder's polarizability and
+(T) correction, the roofline of the dominant kernel (the tcgen05 GEMM, timed live
 with CUDA events during the timed steps), the end-to-end number through the
 C ABI with host buffers, the SM clocks seen during the timed region and a CPU
 baseline (the factorised FP64 oracle, one sampled residual on the host cores).
