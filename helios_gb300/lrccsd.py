@@ -1,0 +1,538 @@
+"""LR-CCSD excited states (lr-r-ccsd) on the GB300 CCSD engine.
+
+helios runs linear-response CCSD after a converged r-ccsd when
+``states:excited-states-number`` > 0 (getEnergy, src/modules/mod_property.f90:
+159-175; src/methods/coupledCluster/lrccsd/mod_lrccsd.f90). It solves the
+right eigenproblem (H-bar - E_cc) r = omega r over singles and doubles, one
+state at a time, with its own iteration, and reports E_CCSD + omega.
+
+The sigma vector (H-bar - E_cc) r needs no equations of its own here. The
+r-ccsd residual Omega(t) that the engine evaluates is a polynomial of degree
+four in the amplitudes, and its Jacobian at the converged amplitudes is
+H-bar - E_cc on singlet excitations, written in the spin-adapted coordinates
+t1[i, a], t2[i, j, a, b]. The odd part of Omega(t + h r) in h is
+h J r + h^3 K(r), so
+
+    J r = [8 (Omega(t + h r) - Omega(t - h r)) - (Omega(t + 2h r) - Omega(t - 2h r))] / (12 h)
+
+holds exactly. The four residuals are four copies of the molecule in ONE
+engine batch, and every state being solved adds four copies, so all states
+advance in the same launches. The engine hands a residual back through one
+stepCC: after ``set_guess(x)`` (which also clears the DIIS history, so the
+iteration mixes nothing) and one ``iterationCC`` with unit steps,
+t1' = x1 + d1 / (F_ii - F_aa) and t2' = x2 + 3 Omega2 / (F_ii + F_jj - F_aa - F_bb)
+(mod_cc.f90:987-1017).
+
+The host part restates the reference's iteration on those coordinates:
+
+* stepLR (mod_lrccsd.f90:216-326), normalize (:393-453), orthogonalization
+  (:457-527), pushLRVectors / newLRVectors / diisDotProduct (:1081-1225) and
+  energyLR (:330-389). The reference works on spin orbitals and sums over its
+  unique amplitudes (i<j, a<b). A singlet vector's spin-orbital form follows
+  from the spatial one by the amplitude rules of convertSpatialToSpinCC
+  (mod_cc.f90:2601-2678), which turns those sums into
+      <x, y> = 2 sum x1 y1 + sum x2 y2 + 1/2 sum (x2 - x2^ab)(y2 - y2^ab)
+  (x2^ab: a and b swapped). The largest spin-orbital doubles element is
+  max(|x2|, |x2 - x2^ab|). With these, every iterate equals the reference's.
+* prepareGuess / guessState (:1229-1419): the lowest CIS (or 'rpa') roots
+  of A(ia, jb) = 2(ai|jb) - (ab|ji) + delta (e_a - e_i), keeping the singles
+  whose coefficient reaches linear-response:guess-threshold.
+* initLR (:125-172): state k converges to accuracy * 2^(k-1); the states are
+  sorted by omega at the end (resortStates, :531-574). Without
+  orthogonalization the states do not depend on each other and iterate
+  together; with it they run one after another as in the reference.
+* energyLR's reference weight r0 = (2 sum Ft_ia r1 + sum L_iajb r2) / omega,
+  Ft_ia = F_ia + sum_kd L_iakd t1_kd, L_iajb = 2(ia|jb) - (ib|ja) (the
+  spin-summed form of sum Fia r1 + 1/4 sum R(j,b,i,a) r2(i,j,a,b)).
+
+The CIS matrix and r0 need MO integrals on the host; they come from the
+engine's orbitals and the Coulomb matrix of ``coulomb_matrix``, which follows
+the engine's model builder (readMoleculeInformation.f90:216-264).
+
+Triplet states (``states:spin`` = 1) have no spin-adapted closed-shell
+residual to differentiate and are not provided.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, replace
+
+import numpy as np
+
+from . import api
+from .molecules import Molecule
+from .polariz import BOHR_RADIUS, HARTREE_ENERGY, _align
+
+STATUS_CONVERGED, STATUS_MAXITER, STATUS_DIVERGED, STATUS_STAGNATED = 1, -1, -2, -3
+
+
+@dataclass
+class LRKeywords:
+    """``states`` and ``linear-response`` keys (src/input/definebd.f90:71-72, 159-171)."""
+    excited_states_number: int = 1      # states:excited-states-number (0..3; 0 means no LR run)
+    spin: int = 0                       # states:spin (0 singlet)
+    guess: str = "cis"                  # linear-response:guess ('cis' or 'rpa')
+    guess_threshold: float = 0.1        # linear-response:guess-threshold
+    max_iterations: int = 10000         # linear-response:max-iterations
+    accuracy: float = 6                 # linear-response:accuracy (exponent, 10^-value)
+    r1_step: float = 0.03               # linear-response:r1-step
+    r2_step: float = 0.03               # linear-response:r2-step
+    orthogonalization: bool = False     # linear-response:orthogonalization
+    diis_enabled: bool = True           # linear-response:diis-enabled
+    diis_steps: int = 20                # linear-response:diis-steps
+    store_solution_threshold: float = 2  # linear-response:store-solution-threshold (exponent)
+    store_solution_mode: str = "r1r2"   # linear-response:store-solution-mode
+
+
+# ---------------------------------------------------------------- spin-adapted vector algebra
+
+def swap_ab(x2):
+    return x2.transpose(0, 1, 3, 2)
+
+
+def inner(x, y):
+    """Sum over the reference's unique spin-orbital amplitudes of two singlet vectors."""
+    (x1, x2), (y1, y2) = x, y
+    dx, dy = x2 - swap_ab(x2), y2 - swap_ab(y2)
+    return 2.0 * float(np.vdot(x1, y1)) + float(np.vdot(x2, y2)) + 0.5 * float(np.vdot(dx, dy))
+
+
+def inner_full(x, y):
+    """Sum over ALL spin-orbital elements (orthogonalization's overlap, :466-496)."""
+    (x1, x2), (y1, y2) = x, y
+    dx, dy = x2 - swap_ab(x2), y2 - swap_ab(y2)
+    return 2.0 * float(np.vdot(x1, y1)) + 4.0 * float(np.vdot(x2, y2)) + 2.0 * float(np.vdot(dx, dy))
+
+
+def pair_symmetric(x2):
+    """x2 made exactly pair-symmetric, x2[j, i, b, a] = x2[i, j, a, b]: the spin-adapted form of
+    normalize's refill of the antisymmetric r2 from its unique elements (:436-447)."""
+    return 0.5 * (x2 + x2.transpose(1, 0, 3, 2))
+
+
+def max_abs(x):
+    """(max|d1|, max|d2|) of the spin-orbital vector."""
+    x1, x2 = x
+    return float(np.abs(x1).max()), max(float(np.abs(x2).max()), float(np.abs(x2 - swap_ab(x2)).max()))
+
+
+# ---------------------------------------------------------------- integrals on the host
+
+def coulomb_matrix(mol: Molecule, kind: str = "ohno-klopman") -> np.ndarray:
+    """The engine's site Coulomb matrix gamma (centred coordinates, trConst = 1/(a0 Eh))."""
+    c = np.asarray(mol.coords, dtype=np.float64)
+    c = c - c.sum(axis=0) / c.shape[0]
+    g_site = np.asarray(mol.gamma, dtype=np.float64)
+    r = np.sqrt(((c[:, None, :] - c[None, :, :]) ** 2).sum(-1))
+    med = (g_site[:, None] + g_site[None, :]) / 2.0
+    tr = 1.0 / (BOHR_RADIUS * HARTREE_ENERGY)
+    if kind == "ohno-klopman":
+        return med / np.sqrt(1.0 + (tr * med * r) ** 2)
+    if kind == "mataga-nishimoto":
+        return med / (1.0 + tr * med * r)
+    if kind == "hubbard":
+        return np.diag(g_site)
+    raise ValueError(f"unknown coulomb-integrals type {kind!r}")
+
+
+class MOIntegrals:
+    """(pq|rs) blocks of the ZDO model in the MO basis: J[i,a,j,b] = (ia|jb), Kvo[i,a,j,b] = (ab|ij)."""
+
+    def __init__(self, C, G, o):
+        N = C.shape[0]
+        v = N - o
+        Co, Cv = C[:, :o], C[:, o:]
+        Bov = (Co[:, :, None] * Cv[:, None, :]).reshape(N, o * v)
+        Bvv = (Cv[:, :, None] * Cv[:, None, :]).reshape(N, v * v)
+        Boo = (Co[:, :, None] * Co[:, None, :]).reshape(N, o * o)
+        self.J = (Bov.T @ G @ Bov).reshape(o, v, o, v)                            # (ia|jb)
+        self.Kvo = (Bvv.T @ G @ Boo).reshape(v, v, o, o).transpose(2, 0, 3, 1)     # (ab|ij) -> [i,a,j,b]
+        self.L = 2.0 * self.J - self.J.transpose(0, 3, 2, 1)                     # 2(ia|jb) - (ib|ja)
+
+
+def guess_vectors(F, I: MOIntegrals, nstates, kind="cis", threshold=0.1):
+    """prepareGuess + guessState: per state the singles (i, a, c) with |c| >= threshold, and the roots."""
+    o, v = I.J.shape[0], I.J.shape[1]
+    e = np.diag(F)
+    A = (2.0 * I.J - I.Kvo).reshape(o * v, o * v)
+    A[np.diag_indices_from(A)] += (e[None, o:] - e[:o, None]).ravel()
+    if kind == "cis":
+        w, U = np.linalg.eigh(A)
+    elif kind == "rpa":
+        Bm = (2.0 * I.J - I.J.transpose(0, 3, 2, 1)).reshape(o * v, o * v)   # 2(ai|bj) - (aj|bi)
+        w, U = np.linalg.eigh(np.block([[A, Bm], [Bm, A]]))
+        U = U[:o * v]
+    else:
+        raise ValueError(f"linear-response:guess {kind!r}: the guesses are 'cis' and 'rpa'")
+    out = []
+    for k in range(nstates):
+        out.append([(m // v, m % v, float(U[m, k])) for m in range(o * v) if abs(U[m, k]) >= threshold])
+    return out, w
+
+
+def guess_space(F, I: MOIntegrals, n):
+    """The n lowest CIS vectors, whole, as (r1, 0) (the Davidson solver's first basis)."""
+    o, v = I.J.shape[0], I.J.shape[1]
+    e = np.diag(F)
+    A = (2.0 * I.J - I.Kvo).reshape(o * v, o * v)
+    A[np.diag_indices_from(A)] += (e[None, o:] - e[:o, None]).ravel()
+    _, U = np.linalg.eigh(A)
+    return [(U[:, k].reshape(o, v).copy(), np.zeros((o, o, v, v))) for k in range(n)]
+
+
+def seed_vector(sel, o, v):
+    r1 = np.zeros((o, v))
+    for i, a, c in sel:
+        r1[i, a] = c
+    return r1, np.zeros((o, o, v, v))
+
+
+# ---------------------------------------------------------------- the device sigma
+
+class DeviceSigma:
+    """J r for up to ``nvec`` vectors per call: four residual evaluations per vector in one batch."""
+
+    STEPS = (1.0, -1.0, 2.0, -2.0)
+
+    def __init__(self, mol: Molecule, keywords: api.Keywords, t1, t2, C0, nvec=1, h=1e-2, engine=None):
+        kw = replace(keywords, precision="fp64", guess="reference", t1_step=1.0, t2_step=1.0)
+        self.cc = (engine or api.CoupledCluster)([mol] * (4 * nvec), kw)
+        self.cc.initCC()
+        self.t1, self.t2, self.h, self.nvec = t1, t2, h, nvec
+        self.eps = 10.0 ** (-keywords.accuracy)
+        o = t1.shape[0]
+        self.signs, self.D1, self.D2 = [], [], []
+        for k in range(4 * nvec):
+            s = self.cc.scf(k)
+            sg = _align(C0, s["C"])
+            if np.abs(s["C"] * sg[None, :] - C0).max() > 1e-8:
+                raise RuntimeError("the evaluator's orbitals differ from the ground state's beyond a sign")
+            self.signs.append((sg[:o], sg[o:]))
+            e = np.diag(s["F"])
+            eo, ev = e[:o], e[o:]
+            self.D1.append(eo[:, None] - ev[None, :])
+            self.D2.append(eo[:, None, None, None] + eo[None, :, None, None]
+                           - ev[None, None, :, None] - ev[None, None, None, :])
+
+    def _basis(self, k, x1, x2):
+        so, sv = self.signs[k]
+        return (x1 * so[:, None] * sv[None, :],
+                x2 * so[:, None, None, None] * so[None, :, None, None] * sv[None, None, :, None] * sv[None, None, None, :])
+
+    def __call__(self, vecs):
+        if len(vecs) > self.nvec:
+            raise ValueError(f"{len(vecs)} vectors for an evaluator of {self.nvec}")
+        points = []
+        for q, (r1, r2) in enumerate(vecs):
+            for m, c in enumerate(self.STEPS):
+                x1, x2 = self.t1 + c * self.h * r1, self.t2 + c * self.h * r2
+                self.cc.set_guess(4 * q + m, *self._basis(4 * q + m, x1, x2))
+                points.append((x1, x2))
+        for k in range(4 * len(vecs), 4 * self.nvec):      # idle copies restart from t every call
+            self.cc.set_guess(k, *self._basis(k, self.t1, self.t2))
+        self.cc.iterationCC(1, self.eps)
+        out = []
+        for q in range(len(vecs)):
+            om = []
+            for m in range(4):
+                k = 4 * q + m
+                a1, a2 = self._basis(k, *self.cc.amplitudes(k))
+                x1, x2 = points[k]
+                om.append(((a1 - x1) * self.D1[k], (a2 - x2) * self.D2[k] / 3.0))
+            s1, s2 = ((8.0 * (om[0][p] - om[1][p]) - (om[2][p] - om[3][p])) / (12.0 * self.h) for p in range(2))
+            out.append((s1, pair_symmetric(s2)))
+        return out
+
+    def close(self):
+        self.cc.finalizeCC()
+
+
+# ---------------------------------------------------------------- the iteration
+
+class _Rules:
+    """Stop rules of the generic iterator (gIterator.f90:88-210), the iteration block's settings."""
+
+    def __init__(self, kw: api.Keywords, maxiter, eps):
+        self.kw, self.maxiter, self.eps = kw, maxiter, eps
+        self.iteration, self.successful, self.current = 0, 1, 0.0
+
+    def update(self, acc):
+        self.iteration += 1
+        previous, self.current = self.current, acc
+        if self.current < previous:
+            self.successful += 1
+        if self.current < self.eps:
+            return STATUS_CONVERGED
+        if not np.isfinite(self.current) or (self.kw.enable_divergence_check
+                                             and self.current > 10.0 ** self.kw.divergence_threshold):
+            return STATUS_DIVERGED
+        if self.iteration + 1 > self.maxiter:
+            return STATUS_MAXITER
+        if (self.kw.enable_stagnation_check and self.iteration > self.kw.stagnation_check_after
+                and 100.0 * self.successful / self.iteration <= self.kw.stagnation_threshold):
+            return STATUS_STAGNATED
+        return None
+
+
+class _Diis:
+    """pushLRVectors / newLRVectors / diisDotProduct on spin-adapted vectors."""
+
+    def __init__(self, nd):
+        self.nd, self.st, self.sd = nd, [], []
+        self.B = np.zeros((nd + 1, nd + 1))
+
+    def push(self, r, d):
+        self.st.insert(0, (r[0].copy(), r[1].copy()))
+        self.sd.insert(0, (d[0].copy(), d[1].copy()))
+        del self.st[self.nd:], self.sd[self.nd:]
+
+    def extrapolate(self, iteration, r):
+        n = min(iteration, self.nd)
+        B = self.B
+        B[1:n, 1:n] = B[0:n - 1, 0:n - 1].copy()
+        for k in range(n):
+            B[k, 0] = B[0, k] = inner(self.sd[k], self.sd[0])
+        if n == 1:
+            return r
+        A = np.ones((n + 1, n + 1)); A[:n, :n] = B[:n, :n]; A[n, n] = 0.0
+        lam, U = np.linalg.eigh(A)
+        c = (U[:n, :] * U[n, :][None, :] / lam[None, :]).sum(axis=1)
+        return (sum(c[k] * self.st[k][0] for k in range(n)), sum(c[k] * self.st[k][1] for k in range(n)))
+
+
+class _State:
+    def __init__(self, r, kw, lr, eps):
+        self.r = r
+        self.rules = _Rules(kw, lr.max_iterations, eps)
+        self.diis = _Diis(lr.diis_steps) if lr.diis_enabled else None
+        self.status, self.omega = None, 0.0
+
+
+def iterate_states(sigma, seeds, kw: api.Keywords, lr: LRKeywords, held=()):
+    """Run the reference's iteration for every seed vector together; returns the finished states.
+
+    ``sigma`` maps a list of vectors to their J r (one call per iteration);
+    ``held`` are (r1, r2) of states found before (for orthogonalization).
+    """
+    base = 10.0 ** (-lr.accuracy)
+    first = len(held)
+    states = [_State(r, kw, lr, base * 2.0 ** (first + k)) for k, r in enumerate(seeds)]
+    held = list(held)
+    while any(s.status is None for s in states):
+        live = [s for s in states if s.status is None]
+        for s, d in zip(live, sigma([s.r for s in live])):
+            r = s.r
+            # stepLR
+            s.omega = inner(d, r) / inner(r, r)
+            d = (d[0] - s.omega * r[0], d[1] - s.omega * r[1])
+            r = (r[0] - lr.r1_step * d[0], r[1] - lr.r2_step * d[1])
+            acc = max_abs(d)
+            scale = 1.0 / np.sqrt(inner(r, r))
+            r = (r[0] * scale, pair_symmetric(r[1]) * scale)
+            if lr.orthogonalization and held:
+                ov = [inner_full(r, h) for h in held]
+                r = (r[0] - sum(c * h[0] for c, h in zip(ov, held)), r[1] - sum(c * h[1] for c, h in zip(ov, held)))
+            if max(acc) >= s.rules.eps and s.diis is not None:
+                s.diis.push(r, d)
+                r = s.diis.extrapolate(s.rules.iteration + 1, r)
+            s.r = r
+            s.status = s.rules.update(max(acc))
+    return states
+
+
+def davidson_states(sigma, seeds, nroots, F, kw: api.Keywords, lr: LRKeywords, track=None, max_space=None):
+    """The lowest ``nroots`` roots of J by block Davidson (not the reference's iteration).
+
+    The basis starts from ``seeds`` (more of them than roots, so that every
+    symmetry of the low roots is present) and stays orthonormal in ``inner``.
+    The lowest ``track`` Ritz pairs of the projected matrix (more than
+    ``nroots``: a state dominated by doubles starts high in a basis of CIS
+    vectors and has to be followed down) are refined with the residual divided
+    by (theta - orbital energy differences) until max|residual| of root k is
+    below accuracy * 2^k (the reference's per-state targets; the extra roots
+    take the last one). Each iteration evaluates the new basis vectors in one
+    ``sigma`` call. Deterministic: it converges to the lowest roots of the
+    symmetries the seeds span, whatever the rounding of the sigma vectors.
+    """
+    k = min(track or nroots + 4, len(seeds))
+    o, v = seeds[0][0].shape
+    e = np.diag(F)
+    eo, ev = e[:o], e[o:]
+    D1 = ev[None, :] - eo[:, None]
+    D2 = (ev[None, None, :, None] + ev[None, None, None, :] - eo[:, None, None, None] - eo[None, :, None, None])
+    max_space = max_space or max(8 * k, 2 * len(seeds), 16)
+    targets = [10.0 ** (-lr.accuracy) * 2.0 ** min(q, nroots - 1) for q in range(k)]
+    V, W = [], []
+
+    def orthonormal(x):
+        n0 = np.sqrt(max(inner(x, x), 0.0))
+        if n0 == 0.0:
+            return None
+        x = (x[0] / n0, x[1] / n0)
+        for _ in range(2):
+            for b in V:
+                c = inner(b, x)
+                x = (x[0] - c * b[0], x[1] - c * b[1])
+        n = np.sqrt(max(inner(x, x), 0.0))
+        return None if n < 1e-10 else (x[0] / n, x[1] / n)
+
+    def extend(vectors):
+        new = []
+        for x in vectors:
+            y = orthonormal(x)
+            if y is not None:
+                V.append(y)
+                new.append(y)
+        for lo in range(0, len(new), sigma.nvec):
+            W.extend(sigma(new[lo:lo + sigma.nvec]))
+        return len(new)
+
+    extend(list(seeds))
+    states = [_State(None, kw, lr, t) for t in targets]
+    iteration = 0
+    while True:
+        iteration += 1
+        m = len(V)
+        H = np.array([[inner(V[i], W[j]) for j in range(m)] for i in range(m)])
+        theta, Y = np.linalg.eig(H)
+        order = np.argsort(theta.real)[:k]
+        ritz = []
+        for q, idx in enumerate(order):
+            y = Y[:, idx].real
+            x = (sum(y[j] * V[j][0] for j in range(m)), sum(y[j] * V[j][1] for j in range(m)))
+            s = (sum(y[j] * W[j][0] for j in range(m)), sum(y[j] * W[j][1] for j in range(m)))
+            n = np.sqrt(inner(x, x))
+            x, s = (x[0] / n, x[1] / n), (s[0] / n, s[1] / n)
+            w = float(theta[idx].real)
+            res = (s[0] - w * x[0], s[1] - w * x[1])
+            ritz.append((w, x, s, res, max(max_abs(res))))
+        for st, (w, x, _, _, acc) in zip(states, ritz):
+            st.omega, st.r = w, x
+            st.rules.iteration = iteration
+            st.status = STATUS_CONVERGED if acc < st.rules.eps else None
+        if all(st.status == STATUS_CONVERGED for st in states):
+            return states[:nroots]
+        if iteration >= lr.max_iterations:
+            for st in states:
+                st.status = st.status or STATUS_MAXITER
+            return states[:nroots]
+        corr = []
+        for st, (w, x, s, res, acc) in zip(states, ritz):
+            if st.status is None:
+                d1, d2 = w - D1, w - D2
+                d1 = np.where(np.abs(d1) < 1e-3, 1e-3, d1)
+                d2 = np.where(np.abs(d2) < 1e-3, 1e-3, d2)
+                corr.append((res[0] / d1, pair_symmetric(res[1] / d2)))
+        if len(V) + len(corr) > max_space:             # restart on the Ritz vectors
+            V.clear(); W.clear()
+            keep = []
+            for (w, x, s, res, acc) in ritz:
+                y = orthonormal(x)
+                if y is not None:
+                    keep.append(y)
+                    V.append(y)
+            for lo in range(0, len(keep), sigma.nvec):
+                W.extend(sigma(keep[lo:lo + sigma.nvec]))
+        if extend(corr) == 0:
+            for st in states:
+                st.status = st.status or STATUS_STAGNATED
+            return states[:nroots]
+
+
+def linear_response(mol: Molecule, keywords: api.Keywords | None = None, lr: LRKeywords | None = None,
+                    seeds=None, engine=None, solver: str = "reference") -> dict:
+    """getEnergy('r-ccsd') with excited states: the r-ccsd ground state, then lr-r-ccsd.
+
+    Returns energy (E_CCSD), ccsd status/iterations, the ground state's t1, t2
+    and scf (orbitals C, MO Fock F), and per state (sorted by omega, as
+    resortStates): omega, E_total = E_CCSD + omega, r0, ael (average
+    excitation level), status, iterations, r1, r2 (in the orbitals C).
+    ``seeds`` replaces the CIS guess by earlier states (loadSolution): a list
+    of (r1, r2).
+
+    ``solver`` "reference" runs the reference's iteration. Which eigenpair
+    each of its states settles on depends on rounding: the damped step with
+    DIIS amplifies the components of lower states that rounding puts into a
+    vector of another symmetry, so two runs whose sigma vectors differ in the
+    last bits can end on different states (the reference's own OpenMP
+    reductions differ from run to run in the same way). Every state it returns
+    is an eigenpair of the problem. ``solver`` "davidson" returns the lowest
+    roots instead (``davidson_states``), reproducibly.
+    """
+    kw = keywords or api.Keywords()
+    lr = lr or LRKeywords()
+    nstates = lr.excited_states_number
+    if not 1 <= nstates <= 3:
+        raise ValueError("states:excited-states-number must be 1..3 for an LR run")
+    if lr.spin != 0:
+        raise NotImplementedError("states:spin = 1 (triplets) is not provided: the engine's residual is spin-adapted")
+    factory = engine or api.CoupledCluster
+    c0 = factory(mol, kw)
+    c0.initCC()
+    gs = c0.iterate()
+    t1, t2 = c0.amplitudes(0)
+    scf = c0.scf(0)
+    c0.finalizeCC()
+    out = {"energy": float(gs["energy"][0]), "ccsd_status": int(gs["status"]),
+           "ccsd_iterations": int(gs["iterations"]), "t1": t1, "t2": t2, "scf": scf}
+    if gs["status"] != STATUS_CONVERGED:
+        raise RuntimeError(f"r-ccsd did not converge (status {gs['status']}): no LR run")
+    o = t1.shape[0]
+    C, F = scf["C"], scf["F"]
+    I = MOIntegrals(C, coulomb_matrix(mol, kw.coulomb_integrals), o)
+    v = t1.shape[1]
+    davidson_seeds = None
+    if seeds is None:
+        sel, _ = guess_vectors(F, I, nstates, lr.guess, lr.guess_threshold)
+        seeds = [seed_vector(s, o, v) for s in sel]
+        if solver == "davidson":
+            davidson_seeds = guess_space(F, I, min(o * v, max(2 * nstates, nstates + 4)))
+    seeds = list(seeds)[:nstates]
+    if any(inner(s, s) == 0.0 for s in seeds):
+        raise ValueError("a guess vector is empty (no singles reach linear-response:guess-threshold)")
+    if solver not in ("reference", "davidson"):
+        raise ValueError(f"solver {solver!r}: 'reference' or 'davidson'")
+    sequential = lr.orthogonalization and solver == "reference"
+    nvec = 1 if sequential else nstates
+    if solver == "davidson":
+        nvec = min(nstates + 4, len(davidson_seeds or seeds))
+    sig = DeviceSigma(mol, kw, t1, t2, C, nvec=nvec, engine=engine)
+    try:
+        if solver == "davidson":
+            states = davidson_states(sig, davidson_seeds or seeds, nstates, F, kw, lr, track=nvec)
+        elif sequential:
+            states = []
+            for r in seeds:
+                states += iterate_states(sig, [r], kw, lr, held=[s.r for s in states])
+        else:
+            states = iterate_states(sig, seeds, kw, lr)
+    finally:
+        sig.close()
+    Ft = F[:o, o:] + np.einsum("iakd,kd->ia", I.L, t1)
+    rows = []
+    for s in states:
+        r1, r2 = s.r
+        s1 = 2.0 * float((r1 * r1).sum())
+        s2 = inner((0 * r1, r2), (0 * r1, r2))
+        r0 = (2.0 * float((Ft * r1).sum()) + float(np.einsum("iajb,ijab->", I.L, r2))) / s.omega
+        rows.append({"omega": s.omega, "r0": r0, "ael": (s1 + 2 * s2) / (s1 + s2), "status": s.status,
+                     "iterations": s.rules.iteration, "r1": r1, "r2": r2})
+    rows.sort(key=lambda x: x["omega"])
+    for key in ("omega", "r0", "ael", "status", "iterations"):
+        out[key] = np.array([x[key] for x in rows])
+    out["E_total"] = out["energy"] + out["omega"]
+    out["r1"] = [x["r1"] for x in rows]
+    out["r2"] = [x["r2"] for x in rows]
+    return out
+
+
+def stored_seeds(result: dict, lr: LRKeywords | None = None):
+    """dumpSolution / loadSolution (:593-734): the states' amplitudes above the store threshold
+    (in the spin-adapted coordinates), by store-solution-mode, as seeds for the next run."""
+    lr = lr or LRKeywords()
+    thr = 10.0 ** (-lr.store_solution_threshold)
+    seeds = []
+    for r1, r2 in zip(result["r1"], result["r2"]):
+        a1 = np.where(np.abs(r1) > thr, r1, 0.0) if "r1" in lr.store_solution_mode else 0 * r1
+        a2 = np.where(np.abs(r2) > thr, r2, 0.0) if lr.store_solution_mode in ("r2", "r1r2") else 0 * r2
+        seeds.append((a1, a2))
+    return seeds

@@ -1,0 +1,81 @@
+"""lr-r-ccsd on the GPU (helios_gb300.lrccsd over the engine) against the oracle.
+
+The device sigma (four residual evaluations of the engine per vector) must be
+the Jacobian of the closed-shell residual; every state the driver returns
+must be an eigenpair of the reference's own spin-orbital sigma equations
+(proj-lrccsd-spin-hf-*.f90, restated in oracle/lrccsd.py) with energyLR's r0
+and excitation level; the Davidson solver must return the lowest roots. The
+oracle works in the device's orbitals and ground-state amplitudes.
+"""
+import numpy as np
+import pytest
+
+from helios_gb300 import molecules
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def lr():
+    from helios_gb300 import build
+    build.build()
+    from helios_gb300 import lrccsd
+    return lrccsd
+
+
+def test_device_sigma_is_the_closed_shell_jacobian(lr):
+    from helios_gb300 import api
+    from oracle import lrccsd as olr
+    from oracle.ppp import build_model
+    mol = molecules.polyene(6)
+    kw = api.Keywords(bond_alternation=0.1, accuracy=12)
+    cc = api.CoupledCluster(mol, kw)
+    cc.initCC()
+    assert cc.iterate()["status"] == 1
+    t1, t2 = cc.amplitudes(0)
+    s = cc.scf(0)
+    cc.finalizeCC()
+    o, v = t1.shape
+    sig = lr.DeviceSigma(mol, kw, t1, t2, s["C"], nvec=2)
+    rng = np.random.default_rng(5)
+    vecs = []
+    for _ in range(2):
+        r2 = rng.normal(size=(o, o, v, v))
+        vecs.append((rng.normal(size=(o, v)), 0.5 * (r2 + r2.transpose(1, 0, 3, 2))))
+    got = sig(vecs)
+    sig.close()
+    J = olr.closed_shell_jacobian(s["F"], s["C"], build_model(mol, alternation=0.1)["G"], o, t1, t2)
+    for (s1, s2), r in zip(got, vecs):
+        want1, want2 = olr.closed_shell_unpack(J @ olr.closed_shell_pack(*r), o, v)
+        scale = max(np.abs(want1).max(), np.abs(want2).max())
+        assert np.abs(s1 - want1).max() < 1e-9 * scale and np.abs(s2 - want2).max() < 1e-9 * scale
+
+
+@pytest.mark.parametrize("solver", ["reference", "davidson"])
+@pytest.mark.parametrize("mol", [molecules.polyene(4), molecules.polyene(6), molecules.dodecahexaene(),
+                                 molecules.random_molecule(7, 6, 8)],
+                         ids=["butadiene", "hexatriene", "dodecahexaene", "rnd7"])
+def test_states_are_eigenpairs_of_the_reference_equations(lr, mol, solver):
+    from helios_gb300 import api
+    from oracle import lrccsd as olr
+    from oracle.ppp import build_model
+    from oracle.triples import spin_amplitudes
+    kw = api.Keywords(bond_alternation=0.1, accuracy=12)
+    got = lr.linear_response(mol, kw, lr.LRKeywords(excited_states_number=3, accuracy=8), solver=solver)
+    assert got["ccsd_status"] == 1 and list(got["status"]) == [1, 1, 1]
+    model = build_model(mol, alternation=0.1)
+    C, F, t1, t2 = got["scf"]["C"], got["scf"]["F"], got["t1"], got["t2"]
+    o = t1.shape[0]
+    P = olr.SpinProblem(C, model["G"], model["core"], o, t1, t2)
+    X = olr.intermediates(P)
+    spec = np.sort(np.linalg.eigvals(olr.closed_shell_jacobian(F, C, model["G"], o, t1, t2)).real)
+    for k in range(3):
+        w = got["omega"][k]
+        assert np.min(np.abs(spec - w)) < 1e-8
+        r1s, r2s = spin_amplitudes(got["r1"][k], got["r2"][k])
+        d1, d2 = olr.sigma(P, X, r1s, r2s)
+        assert max(np.abs(d1 - w * r1s).max(), np.abs(d2 - w * r2s).max()) < 1e-7 * 2 ** k
+        _, r0, ael = olr.lr_energy(P, X, r1s, r2s, w)
+        assert got["r0"][k] == pytest.approx(r0, abs=1e-8) and got["ael"][k] == pytest.approx(ael, rel=1e-10)
+    if solver == "davidson":
+        assert np.abs(got["omega"] - spec[:3]).max() < 1e-8
