@@ -11,10 +11,12 @@ per bond ``i j beta kind`` (1-based sites, kind single / double / nonset).
 ``read_input`` returns the molecule, the engine keywords (the keys of
 definebd.f90 that the r-ccsd path reads, with their defaults and their
 power-of-ten ("potentiate") conventions) and the job (method, jobtype,
-polarizability grid, harvest); ``write_input`` writes the same format;
-``run_input`` runs an energy job of method r-ccsd or r-ccsd(t), or a
-polarizability job of r-ccsd. Engine
-options the reference has no key for (precision, guess, mixed_check) go in a
+polarizability grid, harvest, and the ``states`` / ``linear-response`` keys
+of an LR-CCSD run); ``write_input`` writes the same format; ``run_input``
+runs an energy job of method r-ccsd (with its excited states when
+``states:excited-states-number`` > 0, as getEnergy, mod_property.f90:159-175)
+or r-ccsd(t), or a polarizability job of r-ccsd. Engine options the
+reference has no key for (precision, guess, mixed_check, lr-solver) go in a
 ``%engine{ }`` block, which the reference's reader never looks for.
 """
 from __future__ import annotations
@@ -26,6 +28,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import api
+from .lrccsd import LRKeywords
 from .molecules import Molecule
 
 # keys of definebd.f90 that the path reads: (block, key) -> (Keywords field, kind, default)
@@ -53,6 +56,23 @@ _KEYS = {
     ("engine", "mixed-check"): ("mixed_check", "str", "emulated"),
 }
 
+# keys of the states and linear-response blocks (definebd.f90:71-72, 159-171) -> LRKeywords field
+_LR_KEYS = {
+    ("states", "excited-states-number"): ("excited_states_number", "int"),
+    ("states", "spin"): ("spin", "int"),
+    ("linear-response", "guess"): ("guess", "str"),
+    ("linear-response", "guess-threshold"): ("guess_threshold", "float"),
+    ("linear-response", "max-iterations"): ("max_iterations", "int"),
+    ("linear-response", "accuracy"): ("accuracy", "float"),
+    ("linear-response", "r1-step"): ("r1_step", "float"),
+    ("linear-response", "r2-step"): ("r2_step", "float"),
+    ("linear-response", "orthogonalization"): ("orthogonalization", "bool"),
+    ("linear-response", "diis-enabled"): ("diis_enabled", "bool"),
+    ("linear-response", "diis-steps"): ("diis_steps", "int"),
+    ("linear-response", "store-solution-threshold"): ("store_solution_threshold", "float"),
+    ("linear-response", "store-solution-mode"): ("store_solution_mode", "str"),
+}
+
 
 @dataclass
 class Job:
@@ -64,6 +84,8 @@ class Job:
     harvest: bool = False              # system:harvest
     output_file: str = "%input%"       # general:output-file
     symbols: list = field(default_factory=list)
+    lr: LRKeywords = field(default_factory=lambda: LRKeywords(excited_states_number=0))  # states, linear-response
+    lr_solver: str = "reference"       # engine:lr-solver ("reference" iteration or "davidson")
 
 
 def strip_comments(text: str) -> str:
@@ -155,6 +177,11 @@ def read_input(source: str) -> tuple[Molecule, api.Keywords, Job]:
     job.points = int(float(pz.get("points", job.points)))
     job.derive_step = float(pz.get("derive-step", job.derive_step))
     job.harvest = _value("bool", sysb["harvest"]) if "harvest" in sysb else False
+    for (blk, key), (attr, kind) in _LR_KEYS.items():
+        if key in blocks.get(blk, {}):
+            setattr(job.lr, attr, _value(kind, blocks[blk][key]))
+    if "lr-solver" in blocks.get("engine", {}):
+        job.lr_solver = _value("str", blocks["engine"]["lr-solver"])
     return mol, kw, job
 
 
@@ -171,12 +198,19 @@ def write_input(mol: Molecule, kw: api.Keywords | None = None, job: Job | None =
         if kind == "bool":
             v = "true" if v else "false"
         by_block.setdefault(blk, []).append(f"  {key} = {v}")
+    by_block["engine"].append(f"  lr-solver = {job.lr_solver}")
     for blk, items in by_block.items():
         lines += [f"%{blk}{{", ",\n".join(items), "}", ""]
     lines += ["%field{", ",\n".join(f"  along-{a} = {float(v)!r}" for a, v in zip("xyz", kw.field)), "}", ""]
     lines += ["%polariz{", f"  components = {job.components},", f"  points = {job.points},",
               f"  derive-step = {job.derive_step!r}", "}", ""]
     lines += ["%system{", f"  harvest = {'true' if job.harvest else 'false'}", "}", ""]
+    by_block = {}
+    for (blk, key), (attr, kind) in _LR_KEYS.items():
+        v = getattr(job.lr, attr)
+        by_block.setdefault(blk, []).append(f"  {key} = {('true' if v else 'false') if kind == 'bool' else v}")
+    for blk, items in by_block.items():
+        lines += [f"%{blk}{{", ",\n".join(items), "}", ""]
     sym = symbols or ["C"] * mol.n_sites
     ne = int(np.sum(mol.nels))
     lines += ["%molecule{", mol.name, str(mol.n_sites), str(len(mol.bonds)), str(ne - ne // 2), str(ne // 2)]
@@ -189,13 +223,20 @@ def write_input(mol: Molecule, kw: api.Keywords | None = None, job: Job | None =
     return "\n".join(lines)
 
 
-def run_input(source: str, harvest_file: str | None = None) -> dict:
-    """Run the job of an input file on the engine (methods r-ccsd and r-ccsd(t))."""
+def run_input(source: str, harvest_file: str | None = None, engine=None) -> dict:
+    """Run the job of an input file on the engine (methods r-ccsd and r-ccsd(t)).
+
+    ``engine`` replaces api.CoupledCluster (a stand-in for tests without a GPU)."""
     mol, kw, job = read_input(source)
     if job.methods not in (["r-ccsd"], ["r-ccsd(t)"]):
         raise ValueError(f"methods {job.methods}: the engine runs r-ccsd and r-ccsd(t)")
+    if job.jobtype == "energy" and job.methods == ["r-ccsd"] and job.lr.excited_states_number > 0:
+        from . import lrccsd
+        lr = lrccsd.linear_response(mol, kw, job.lr, engine=engine, solver=job.lr_solver)
+        return {"job": job, "energy": lr["ccsd_energy"], "status": lr["ccsd_status"],
+                "iterations": lr["ccsd_iterations"], "excited": lr}
     if job.jobtype == "energy":
-        cc = api.CoupledCluster(mol, kw)
+        cc = (engine or api.CoupledCluster)(mol, kw)
         cc.initCC()
         out = cc.iterate()
         res = {"job": job, "energy": out["energy"], "status": out["status"], "iterations": out["iterations"]}
@@ -233,3 +274,9 @@ if __name__ == "__main__":
         if "triples" in r:
             print(f"(T) {r['triples']['T']:.12f} eV  E_CCSD(T) {r['energy_ccsd_t_textbook']:.12f} eV  "
                   f"(reference convention: {r['energy_ccsd_t']:.12f} eV)")
+        if "excited" in r:
+            x = r["excited"]
+            for k in range(len(x["omega"])):
+                print(f"state {k + 1}: omega {x['omega'][k]:.10f} eV  E_total {x['E_total'][k]:.12f} eV  "
+                      f"r0 {x['r0'][k]:+.6f}  excitation level {x['ael'][k]:.6f}  "
+                      f"status {x['status'][k]} iterations {x['iterations'][k]}")

@@ -473,7 +473,8 @@ def linear_response(mol: Molecule, keywords: api.Keywords | None = None, lr: LRK
     scf = c0.scf(0)
     c0.finalizeCC()
     out = {"energy": float(gs["energy"][0]), "ccsd_status": int(gs["status"]),
-           "ccsd_iterations": int(gs["iterations"]), "t1": t1, "t2": t2, "scf": scf}
+           "ccsd_iterations": int(gs["iterations"]), "ccsd_energy": np.array(gs["energy"]),
+           "t1": t1, "t2": t2, "scf": scf}
     if gs["status"] != STATUS_CONVERGED:
         raise RuntimeError(f"r-ccsd did not converge (status {gs['status']}): no LR run")
     o = t1.shape[0]

@@ -84,3 +84,32 @@ def test_unknown_method_or_job_is_an_error():
     text = _dodecahexaene_text().replace("method = r-ccsd", "method = u-ccsd")
     with pytest.raises(ValueError):
         inputfile.run_input(text)
+
+
+def test_states_and_linear_response_blocks():
+    text = _dodecahexaene_text().replace(
+        "%scf{ accuracy = 11 }",
+        "%scf{ accuracy = 11 }\n%states{ excited-states-number = 2 }\n"
+        "%Linear-Response{ accuracy = 7, orthogonalization = true, guess = rpa, r1-step = 0.05 }\n"
+        "%engine{ lr-solver = davidson }")
+    mol, kw, job = inputfile.read_input(text)
+    assert job.lr.excited_states_number == 2 and job.lr.spin == 0
+    assert job.lr.accuracy == 7 and job.lr.orthogonalization is True and job.lr.guess == "rpa"
+    assert job.lr.r1_step == 0.05 and job.lr.r2_step == 0.03 and job.lr.diis_steps == 20     # defaults
+    assert job.lr_solver == "davidson" and kw.precision == "mixed"                          # both engine blocks
+    m2, kw2, job2 = inputfile.read_input(inputfile.write_input(mol, kw, job))
+    assert job2.lr == job.lr and job2.lr_solver == job.lr_solver
+    # no states block: no LR run
+    assert inputfile.read_input(_dodecahexaene_text())[2].lr.excited_states_number == 0
+
+
+def test_energy_job_with_excited_states_runs_lr(tmp_path):
+    from fake_engine import FakeCoupledCluster
+    mol = molecules.polyene(4)
+    job = inputfile.Job(lr=inputfile.LRKeywords(excited_states_number=2, accuracy=7), lr_solver="davidson")
+    r = inputfile.run_input(inputfile.write_input(mol, api.Keywords(bond_alternation=0.1, accuracy=12), job),
+                            engine=FakeCoupledCluster)
+    x = r["excited"]
+    assert r["status"] == 1 and list(x["status"]) == [1, 1]
+    assert np.allclose(x["E_total"], r["energy"][0] + x["omega"])
+    assert 0 < x["omega"][0] < x["omega"][1]

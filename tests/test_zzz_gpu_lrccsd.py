@@ -79,3 +79,15 @@ def test_states_are_eigenpairs_of_the_reference_equations(lr, mol, solver):
         assert got["r0"][k] == pytest.approx(r0, abs=1e-8) and got["ael"][k] == pytest.approx(ael, rel=1e-10)
     if solver == "davidson":
         assert np.abs(got["omega"] - spec[:3]).max() < 1e-8
+
+
+def test_input_file_energy_job_with_states(lr):
+    from helios_gb300 import api, inputfile
+    mol = molecules.polyene(6)
+    kw = api.Keywords(bond_alternation=0.1, accuracy=12)
+    job = inputfile.Job(lr=lr.LRKeywords(excited_states_number=2, accuracy=8), lr_solver="davidson")
+    r = inputfile.run_input(inputfile.write_input(mol, kw, job))
+    want = lr.linear_response(mol, kw, lr.LRKeywords(excited_states_number=2, accuracy=8), solver="davidson")
+    assert r["status"] == 1 and list(r["excited"]["status"]) == [1, 1]
+    assert np.abs(r["excited"]["omega"] - want["omega"]).max() < 1e-9
+    assert np.allclose(r["excited"]["E_total"], r["energy"][0] + r["excited"]["omega"])
