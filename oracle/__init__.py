@@ -9,6 +9,8 @@ path, and the reference (Fortran with compiler-specific extensions and no
 build files) cannot be built or run here. The restatement is pinned instead
 by the agreement of independent codes (literal, factorised and textbook
 spin-orbital CCSD; the reference's spin-orbital (T) loop and the published
-(T)) and by exact invariants, in tests/test_oracle.py and
-tests/test_oracle_triples.py.
+(T); the reference's LR-CCSD sigma equations and the exact determinant-space
+similarity-transformed Hamiltonian) and by exact invariants, in
+tests/test_oracle.py, tests/test_oracle_triples.py and
+tests/test_oracle_lrccsd.py.
 """
