@@ -91,3 +91,21 @@ def test_input_file_energy_job_with_states(lr):
     assert r["status"] == 1 and list(r["excited"]["status"]) == [1, 1]
     assert np.abs(r["excited"]["omega"] - want["omega"]).max() < 1e-9
     assert np.allclose(r["excited"]["E_total"], r["energy"][0] + r["excited"]["omega"])
+
+
+@pytest.mark.parametrize("mol", [molecules.dodecahexaene(), molecules.ladder(8)], ids=["dodecahexaene", "ladder-8"])
+def test_reference_iteration_reproduces_the_oracles_states(lr, mol):
+    # on these molecules the reference's iteration ends on the same three states whatever the
+    # rounding (measured on the oracle with noise up to 1e-11 added to every sigma vector)
+    from helios_gb300 import api
+    from oracle import lrccsd as olr
+    from oracle.ppp import build_model
+    kw = api.Keywords(bond_alternation=0.1, accuracy=12)
+    got = lr.linear_response(mol, kw, lr.LRKeywords(excited_states_number=3, accuracy=8))
+    model = build_model(mol, alternation=0.1)
+    o = got["t1"].shape[0]
+    want = olr.lr_solve(got["scf"]["C"], model["G"], model["core"], got["scf"]["F"], o, got["t1"], got["t2"],
+                        nstates=3, eps=1e-8)
+    assert list(got["status"]) == [1, 1, 1] and list(want["status"]) == [1, 1, 1]
+    assert np.abs(got["omega"] - want["omega"]).max() < 1e-8
+    assert np.abs(got["r0"] - want["r0"]).max() < 1e-7 and np.abs(got["ael"] - want["ael"]).max() < 1e-7
