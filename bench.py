@@ -322,6 +322,22 @@ def run_gb300(args):
         extra["triples"] = {"molecule": "ladder-64 (o = v = 32)", "ccsd_status": int(rt["status"]),
                             "ccsd_solve_s": tmt["solve_ms"] / 1e3, "T_eV": tt["T"], "E4_eV": tt["E4"],
                             "E5_eV": tt["E5"], "reference_term_eV": tt["reference_term"], "triples_s": secs_t}
+    # --- LR-CCSD: the three lowest singlet excited states of the same ladder (Davidson on the
+    #     engine's residual Jacobian); a failure here is recorded, not raised
+    if args.lr:
+        from helios_gb300 import lrccsd
+        try:
+            t0l = time.perf_counter()
+            rl = lrccsd.linear_response(molecules.ladder(64), api.Keywords(bond_alternation=0.1, accuracy=10),
+                                        lrccsd.LRKeywords(excited_states_number=3, accuracy=6, max_iterations=60),
+                                        solver="davidson")
+            extra["lr_ccsd"] = {"molecule": "ladder-64 (o = v = 32)", "solver": "davidson", "states": 3,
+                                "seconds": time.perf_counter() - t0l, "omega_eV": [float(x) for x in rl["omega"]],
+                                "status": [int(x) for x in rl["status"]], "iterations": int(max(rl["iterations"])),
+                                "sigma_calls": rl["sigma_calls"], "engine_copies": rl["engine_copies"],
+                                "r0": [float(x) for x in rl["r0"]], "excitation_level": [float(x) for x in rl["ael"]]}
+        except Exception as exc:                      # noqa: BLE001 -- reported in the JSON line
+            extra["lr_ccsd"] = {"error": f"{type(exc).__name__}: {exc}"}
     # --- end to end through the C ABI with host buffers
     e2e = run_e2e(api, mol, kw, max(1, min(args.steps, 3)))
     # --- roofline of the tcgen05 GEMM, live over the timed steps
@@ -500,6 +516,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-polariz", dest="polariz", action="store_false", help="skip the polarizability leg")
     ap.add_argument("--no-triples", dest="triples", action="store_false", help="skip the (T) leg")
+    ap.add_argument("--no-lr", dest="lr", action="store_false", help="skip the LR-CCSD leg")
     ap.add_argument("--ref-pairs", type=int, default=48, help="doubles pairs per reference-arm step")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -89,18 +89,24 @@ def swap_ab(x2):
     return x2.transpose(0, 1, 3, 2)
 
 
+def _dots(x, y):
+    """(sum x1 y1, sum x2 y2, sum x2 y2^ab) without temporaries of the doubles size."""
+    return (float(np.vdot(x[0], y[0])), float(np.vdot(x[1], y[1])),
+            float(np.einsum("ijab,ijba->", x[1], y[1], optimize=False)))
+
+
 def inner(x, y):
-    """Sum over the reference's unique spin-orbital amplitudes of two singlet vectors."""
-    (x1, x2), (y1, y2) = x, y
-    dx, dy = x2 - swap_ab(x2), y2 - swap_ab(y2)
-    return 2.0 * float(np.vdot(x1, y1)) + float(np.vdot(x2, y2)) + 0.5 * float(np.vdot(dx, dy))
+    """Sum over the reference's unique spin-orbital amplitudes of two singlet vectors:
+    2 sum x1 y1 + sum x2 y2 + 1/2 sum (x2 - x2^ab)(y2 - y2^ab) = 2 x1.y1 + 2 x2.y2 - x2.y2^ab."""
+    s1, s2, sx = _dots(x, y)
+    return 2.0 * s1 + 2.0 * s2 - sx
 
 
 def inner_full(x, y):
-    """Sum over ALL spin-orbital elements (orthogonalization's overlap, :466-496)."""
-    (x1, x2), (y1, y2) = x, y
-    dx, dy = x2 - swap_ab(x2), y2 - swap_ab(y2)
-    return 2.0 * float(np.vdot(x1, y1)) + 4.0 * float(np.vdot(x2, y2)) + 2.0 * float(np.vdot(dx, dy))
+    """Sum over ALL spin-orbital elements (orthogonalization's overlap, :466-496):
+    2 x1.y1 + 4 x2.y2 + 2 (x2 - x2^ab).(y2 - y2^ab) = 2 x1.y1 + 8 x2.y2 - 4 x2.y2^ab."""
+    s1, s2, sx = _dots(x, y)
+    return 2.0 * s1 + 8.0 * s2 - 4.0 * sx
 
 
 def pair_symmetric(x2):
@@ -198,6 +204,7 @@ class DeviceSigma:
         self.cc = (engine or api.CoupledCluster)([mol] * (4 * nvec), kw)
         self.cc.initCC()
         self.t1, self.t2, self.h, self.nvec = t1, t2, h, nvec
+        self.calls = 0                                      # engine iterations (one per call)
         self.eps = 10.0 ** (-keywords.accuracy)
         o = t1.shape[0]
         self.signs, self.D1, self.D2 = [], [], []
@@ -230,6 +237,7 @@ class DeviceSigma:
         for k in range(4 * len(vecs), 4 * self.nvec):      # idle copies restart from t every call
             self.cc.set_guess(k, *self._basis(k, self.t1, self.t2))
         self.cc.iterationCC(1, self.eps)
+        self.calls += 1
         out = []
         for q in range(len(vecs)):
             om = []
@@ -389,10 +397,16 @@ def davidson_states(sigma, seeds, nroots, F, kw: api.Keywords, lr: LRKeywords, t
     extend(list(seeds))
     states = [_State(None, kw, lr, t) for t in targets]
     iteration = 0
+    H = np.zeros((0, 0))
     while True:
         iteration += 1
-        m = len(V)
-        H = np.array([[inner(V[i], W[j]) for j in range(m)] for i in range(m)])
+        m, m0 = len(V), H.shape[0]
+        Hn = np.zeros((m, m))                          # projected matrix, new rows and columns only
+        Hn[:m0, :m0] = H
+        for i in range(m):
+            for j in range(m0 if i < m0 else 0, m):
+                Hn[i, j] = inner(V[i], W[j])
+        H = Hn
         theta, Y = np.linalg.eig(H)
         order = np.argsort(theta.real)[:k]
         ritz = []
@@ -424,6 +438,7 @@ def davidson_states(sigma, seeds, nroots, F, kw: api.Keywords, lr: LRKeywords, t
                 corr.append((res[0] / d1, pair_symmetric(res[1] / d2)))
         if len(V) + len(corr) > max_space:             # restart on the Ritz vectors
             V.clear(); W.clear()
+            H = np.zeros((0, 0))
             keep = []
             for (w, x, s, res, acc) in ritz:
                 y = orthonormal(x)
@@ -508,6 +523,8 @@ def linear_response(mol: Molecule, keywords: api.Keywords | None = None, lr: LRK
             states = iterate_states(sig, seeds, kw, lr)
     finally:
         sig.close()
+    out["sigma_calls"] = sig.calls
+    out["engine_copies"] = 4 * sig.nvec
     Ft = F[:o, o:] + np.einsum("iakd,kd->ia", I.L, t1)
     rows = []
     for s in states:
