@@ -69,6 +69,7 @@ _LR_KEYS = {
     ("linear-response", "orthogonalization"): ("orthogonalization", "bool"),
     ("linear-response", "diis-enabled"): ("diis_enabled", "bool"),
     ("linear-response", "diis-steps"): ("diis_steps", "int"),
+    ("linear-response", "store-solution"): ("store_solution", "bool"),
     ("linear-response", "store-solution-threshold"): ("store_solution_threshold", "float"),
     ("linear-response", "store-solution-mode"): ("store_solution_mode", "str"),
 }
@@ -253,7 +254,8 @@ def run_input(source: str, harvest_file: str | None = None, engine=None) -> dict
     if job.jobtype == "polarizability":
         from . import properties
         res, report = properties.polarizability_job(mol, kw, scales=job.components, npoints=job.points,
-                                                    step=job.derive_step, harvest_file=harvest_file if job.harvest else None)
+                                                    step=job.derive_step, harvest_file=harvest_file if job.harvest else None,
+                                                    lr=job.lr, lr_solver=job.lr_solver, engine=engine)
         return {"job": job, "properties": res, "report": report}
     raise ValueError(f"jobtype {job.jobtype!r}: the engine runs energy and polarizability jobs")
 

@@ -79,6 +79,7 @@ class LRKeywords:
     orthogonalization: bool = False     # linear-response:orthogonalization
     diis_enabled: bool = True           # linear-response:diis-enabled
     diis_steps: int = 20                # linear-response:diis-steps
+    store_solution: bool = True         # linear-response:store-solution (seed the next run, e.g. the next field point)
     store_solution_threshold: float = 2  # linear-response:store-solution-threshold (exponent)
     store_solution_mode: str = "r1r2"   # linear-response:store-solution-mode
 
@@ -454,7 +455,7 @@ def davidson_states(sigma, seeds, nroots, F, kw: api.Keywords, lr: LRKeywords, t
 
 
 def linear_response(mol: Molecule, keywords: api.Keywords | None = None, lr: LRKeywords | None = None,
-                    seeds=None, engine=None, solver: str = "reference") -> dict:
+                    seeds=None, seed_orbitals=None, engine=None, solver: str = "reference") -> dict:
     """getEnergy('r-ccsd') with excited states: the r-ccsd ground state, then lr-r-ccsd.
 
     Returns energy (E_CCSD), ccsd status/iterations, the ground state's t1, t2
@@ -462,7 +463,8 @@ def linear_response(mol: Molecule, keywords: api.Keywords | None = None, lr: LRK
     resortStates): omega, E_total = E_CCSD + omega, r0, ael (average
     excitation level), status, iterations, r1, r2 (in the orbitals C).
     ``seeds`` replaces the CIS guess by earlier states (loadSolution): a list
-    of (r1, r2).
+    of (r1, r2), in the orbitals ``seed_orbitals`` when given (their signs are
+    matched to this run's orbitals).
 
     ``solver`` "reference" runs the reference's iteration. Which eigenpair
     each of its states settles on depends on rounding: the damped step with
@@ -503,6 +505,12 @@ def linear_response(mol: Molecule, keywords: api.Keywords | None = None, lr: LRK
         if solver == "davidson":
             davidson_seeds = guess_space(F, I, min(o * v, max(2 * nstates, nstates + 4)))
     seeds = list(seeds)[:nstates]
+    if seed_orbitals is not None:
+        sg = _align(C, seed_orbitals)
+        so, sv = sg[:o], sg[o:]
+        seeds = [(a1 * so[:, None] * sv[None, :],
+                  a2 * so[:, None, None, None] * so[None, :, None, None] * sv[None, None, :, None]
+                  * sv[None, None, None, :]) for a1, a2 in seeds]
     if any(inner(s, s) == 0.0 for s in seeds):
         raise ValueError("a guess vector is empty (no singles reach linear-response:guess-threshold)")
     if solver not in ("reference", "davidson"):

@@ -471,13 +471,52 @@ def read_harvester(path: str) -> list[dict]:
     return out
 
 
+def state_energy_grids(mol: Molecule, keywords: api.Keywords | None = None, lr=None, scales: str = "x",
+                       npoints: int = 5, step: float = 0.02, solver: str = "reference", engine=None):
+    """getPolarizability with excited states (mod_property.f90:426-443): at every grid point the
+    r-ccsd ground state and its LR-CCSD states (getEnergy(method, nStates)), one grid per state
+    0..nStates. With linear-response:store-solution (the default) each point starts from the
+    previous point's states (dumpSolution / loadSolution, mod_lrccsd.f90:593-734), so a state
+    keeps its identity along the grid; the points run one after another for that reason."""
+    from . import lrccsd
+    kw = keywords or api.Keywords()
+    n = lr.excited_states_number
+    grids = [EnergyGrid(npoints, step, scales) for _ in range(n + 1)]
+    seeds = seed_C = None
+    for pt in field_points(scales, npoints):
+        r = lrccsd.linear_response(field_molecule(mol, [p * step for p in pt]), kw, lr, seeds=seeds,
+                                   seed_orbitals=seed_C, engine=engine, solver=solver)
+        grids[0].energies[pt] = r["energy"]
+        grids[0].iterations[pt], grids[0].status[pt] = r["ccsd_iterations"], r["ccsd_status"]
+        for k in range(n):
+            grids[k + 1].energies[pt] = float(r["E_total"][k])
+            grids[k + 1].iterations[pt], grids[k + 1].status[pt] = int(r["iterations"][k]), int(r["status"][k])
+        if lr.store_solution:
+            seeds, seed_C = lrccsd.stored_seeds(r, lr), r["scf"]["C"]
+    return grids
+
+
 def polarizability_job(mol: Molecule, keywords: api.Keywords | None = None, scales: str = "x", npoints: int = 5,
                        step: float = 0.02, seed: bool = True, harvest_file: str | None = None,
-                       method: str = "r-ccsd"):
-    """getPolarizability + showPolarizability (+ the harvester) for one molecule."""
-    grid = energy_grid(mol, keywords, scales, npoints, step, seed)
-    res, report, harvest = show_polarizability(grid, mol, method)
-    if harvest_file:
-        store_harvester(harvest_file, harvester_record(grid, mol, harvest, method))
-    res["grid"] = grid
-    return res, report
+                       method: str = "r-ccsd", lr=None, lr_solver: str = "reference", engine=None):
+    """getPolarizability + showPolarizability (+ the harvester) for one molecule.
+
+    With ``lr`` (LRKeywords with excited_states_number > 0) every state 0..n gets its grid, its
+    report section ("State #k") and its harvester record; ``res["states"]`` holds the results of
+    states 1..n."""
+    if lr is not None and lr.excited_states_number > 0:
+        grids = state_energy_grids(mol, keywords, lr, scales, npoints, step, lr_solver, engine)
+    else:
+        grids = [energy_grid(mol, keywords, scales, npoints, step, seed)]
+    results, reports = [], []
+    for state, grid in enumerate(grids):
+        res, report, harvest = show_polarizability(grid, mol, method, state)
+        if harvest_file:
+            store_harvester(harvest_file, harvester_record(grid, mol, harvest, method, state))
+        res["grid"] = grid
+        results.append(res)
+        reports.append(report)
+    out = results[0]
+    if len(results) > 1:
+        out["states"] = results[1:]
+    return out, "\n".join(reports)

@@ -146,3 +146,29 @@ def test_triplets_and_bad_state_counts_are_refused():
         lrccsd.linear_response(mol, lr=lrccsd.LRKeywords(spin=1), engine=FakeCoupledCluster)
     with pytest.raises(ValueError):
         lrccsd.linear_response(mol, lr=lrccsd.LRKeywords(excited_states_number=0), engine=FakeCoupledCluster)
+
+
+def test_excited_state_polarizability_on_the_fake_engine(tmp_path):
+    from helios_gb300 import properties
+    from oracle.polariz import alpha
+    mol, step = molecules.polyene(4), 0.05
+    kw = api.Keywords(bond_alternation=0.1, accuracy=12)
+    lr = lrccsd.LRKeywords(excited_states_number=2, accuracy=9)
+    path = str(tmp_path / "states.hrv")
+    res, report = properties.polarizability_job(mol, kw, "x", 3, step, harvest_file=path, lr=lr,
+                                                lr_solver="davidson", engine=FakeCoupledCluster)
+    E = {0: [], 1: [], 2: []}
+    for p in (-1, 0, 1):                     # the oracle: E_CCSD and its lowest Jacobian roots per field
+        model = build_model(mol, alternation=0.1, field=(p * step, 0.0, 0.0))
+        scf = rhf(model)
+        F, eref = mo_fock(model, scf["V"], scf["D"])
+        o = model["nel"] // 2
+        out = ccsd_fact.ccsd(F, scf["V"], model["G"], eref, o, eps=1e-12)
+        w = np.sort(np.linalg.eigvals(olr.closed_shell_jacobian(F, scf["V"], model["G"], o, out["t1"], out["t2"])).real)
+        E[0].append(out["energy"][0]); E[1].append(out["energy"][0] + w[0]); E[2].append(out["energy"][0] + w[1])
+    assert res["stencils"][3]["alpha"]["xx"] == pytest.approx(alpha(E[0], step), rel=1e-6)
+    for k in (1, 2):
+        assert res["states"][k - 1]["stencils"][3]["alpha"]["xx"] == pytest.approx(alpha(E[k], step), rel=1e-5)
+    assert "State #1" in report and "State #2" in report
+    recs = properties.read_harvester(path)
+    assert [r["state"] for r in recs] == [0, 1, 2]

@@ -109,3 +109,29 @@ def test_reference_iteration_reproduces_the_oracles_states(lr, mol):
     assert list(got["status"]) == [1, 1, 1] and list(want["status"]) == [1, 1, 1]
     assert np.abs(got["omega"] - want["omega"]).max() < 1e-8
     assert np.abs(got["r0"] - want["r0"]).max() < 1e-7 and np.abs(got["ael"] - want["ael"]).max() < 1e-7
+
+
+def test_excited_state_polarizability(lr):
+    from helios_gb300 import api, properties
+    from oracle import ccsd_fact
+    from oracle import lrccsd as olr
+    from oracle.polariz import alpha
+    from oracle.ppp import build_model
+    from oracle.rhf import mo_fock, rhf
+    mol, step = molecules.polyene(6), 0.05
+    kw = api.Keywords(bond_alternation=0.1, accuracy=12)
+    res, report = properties.polarizability_job(mol, kw, "x", 3, step, lr=lr.LRKeywords(excited_states_number=2,
+                                                accuracy=9), lr_solver="davidson")
+    E = {0: [], 1: [], 2: []}
+    for p in (-1, 0, 1):
+        model = build_model(mol, alternation=0.1, field=(p * step, 0.0, 0.0))
+        scf = rhf(model)
+        F, eref = mo_fock(model, scf["V"], scf["D"])
+        o = model["nel"] // 2
+        out = ccsd_fact.ccsd(F, scf["V"], model["G"], eref, o, eps=1e-12)
+        w = np.sort(np.linalg.eigvals(olr.closed_shell_jacobian(F, scf["V"], model["G"], o, out["t1"], out["t2"])).real)
+        E[0].append(out["energy"][0]); E[1].append(out["energy"][0] + w[0]); E[2].append(out["energy"][0] + w[1])
+    assert res["stencils"][3]["alpha"]["xx"] == pytest.approx(alpha(E[0], step), rel=1e-6)
+    for k in (1, 2):
+        assert res["states"][k - 1]["stencils"][3]["alpha"]["xx"] == pytest.approx(alpha(E[k], step), rel=1e-5)
+    assert "State #2" in report
