@@ -338,6 +338,32 @@ def run_gb300(args):
                                 "r0": [float(x) for x in rl["r0"]], "excitation_level": [float(x) for x in rl["ael"]]}
         except Exception as exc:                      # noqa: BLE001 -- reported in the JSON line
             extra["lr_ccsd"] = {"error": f"{type(exc).__name__}: {exc}"}
+        # the reference's own iteration on dodecahexaene, beside its CPU restatement (the oracle's
+        # spin-orbital equations, numpy, one process) on the same orbitals and amplitudes
+        try:
+            kwd = api.Keywords(bond_alternation=0.1, accuracy=12)
+            lrd = lrccsd.LRKeywords(excited_states_number=3, accuracy=8)
+            t0l = time.perf_counter()
+            rd = lrccsd.linear_response(molecules.dodecahexaene(), kwd, lrd)
+            gpu_s = time.perf_counter() - t0l
+            leg = {"molecule": "dodecahexaene (o = v = 6)", "solver": "reference", "seconds": gpu_s,
+                   "omega_eV": [float(x) for x in rd["omega"]], "iterations": [int(x) for x in rd["iterations"]],
+                   "sigma_calls": rd["sigma_calls"]}
+            if not args.no_cpu:
+                from oracle import lrccsd as olr
+                from oracle.ppp import build_model
+                md = build_model(molecules.dodecahexaene(), alternation=0.1)
+                t0c = time.perf_counter()
+                want = olr.lr_solve(rd["scf"]["C"], md["G"], md["core"], rd["scf"]["F"], rd["t1"].shape[0],
+                                    rd["t1"], rd["t2"], nstates=3, eps=1e-8)
+                leg["cpu_baseline"] = {"seconds": time.perf_counter() - t0c, "kind": "port", "cores": 1,
+                                       "sample": "the reference's spin-orbital LR iteration restated in numpy "
+                                                 "(oracle/lrccsd.py), same orbitals and amplitudes",
+                                       "omega_eV": [float(x) for x in want["omega"]],
+                                       "iterations": [int(x) for x in want["iterations"]]}
+            extra["lr_ccsd_reference_iteration"] = leg
+        except Exception as exc:                      # noqa: BLE001 -- reported in the JSON line
+            extra["lr_ccsd_reference_iteration"] = {"error": f"{type(exc).__name__}: {exc}"}
     # --- end to end through the C ABI with host buffers
     e2e = run_e2e(api, mol, kw, max(1, min(args.steps, 3)))
     # --- roofline of the tcgen05 GEMM, live over the timed steps
