@@ -156,12 +156,19 @@ class MOIntegrals:
         self.L = 2.0 * self.J - self.J.transpose(0, 3, 2, 1)                     # 2(ia|jb) - (ib|ja)
 
 
-def guess_vectors(F, I: MOIntegrals, nstates, kind="cis", threshold=0.1):
-    """prepareGuess + guessState: per state the singles (i, a, c) with |c| >= threshold, and the roots."""
+def cis_matrix(F, I: MOIntegrals):
+    """A(ia, jb) = 2(ai|jb) - (ab|ji) + delta (e_a - e_i) (prepareGuess, mod_lrccsd.f90:1262-1276)."""
     o, v = I.J.shape[0], I.J.shape[1]
     e = np.diag(F)
     A = (2.0 * I.J - I.Kvo).reshape(o * v, o * v)
     A[np.diag_indices_from(A)] += (e[None, o:] - e[:o, None]).ravel()
+    return A
+
+
+def guess_vectors(F, I: MOIntegrals, nstates, kind="cis", threshold=0.1):
+    """prepareGuess + guessState: per state the singles (i, a, c) with |c| >= threshold, and the roots."""
+    o, v = I.J.shape[0], I.J.shape[1]
+    A = cis_matrix(F, I)
     if kind == "cis":
         w, U = np.linalg.eigh(A)
     elif kind == "rpa":
@@ -179,10 +186,7 @@ def guess_vectors(F, I: MOIntegrals, nstates, kind="cis", threshold=0.1):
 def guess_space(F, I: MOIntegrals, n):
     """The n lowest CIS vectors, whole, as (r1, 0) (the Davidson solver's first basis)."""
     o, v = I.J.shape[0], I.J.shape[1]
-    e = np.diag(F)
-    A = (2.0 * I.J - I.Kvo).reshape(o * v, o * v)
-    A[np.diag_indices_from(A)] += (e[None, o:] - e[:o, None]).ravel()
-    _, U = np.linalg.eigh(A)
+    _, U = np.linalg.eigh(cis_matrix(F, I))
     return [(U[:, k].reshape(o, v).copy(), np.zeros((o, o, v, v))) for k in range(n)]
 
 
