@@ -123,7 +123,9 @@ def test_reference_iteration_reproduces_the_oracles_states(lr, mol):
                         nstates=3, eps=1e-8)
     assert list(got["status"]) == [1, 1, 1] and list(want["status"]) == [1, 1, 1]
     assert np.abs(got["omega"] - want["omega"]).max() < 1e-8
-    assert np.abs(got["r0"] - want["r0"]).max() < 1e-7 and np.abs(got["ael"] - want["ael"]).max() < 1e-7
+    # r0 follows the sign of the eigenvector, which the guess fixes; compare magnitudes
+    assert np.abs(np.abs(got["r0"]) - np.abs(want["r0"])).max() < 1e-7
+    assert np.abs(got["ael"] - want["ael"]).max() < 1e-7
 
 
 def test_excited_state_polarizability(lr):
