@@ -13,6 +13,7 @@ import pytest
 from helios_gb300 import molecules
 
 pytestmark = pytest.mark.gpu
+_LR = {"accuracy": 8, "max_iterations": 3000}        # LR targets 1e-8 * 2^k; a bound on the run time
 
 
 @pytest.fixture(scope="module")
@@ -76,7 +77,7 @@ def test_states_are_eigenpairs_of_the_reference_equations(lr, mol, solver):
     from oracle.ppp import build_model
     from oracle.triples import spin_amplitudes
     kw = api.Keywords(bond_alternation=0.1, accuracy=12)
-    got = lr.linear_response(mol, kw, lr.LRKeywords(excited_states_number=3, accuracy=8, max_iterations=3000), solver=solver)
+    got = lr.linear_response(mol, kw, lr.LRKeywords(**_LR, excited_states_number=3), solver=solver)
     assert got["ccsd_status"] == 1 and list(got["status"]) == [1, 1, 1]
     model = build_model(mol, alternation=0.1)
     C, F, t1, t2 = got["scf"]["C"], got["scf"]["F"], got["t1"], got["t2"]
@@ -100,9 +101,9 @@ def test_input_file_energy_job_with_states(lr):
     from helios_gb300 import api, inputfile
     mol = molecules.polyene(6)
     kw = api.Keywords(bond_alternation=0.1, accuracy=12)
-    job = inputfile.Job(lr=lr.LRKeywords(excited_states_number=2, accuracy=8, max_iterations=3000), lr_solver="davidson")
+    job = inputfile.Job(lr=lr.LRKeywords(**_LR, excited_states_number=2), lr_solver="davidson")
     r = inputfile.run_input(inputfile.write_input(mol, kw, job))
-    want = lr.linear_response(mol, kw, lr.LRKeywords(excited_states_number=2, accuracy=8, max_iterations=3000), solver="davidson")
+    want = lr.linear_response(mol, kw, lr.LRKeywords(**_LR, excited_states_number=2), solver="davidson")
     assert r["status"] == 1 and list(r["excited"]["status"]) == [1, 1]
     assert np.abs(r["excited"]["omega"] - want["omega"]).max() < 1e-9
     assert np.allclose(r["excited"]["E_total"], r["energy"][0] + r["excited"]["omega"])
@@ -116,7 +117,7 @@ def test_reference_iteration_reproduces_the_oracles_states(lr, mol):
     from oracle import lrccsd as olr
     from oracle.ppp import build_model
     kw = api.Keywords(bond_alternation=0.1, accuracy=12)
-    got = lr.linear_response(mol, kw, lr.LRKeywords(excited_states_number=3, accuracy=8, max_iterations=3000))
+    got = lr.linear_response(mol, kw, lr.LRKeywords(**_LR, excited_states_number=3))
     model = build_model(mol, alternation=0.1)
     o = got["t1"].shape[0]
     want = olr.lr_solve(got["scf"]["C"], model["G"], model["core"], got["scf"]["F"], o, got["t1"], got["t2"],
