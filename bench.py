@@ -11,8 +11,9 @@ stop rule: that residual < 1e-7).
 value = polyene solves per second over all ranks (replicas: every rank solves
 its own polyene, no device collective). The same line carries the plain FP64
 GPU path's time to 1e-6 eV on the same molecule, the 512-molecule ensemble
-throughput (mixed and plain FP64), the 64-site ladder's polarizability and
-(T) correction, the roofline of the dominant kernel (the tcgen05 GEMM, timed live
+throughput (mixed and plain FP64), the 64-site ladder's polarizability, (T)
+correction and lowest LR-CCSD excited states, the reference's LR iteration on
+dodecahexaene beside its CPU restatement, the roofline of the dominant kernel (the tcgen05 GEMM, timed live
 with CUDA events during the timed steps), the end-to-end number through the
 C ABI with host buffers, the SM clocks seen during the timed region and a CPU
 baseline (the factorised FP64 oracle, one sampled residual on the host cores).
