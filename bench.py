@@ -343,7 +343,7 @@ def run_gb300(args):
         # spin-orbital equations, numpy, one process) on the same orbitals and amplitudes
         try:
             kwd = api.Keywords(bond_alternation=0.1, accuracy=12)
-            lrd = lrccsd.LRKeywords(excited_states_number=3, accuracy=8)
+            lrd = lrccsd.LRKeywords(excited_states_number=3, accuracy=8, max_iterations=2000)
             t0l = time.perf_counter()
             rd = lrccsd.linear_response(molecules.dodecahexaene(), kwd, lrd)
             gpu_s = time.perf_counter() - t0l
