@@ -356,7 +356,7 @@ def run_gb300(args):
                 md = build_model(molecules.dodecahexaene(), alternation=0.1)
                 t0c = time.perf_counter()
                 want = olr.lr_solve(rd["scf"]["C"], md["G"], md["core"], rd["scf"]["F"], rd["t1"].shape[0],
-                                    rd["t1"], rd["t2"], nstates=3, eps=1e-8)
+                                    rd["t1"], rd["t2"], nstates=3, eps=1e-8, maxiter=2000)
                 leg["cpu_baseline"] = {"seconds": time.perf_counter() - t0c, "kind": "port", "cores": 1,
                                        "sample": "the reference's spin-orbital LR iteration restated in numpy "
                                                  "(oracle/lrccsd.py), same orbitals and amplitudes",
