@@ -250,6 +250,7 @@ def run_gb300(args):
     if args.batch > 0:
         mols = molecules.ensemble(learned.HELD_OUT_SEED, args.batch)
         extra["batch"] = {"molecules": args.batch, "seeds": [learned.HELD_OUT_SEED, learned.HELD_OUT_SEED + args.batch - 1]}
+        e_mixed = {}
         for g in (["learned", "reference"] if guess == "learned" else ["reference"]):
             cb = api.CoupledCluster(mols, api.Keywords(bond_alternation=0.1, accuracy=8, precision="mixed", guess=g))
             # warm-up solve with live GEMM timing: tensor-core work issued by the batch
@@ -263,6 +264,7 @@ def run_gb300(args):
             tb = cb.timing()
             cb.finalizeCC()
             secs = (tb["init_ms"] + tb["solve_ms"]) / 1e3
+            e_mixed[g] = (out["energy"][:, 0].copy(), out["status"].copy())
             peak_t = (peaks[1] or peaks[0]) * 1e12
             wsecs = (tw["init_ms"] + tw["solve_ms"]) / 1e3
             extra["batch"][g + "_guess"] = {
@@ -287,6 +289,11 @@ def run_gb300(args):
                                             "mean_iterations": float(o64["iterations"].mean())}
             best = extra["batch"].get("learned_guess", extra["batch"].get("reference_guess"))
             extra["batch"]["speedup_mixed_vs_fp64"] = s64 / best["seconds"]
+            # every member's mixed energy against its plain FP64 energy (both at residual 1e-8)
+            for g, (em, sm) in e_mixed.items():
+                both = (sm == 1) & (o64["status"] == 1)
+                extra["batch"][g + "_guess"]["max_abs_dE_mixed_vs_fp64_eV"] = (
+                    float(abs(em[both] - o64["energy"][both, 0]).max()) if both.any() else None)
     # --- finite-field alpha_xx of the 2 x 32 ladder: five field points solved as one batch
     if args.polariz:
         from helios_gb300 import polariz

@@ -1152,7 +1152,9 @@ std::mutex g_na_mutex;
 unsigned char *g_na_base[NA_MAX_DEVICES] = {};
 
 // Address of the static scratch on the current device, looked up once per
-// device (the first call on a device must not be inside a stream capture).
+// device (the first call on a device must not be inside a stream capture) and
+// kept for the life of the library: a device reset while it is loaded would
+// leave a stale address, and is not supported.
 int na_setup(unsigned char **base)
 {
     int dev = 0;
@@ -1196,10 +1198,17 @@ extern "C" int hx_gemm_noalloc(const double *dA, const double *dB, double *dC, i
         hx_set_error("hx_gemm_noalloc: precision must be 1 (3 slices) or 2 (5 slices)");
         return HX_ERR_ARG;
     }
+    cudaStream_t s = (cudaStream_t)stream;
+    // the call ends with a read-back and a stream synchronisation, neither of
+    // which a capture may record: refuse before touching the stream
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+        hx_set_error("hx_gemm_noalloc: the stream is being captured (the call synchronises its stream)");
+        return HX_ERR_ARG;
+    }
     unsigned char *base = nullptr;
     int rc = na_setup(&base);
     if (rc != HX_OK) return rc;
-    cudaStream_t s = (cudaStream_t)stream;
     const bool high = precision == 2;
     const int S = high ? High::S : Low::S, BN = high ? High::BN : Low::BN;
 

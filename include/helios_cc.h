@@ -253,13 +253,17 @@ int hx_gemm(const double *A, const double *B, double *C, int32_t M, int32_t N, i
  * allocator: the operand slices, row exponents, error word and descriptors
  * live in one static device array of about 6.4 MB, whose address is looked
  * up once per device (cudaGetSymbolAddress) on the first call; make that
- * first call before any stream capture. Dimensions above
- * HX_NOALLOC_MAX_DIM return HX_ERR_ARG. C is zeroed and accumulated on
- * `stream` (a cudaStream_t; NULL = the legacy default stream), and the call
- * returns after the stream has synchronised. Results equal hx_gemm's bit for
- * bit wherever hx_gemm uses the tensor cores (M*N*K >= 4e6). The scratch is
- * shared: calls that overlap in time, on any streams or host threads, race
- * and corrupt each other's results. */
+ * first call before any stream capture. The address is kept for the life of
+ * the library, so a device reset (cudaDeviceReset) while the library is
+ * loaded is not supported. Dimensions above HX_NOALLOC_MAX_DIM return
+ * HX_ERR_ARG. C is zeroed and accumulated on `stream` (a cudaStream_t;
+ * NULL = the legacy default stream), and the call returns after the stream
+ * has synchronised: it reads the kernel's error word back, so a call on a
+ * stream that is being captured returns HX_ERR_ARG and leaves the capture
+ * untouched. Results equal hx_gemm's bit for bit wherever hx_gemm uses the
+ * tensor cores (M*N*K >= 1e4). The scratch is shared: calls that overlap in
+ * time, on any streams or host threads, race and corrupt each other's
+ * results. */
 #define HX_NOALLOC_MAX_DIM 512
 int hx_gemm_noalloc(const double *A, const double *B, double *C, int32_t M, int32_t N, int32_t K,
                     int32_t precision, void *stream);

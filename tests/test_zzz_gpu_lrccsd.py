@@ -69,8 +69,8 @@ def _spectrum(name, F, C, G, o, t1, t2):
 
 @pytest.mark.parametrize("solver", ["reference", "davidson"])
 @pytest.mark.parametrize("mol", [molecules.polyene(4), molecules.polyene(6), molecules.dodecahexaene(),
-                                 molecules.random_molecule(7, 6, 8)],
-                         ids=["butadiene", "hexatriene", "dodecahexaene", "rnd7"])
+                                 molecules.random_molecule(7, 6, 8), molecules.ladder(8)],
+                         ids=["butadiene", "hexatriene", "dodecahexaene", "rnd7", "ladder-8"])
 def test_states_are_eigenpairs_of_the_reference_equations(lr, mol, solver):
     from helios_gb300 import api
     from oracle import lrccsd as olr
@@ -109,10 +109,13 @@ def test_input_file_energy_job_with_states(lr):
     assert np.allclose(r["excited"]["E_total"], r["energy"][0] + r["excited"]["omega"])
 
 
-@pytest.mark.parametrize("mol", [molecules.dodecahexaene(), molecules.ladder(8)], ids=["dodecahexaene", "ladder-8"])
+@pytest.mark.parametrize("mol", [molecules.dodecahexaene()], ids=["dodecahexaene"])
 def test_reference_iteration_reproduces_the_oracles_states(lr, mol):
-    # on these molecules the reference's iteration ends on the same three states whatever the
-    # rounding (measured on the oracle with noise up to 1e-11 added to every sigma vector)
+    # on dodecahexaene the reference's iteration ends on the same three states whatever the
+    # rounding (the oracle with noise up to 1e-9 added to every sigma vector, on x86 and Arm).
+    # The 2 x 4 ladder is not such a molecule: the oracle itself ends on 3.880/4.039/5.591 eV
+    # from x86 orbitals and on 4.039/5.591/5.667 eV from the GPU's, so its reference-iteration
+    # states are checked one by one (test_states_are_eigenpairs_of_the_reference_equations)
     from helios_gb300 import api
     from oracle import lrccsd as olr
     from oracle.ppp import build_model
