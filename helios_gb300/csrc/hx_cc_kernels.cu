@@ -169,11 +169,15 @@ __global__ void k_assemble(const CCMol *mols, const int *active)
 }
 
 // ---------------------------------------------------------------- step
-// d1 = r1, d2 = 2 r2(ijab) - r2(ijba); t1 += s1 d1/D1; t2 += 3 s2 r2/D2.
-// Writes the new amplitudes and the DIIS error vector (d1, 3 r2) into the
-// history slot `slot`, and per-block maxima of |d1|, |d2| into part.
+// d1 = r1, d2 = 2 r2(ijab) - r2(ijba); t1 += s1 d1/D1 and, by the projection
+// type of stepCC (mod_cc.f90:1007-1008),
+//   "2-1" (proj 2): t2 += s2 (2 d2(ijab) + d2(ijba))/D2 = 3 s2 r2/D2,
+//   "1"   (proj 1): t2 += s2 d2(ijab)/D2.
+// Writes the new amplitudes and the DIIS error vector (d1, 3 r2 or d2, as
+// pushCCVectors :1417-1420) into the history slot `slot`, and per-block
+// maxima of |d1|, |d2| into part.
 __global__ void k_step(const CCMol *mols, const DiisMol *diis, const int *active, double s1, double s2,
-                       int use_diis, double *part, int nblk)
+                       int use_diis, int proj, double *part, int nblk)
 {
     if (skip(active)) return;
     const CCMol &m = mols[blockIdx.y];
@@ -205,9 +209,10 @@ __global__ void k_step(const CCMol *mols, const DiisMol *diis, const int *active
             double w = m.r2[min(p1, q1) * ov + max(p1, q1)];
             double d2 = 2.0 * w - m.r2[min(p2, q2) * ov + max(p2, q2)];
             mx2 = fmax(mx2, fabs(d2));
-            double t = m.t2[f] + 3.0 * s2 * w / m.D2[f];
+            const double g = proj == 1 ? d2 : 3.0 * w;
+            double t = m.t2[f] + s2 * g / m.D2[f];
             m.t2[f] = t;
-            if (Ht) { Ht[e] = t; He[e] = 3.0 * w; }
+            if (Ht) { Ht[e] = t; He[e] = g; }
         }
     }
     double r1 = block_red(mx1, true);
@@ -495,9 +500,9 @@ cudaError_t hx_ew_setup2(const CCMol *m, const int *act, int nmol, long long max
 }
 
 cudaError_t hx_step(const CCMol *m, const DiisMol *h, const int *act, int nmol, double s1, double s2,
-                    int use_diis, double *part, int nblk, cudaStream_t s)
+                    int use_diis, int proj, double *part, int nblk, cudaStream_t s)
 {
-    k_step<<<dim3(nblk, nmol), NT, 0, s>>>(m, h, act, s1, s2, use_diis, part, nblk);
+    k_step<<<dim3(nblk, nmol), NT, 0, s>>>(m, h, act, s1, s2, use_diis, proj, part, nblk);
     hx_count_launches(2);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;

@@ -765,7 +765,8 @@ static int iteration_body(hx_ccsd *h, double eps)
     HX_TRY(run_group(h, P[k++]));                                    // r1 += Vs Xv
     HX_TRY(run_group(h, P[k++]));                                    // r1 -= Boo UG
     const int use_diis = h->p.diis_enabled ? 1 : 0;
-    HX_CU(hx_step(h->d_cc, h->d_diis, h->d_active, nm, h->p.t1_step, h->p.t2_step, use_diis, h->d_part, h->nblk, h->st));
+    HX_CU(hx_step(h->d_cc, h->d_diis, h->d_active, nm, h->p.t1_step, h->p.t2_step, use_diis, h->p.projection_type,
+                  h->d_part, h->nblk, h->st));
     if (use_diis) HX_CU(hx_diis(h->d_cc, h->d_diis, h->d_active, nm, h->d_gate, h->d_part, h->nblk, h->p.diis_steps, h->st));
     HX_CU(hx_energy(h->d_cc, h->d_active, nm, h->d_part, h->nblk, h->st));
     return HX_OK;
@@ -781,7 +782,6 @@ static int fetch_results(hx_ccsd *h)
 int hx_ccsd_iterate(hx_ccsd *h, int32_t iteration, double eps, double acc[5])
 {
     if (!h || !h->initialized) { hx_set_error("hx_ccsd_iterate before hx_ccsd_init"); return HX_ERR_STATE; }
-    if (h->p.projection_type != 2) { hx_set_error("projection-type 1 is not built on the GPU path"); return HX_ERR_UNSUPPORTED; }
     (void)iteration;
     HX_TRY(iteration_body(h, eps));
     HX_TRY(fetch_results(h));
@@ -869,7 +869,6 @@ static const int kMaxFp64Returns = 3;
 
 static int solve_all(hx_ccsd *h, int maxiter, double eps)
 {
-    if (h->p.projection_type != 2) { hx_set_error("projection-type 1 is not built on the GPU path"); return HX_ERR_UNSUPPORTED; }
     const bool mixed = h->tce != nullptr;
     const int check_ph = h->p.mixed_check == 1 ? PH_FP64 : PH_EXACT;
     int remaining = 0;

@@ -20,7 +20,7 @@ cudaError_t hx_ew_assemble(const CCMol *m, const int *act, int nmol, long long m
 cudaError_t hx_ew_setup(const CCMol *m, const int *act, int nmol, long long maxw, int guess, cudaStream_t s);
 cudaError_t hx_ew_setup2(const CCMol *m, const int *act, int nmol, long long maxw, int guess, cudaStream_t s);
 cudaError_t hx_step(const CCMol *m, const DiisMol *h, const int *act, int nmol, double s1, double s2,
-                    int use_diis, double *part, int nblk, cudaStream_t s);
+                    int use_diis, int proj, double *part, int nblk, cudaStream_t s);
 cudaError_t hx_diis(const CCMol *m, const DiisMol *h, const int *act, int nmol, const double *gate, double *part,
                     int nblk, int nd_max, cudaStream_t s);
 cudaError_t hx_energy(const CCMol *m, const int *act, int nmol, double *part, int nblk, cudaStream_t s);

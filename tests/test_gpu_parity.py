@@ -89,6 +89,20 @@ def test_other_coulomb_models(api, coulomb):
     assert abs(out["ecorr"] - ref["ecorr"]) < 1e-8
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_projection_type_1_matches_literal_oracle(api, precision):
+    # coupled-cluster:projection-type = 1: stepCC divides d2(ijab) itself by the
+    # denominator and DIIS mixes d2 (mod_cc.f90:1007, :1417); same fixed point as "2-1"
+    from oracle.literal import solve_literal
+    for mol in (molecules.dodecahexaene(), molecules.random_molecule(11, 8, 14)):
+        ref = solve_literal(mol, alternation=0.1, eps=1e-10, projtype=1)
+        out = api.get_energy(mol, _kw(api, projection_type="1", precision=precision))
+        assert ref["status"] == 1 and out["status"] == 1
+        assert abs(out["ecorr"] - ref["ecorr"]) < (1e-8 if precision == "fp64" else 1e-6)
+        if precision == "fp64":
+            assert abs(out["iterations"] - ref["iterations"]) <= 1
+
+
 def test_batch_matches_individual_oracle(api):
     from oracle.literal import solve_literal
     mols = [molecules.random_molecule(s, 8, 14) for s in (11, 12, 13, 14, 15)] + [molecules.polyene(4)]
