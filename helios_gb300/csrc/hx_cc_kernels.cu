@@ -1,20 +1,31 @@
 // Elementwise, reduction and DIIS kernels of the CCSD iteration (FP64, HBM bound).
 //
-// All kernels are grouped over the molecules of a batch: blockIdx.y selects
-// the molecule, blockIdx.x strides over its elements, and molecules whose
-// `active` flag is 0 return at once. Reductions are two-pass (fixed per-block
-// partials, then an ordered sum), so repeated runs are bitwise identical.
+// All kernels are grouped over the molecules of a batch with a balanced
+// schedule (HxSched, hx_plan.h): every molecule owns a run of blocks in
+// proportion to its work, a block finds its molecule by binary search over
+// the prefix sums, and blocks of molecules whose `active` flag is 0 return at
+// once. Reductions are two-pass (fixed per-block partials, then an ordered
+// sum per molecule), so repeated runs are bitwise identical.
+//
+// The amplitude tail of an iteration (stepCC, pushCCVectors, diisDotProduct,
+// newCCVectors and energyCC; mod_cc.f90:987-1017, 1390-1423, 1514-1555,
+// 2133-2193, 1916-1952) works on "pair units": v x v blocks [a][b] of the
+// pair matrix for occupied pairs (i, j), staged in shared memory so that the
+// (a, b) transposes the equations need are read and written coalesced.
+//   k_step_push   residual assembly (r2 + X2 + X2 pair-transposed), the
+//                 Jacobi step, the push into the DIIS ring and the dots of
+//                 the new error vector with every stored one, per unit;
+//   k_diis_solve  per molecule: maxima, Gram row, bordered solve;
+//   k_extrapolate t = sum c_k t_k written to both halves of t2, and the
+//                 energy partials of the result.
+// Only the canonical blocks i <= j are stepped and stored, as the reference
+// stores only the pairs (ia) <= (jb).
 #include "hx_common.cuh"
 #include "hx_plan.h"
 #include "hx_kernels.h"
 
 namespace {
 constexpr int NT = 256;
-
-__device__ __forceinline__ bool skip(const int *active) { return active && !active[blockIdx.y]; }
-
-#define GRID_LOOP(i, n) for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < (n); \
-                             i += (long long)gridDim.x * blockDim.x)
 
 __device__ double warp_sum(double v)
 {
@@ -26,7 +37,8 @@ __device__ double warp_max(double v)
     for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
 }
-// block-wide reduction (sum or max) of blockDim.x == NT threads
+// block-wide reduction (sum or max) of blockDim.x == NT threads; the result is
+// valid in thread 0 and the shared scratch may be reused after the call
 __device__ double block_red(double v, bool mx)
 {
     __shared__ double sh[NT / 32];
@@ -37,26 +49,44 @@ __device__ double block_red(double v, bool mx)
     __syncthreads();
     v = (threadIdx.x < NT / 32) ? sh[threadIdx.x] : 0.0;
     if (w == 0) v = mx ? warp_max(v) : warp_sum(v);
-    return v;   // valid in thread 0
+    return v;
 }
+
+// molecule of block b: the last m with start[m] <= b
+__device__ __forceinline__ int sched_mol(const int *__restrict__ start, int nmol, int b)
+{
+    int lo = 0, hi = nmol - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (start[mid] <= b) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Element-wise kernels: block b of molecule mol covers HX_EW_CHUNK elements.
+#define EW_PROLOGUE                                                                      \
+    const int mol_ = sched_mol(start, nmol, blockIdx.x);                                 \
+    if (active && !active[mol_]) return;                                                 \
+    const CCMol &m = mols[mol_];                                                         \
+    const long long base_ = (long long)(blockIdx.x - start[mol_]) * HX_EW_CHUNK;
+#define EW_LOOP(e, n)                                                                    \
+    for (long long e = base_ + threadIdx.x, end_ = min(base_ + HX_EW_CHUNK, (long long)(n)); e < end_; e += NT)
+#define EW_ARGS const CCMol *__restrict__ mols, const int *__restrict__ active, const int *__restrict__ start, int nmol
 
 // ---------------------------------------------------------------- dressing
 // X = [Co | Cv], Y = [Co | Cv]; the t1 corrections are added by GEMMs.
-__global__ void k_dress_init(const CCMol *mols, const int *active)
+__global__ void k_dress_init(EW_ARGS)
 {
-    if (skip(active)) return;
-    const CCMol &m = mols[blockIdx.y];
-    const long long nn = (long long)m.N * m.N;
-    GRID_LOOP(e, nn) { m.X[e] = m.Cmo[e]; m.Y[e] = m.Cmo[e]; }
+    EW_PROLOGUE
+    EW_LOOP(e, (long long)m.N * m.N) { m.X[e] = m.Cmo[e]; m.Y[e] = m.Cmo[e]; }
 }
 
 // H2 = h - G o Pm + 2 diag(G diag Pm), Pm = Yo Xo^T (dressed half density)
-__global__ void k_dress_fock(const CCMol *mols, const int *active)
+__global__ void k_dress_fock(EW_ARGS)
 {
-    if (skip(active)) return;
-    const CCMol &m = mols[blockIdx.y];
+    EW_PROLOGUE
     const int n = m.N;
-    GRID_LOOP(e, (long long)n * n) {
+    EW_LOOP(e, (long long)n * n) {
         int i = (int)(e / n), j = (int)(e % n);
         double f = m.h[e] - m.G[e] * m.Pm[e];
         if (i == j) {
@@ -69,13 +99,12 @@ __global__ void k_dress_fock(const CCMol *mols, const int *active)
 }
 
 // ZDO pair products of the dressed factors.
-__global__ void k_zdo_products(const CCMol *mols, const int *active)
+__global__ void k_zdo_products(EW_ARGS)
 {
-    if (skip(active)) return;
-    const CCMol &m = mols[blockIdx.y];
+    EW_PROLOGUE
     const int n = m.N, o = m.o, v = m.v;
     const long long nia = (long long)n * o * v, noo = (long long)n * o * o, nvv = (long long)n * v * v;
-    GRID_LOOP(e, nia + noo + nvv) {
+    EW_LOOP(e, nia + noo + nvv) {
         if (e < nia) {
             int mu = (int)(e / (o * v)), r = (int)(e % (o * v)), i = r / v, a = r % v;
             m.Bia[e] = m.X[mu * n + o + a] * m.Y[mu * n + i];
@@ -91,29 +120,12 @@ __global__ void k_zdo_products(const CCMol *mols, const int *active)
     }
 }
 
-// u[i][a][j][b] = 2 t[i][a][j][b] - t[i][b][j][a]
-__global__ void k_make_u(const CCMol *mols, const int *active)
-{
-    if (skip(active)) return;
-    const CCMol &m = mols[blockIdx.y];
-    const int o = m.o, v = m.v;
-    GRID_LOOP(e, (long long)o * v * o * v) {
-        int b = (int)(e % v);
-        long long r = e / v;
-        int j = (int)(r % o); r /= o;
-        int a = (int)(r % v);
-        int i = (int)(r / v);
-        m.u[e] = 2.0 * m.t2[e] - m.t2[(((long long)i * v + b) * o + j) * v + a];
-    }
-}
-
 // Ts[i][mu][j][nu] *= G[mu][nu]
-__global__ void k_gamma_scale(const CCMol *mols, const int *active)
+__global__ void k_gamma_scale(EW_ARGS)
 {
-    if (skip(active)) return;
-    const CCMol &m = mols[blockIdx.y];
+    EW_PROLOGUE
     const int n = m.N, o = m.o;
-    GRID_LOOP(e, (long long)o * n * o * n) {
+    EW_LOOP(e, (long long)o * n * o * n) {
         int nu = (int)(e % n);
         int mu = (int)((e / ((long long)n * o)) % n);
         m.Ts[e] *= m.G[mu * n + nu];
@@ -121,12 +133,11 @@ __global__ void k_gamma_scale(const CCMol *mols, const int *active)
 }
 
 // r1[i][a] = Fd[o+a][i];  Fvv2 = Fd_vv;  Foo2 = Fd_oo
-__global__ void k_fock_blocks(const CCMol *mols, const int *active)
+__global__ void k_fock_blocks(EW_ARGS)
 {
-    if (skip(active)) return;
-    const CCMol &m = mols[blockIdx.y];
+    EW_PROLOGUE
     const int n = m.N, o = m.o, v = m.v;
-    GRID_LOOP(e, (long long)o * v + v * v + o * o) {
+    EW_LOOP(e, (long long)o * v + v * v + o * o) {
         if (e < o * v) {
             int i = (int)(e / v), a = (int)(e % v);
             m.r1[e] = m.Fd[(o + a) * n + i];
@@ -140,13 +151,12 @@ __global__ void k_fock_blocks(const CCMol *mols, const int *active)
     }
 }
 
-// X2[i][a][j][b] = 0.5 Cp[i][a][j][b] + Cp[j][a][i][b]
-__global__ void k_c_combine(const CCMol *mols, const int *active)
+// X2[i][a][j][b] = 0.5 Cp[i][a][j][b] + Cp[j][a][i][b]  (consecutive b read consecutively)
+__global__ void k_c_combine(EW_ARGS)
 {
-    if (skip(active)) return;
-    const CCMol &m = mols[blockIdx.y];
+    EW_PROLOGUE
     const int o = m.o, v = m.v;
-    GRID_LOOP(e, (long long)o * v * o * v) {
+    EW_LOOP(e, (long long)o * v * o * v) {
         int b = (int)(e % v);
         long long r = e / v;
         int j = (int)(r % o); r /= o;
@@ -156,148 +166,256 @@ __global__ void k_c_combine(const CCMol *mols, const int *active)
     }
 }
 
-// r2 += X2 + X2^T (pair transpose)
-__global__ void k_assemble(const CCMol *mols, const int *active)
+// ---------------------------------------------------------------- pair units
+// Units of one molecule: unit 0 is the singles; unit u >= 1 holds the v x v
+// blocks [(u-1) g, min(u g, nb)) of the occupied pairs (i, j), in row-major
+// order of the upper triangle i <= j (SK_UP) or of the whole o x o grid
+// (SK_FULL), g = hx_unit_blocks(v). A unit's blocks sit in shared memory as
+// [block][a][b] with rows padded to v + 1 (transposed reads spread over banks).
+struct Unit {
+    int mol, u, k0, nb;   // molecule, unit, first block, blocks in this unit
+};
+
+// (i, j) of block k of the upper triangle (row i starts at i o - i (i - 1) / 2)
+__device__ __forceinline__ void up_block(int k, int o, int &i, int &j)
 {
-    if (skip(active)) return;
-    const CCMol &m = mols[blockIdx.y];
-    const long long ov = (long long)m.o * m.v;
-    GRID_LOOP(e, ov * ov) {
-        long long p = e / ov, q = e % ov;
-        m.r2[e] += m.X2[e] + m.X2[q * ov + p];
+    const double s = 2.0 * o + 1.0;
+    int r = (int)((s - sqrt(s * s - 8.0 * k)) * 0.5);
+    r = r < 0 ? 0 : (r > o - 1 ? o - 1 : r);
+    while (r > 0 && r * o - r * (r - 1) / 2 > k) --r;
+    while (r + 1 < o && (r + 1) * o - (r + 1) * r / 2 <= k) ++r;
+    i = r;
+    j = r + (k - (r * o - r * (r - 1) / 2));
+}
+
+// This block's unit, and the (i, j) of its pair blocks in bi/bj (shared).
+__device__ __forceinline__ Unit unit_of(const CCMol *mols, const int *start, int nmol, bool upper, int *bi, int *bj)
+{
+    Unit w;
+    w.mol = sched_mol(start, nmol, blockIdx.x);
+    w.u = blockIdx.x - start[w.mol];
+    const CCMol &m = mols[w.mol];
+    const int g = hx_unit_blocks(m.v);
+    const int nbt = upper ? m.o * (m.o + 1) / 2 : m.o * m.o;
+    w.k0 = w.u > 0 ? (w.u - 1) * g : 0;
+    w.nb = w.u > 0 ? min(g, nbt - w.k0) : 0;
+    for (int lb = threadIdx.x; lb < w.nb; lb += blockDim.x) {
+        int i, j;
+        if (upper) up_block(w.k0 + lb, m.o, i, j);
+        else { i = (w.k0 + lb) / m.o; j = (w.k0 + lb) % m.o; }
+        bi[lb] = i;
+        bj[lb] = j;
+    }
+    __syncthreads();
+    return w;
+}
+
+// element e of a unit -> block lb, row a, column b; padded shared-memory index
+struct Elem {
+    int lb, a, b, s;
+};
+__device__ __forceinline__ Elem elem(int e, int v)
+{
+    Elem x;
+    const int vv = v * v;
+    x.lb = e / vv;
+    const int r = e - x.lb * vv;
+    x.a = r / v;
+    x.b = r - x.a * v;
+    x.s = (x.lb * v + x.a) * (v + 1) + x.b;
+    return x;
+}
+__device__ __forceinline__ long long pair_off(int i, int a, int j, int b, int o, int v)
+{
+    return (((long long)i * v + a) * o + j) * v + b;
+}
+
+// u[i][a][j][b] = 2 t[i][a][j][b] - t[i][b][j][a]  (SK_FULL units)
+__global__ void __launch_bounds__(NT) k_make_u(const CCMol *__restrict__ mols, const int *__restrict__ active,
+                                               const int *__restrict__ start, int nmol)
+{
+    extern __shared__ double sm[];
+    __shared__ int bi[64], bj[64];
+    const Unit w = unit_of(mols, start, nmol, false, bi, bj);
+    if ((active && !active[w.mol]) || w.u == 0) return;
+    const CCMol &m = mols[w.mol];
+    const int o = m.o, v = m.v, ne = w.nb * v * v;
+    for (int e = threadIdx.x; e < ne; e += NT) {
+        const Elem x = elem(e, v);
+        sm[x.s] = m.t2[pair_off(bi[x.lb], x.a, bj[x.lb], x.b, o, v)];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < ne; e += NT) {
+        const Elem x = elem(e, v);
+        const double tt = sm[(x.lb * v + x.b) * (v + 1) + x.a];
+        m.u[pair_off(bi[x.lb], x.a, bj[x.lb], x.b, o, v)] = 2.0 * sm[x.s] - tt;
     }
 }
 
-// ---------------------------------------------------------------- step
-// d1 = r1, d2 = 2 r2(ijab) - r2(ijba); t1 += s1 d1/D1 and, by the projection
-// type of stepCC (mod_cc.f90:1007-1008),
-//   "2-1" (proj 2): t2 += s2 (2 d2(ijab) + d2(ijba))/D2 = 3 s2 r2/D2,
-//   "1"   (proj 1): t2 += s2 d2(ijab)/D2.
-// Writes the new amplitudes and the DIIS error vector (d1, 3 r2 or d2, as
-// pushCCVectors :1417-1420) into the history slot `slot`, and per-block
-// maxima of |d1|, |d2| into part.
-__global__ void k_step(const CCMol *mols, const DiisMol *diis, const int *active, double s1, double s2,
-                       int use_diis, int proj, double *part, int nblk)
+// Residual, Jacobi step and DIIS push of one unit (SK_UP units).
+//   singles: d1 = r1; t1 += s1 d1 / D1.
+//   doubles of a block (i, j), i <= j: w = Omega2(ia, jb) assembled as
+//     r2 + X2 + X2 pair-transposed (the E and C/D terms), d2 = 2 w(ab) - w(ba)
+//     (= w on a diagonal block, whose canonical element is the same for both);
+//     g = 3 w ("2-1") or d2 ("1"); t2 += s2 g / D2 with D2 = (F_ii + F_jj) -
+//     (F_aa + F_bb) (the grouping the set-up uses, so (ia,jb) and (jb,ia)
+//     round alike).
+// push = 1: (t, g) go into the ring slot count % nd and part gets the dots of
+// g with every stored error vector (weights as the reference's packed dots:
+// 1, or 1/2 for the two mirror elements (a, b) != (b, a) of a diagonal
+// block); t2 itself is written by k_extrapolate. push = 0 (no DIIS): t1 and
+// both halves of t2 are written here. part[0], part[1] = max|d1|, max|d2|.
+__global__ void __launch_bounds__(NT) k_step_push(const CCMol *__restrict__ mols, const DiisMol *__restrict__ diis,
+                                                  const int *__restrict__ active, const int *__restrict__ start,
+                                                  int nmol, double s1, double s2, int proj, int push,
+                                                  double *__restrict__ part)
 {
-    if (skip(active)) return;
-    const CCMol &m = mols[blockIdx.y];
-    const DiisMol &h = diis[blockIdx.y];
-    const int o = m.o, v = m.v;
-    const long long ov = (long long)o * v, L2 = ov * ov;
-    const int slot = h.count[0] % h.nd;
-    double *Ht = use_diis ? h.Ht + (long long)slot * h.L : nullptr;
-    double *He = use_diis ? h.He + (long long)slot * h.L : nullptr;
-    double mx1 = 0.0, mx2 = 0.0;
-    GRID_LOOP(e, ov + L2) {
-        if (e < ov) {
-            double d = m.r1[e];
-            mx1 = fmax(mx1, fabs(d));
-            double t = m.t1[e] + s1 * d / m.D1[e];
-            m.t1[e] = t;
-            if (Ht) { Ht[e] = t; He[e] = d; }
-        } else {
-            long long f = e - ov;
-            int b = (int)(f % v);
-            long long r = f / v;
-            int j = (int)(r % o); r /= o;
-            int a = (int)(r % v);
-            int i = (int)(r / v);
-            // as the reference, each pair (ia),(jb) takes the value computed for
-            // (ia) <= (jb), so the amplitudes stay exactly pair-symmetric
-            const long long p1 = (long long)i * v + a, q1 = (long long)j * v + b;
-            const long long p2 = (long long)i * v + b, q2 = (long long)j * v + a;
-            double w = m.r2[min(p1, q1) * ov + max(p1, q1)];
-            double d2 = 2.0 * w - m.r2[min(p2, q2) * ov + max(p2, q2)];
-            mx2 = fmax(mx2, fabs(d2));
-            const double g = proj == 1 ? d2 : 3.0 * w;
-            double t = m.t2[f] + s2 * g / m.D2[f];
-            m.t2[f] = t;
-            if (Ht) { Ht[e] = t; He[e] = g; }
+    extern __shared__ double sm[];
+    __shared__ int bi[64], bj[64];
+    const Unit w = unit_of(mols, start, nmol, true, bi, bj);
+    if (active && !active[w.mol]) return;
+    const CCMol &m = mols[w.mol];
+    const DiisMol &h = diis[w.mol];
+    const int o = m.o, v = m.v, n = m.N, ov = o * v;
+    double *P = part + (long long)blockIdx.x * HX_PART_STRIDE;
+    const int cnt = push ? h.count[0] : 0;
+    const int slot = push ? cnt % h.nd : 0, nvec = push ? min(cnt + 1, h.nd) : 0;
+    double *S = sm;                              // the assembled residual of the unit's blocks
+    double mx = 0.0;
+    long long hoff;
+    int ne;
+    if (w.u == 0) {
+        ne = ov;
+        hoff = 0;
+        for (int e = threadIdx.x; e < ov; e += NT) {
+            const double d = m.r1[e];
+            mx = fmax(mx, fabs(d));
+            const double t = m.t1[e] + s1 * d / m.D1[e];
+            if (push) { h.Ht[(long long)slot * h.L + e] = t; h.He[(long long)slot * h.L + e] = d; }
+            else m.t1[e] = t;
+        }
+    } else {
+        ne = w.nb * v * v;
+        hoff = ov + (long long)w.k0 * v * v;
+        // S = r2 + (X2 + X2[q][p]): element (a, b) of block (i, j) takes
+        // X2[j][b][i][a], read with a fastest (coalesced) and added at the
+        // transposed tile position
+        for (int e = threadIdx.x; e < ne; e += NT) {
+            const Elem x = elem(e, v);
+            S[x.s] = m.X2[pair_off(bi[x.lb], x.a, bj[x.lb], x.b, o, v)];
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < ne; e += NT) {
+            const Elem x = elem(e, v);                 // x.a plays b, x.b plays a
+            S[(x.lb * v + x.b) * (v + 1) + x.a] += m.X2[pair_off(bj[x.lb], x.a, bi[x.lb], x.b, o, v)];
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < ne; e += NT) {
+            const Elem x = elem(e, v);
+            S[x.s] = m.r2[pair_off(bi[x.lb], x.a, bj[x.lb], x.b, o, v)] + S[x.s];
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < ne; e += NT) {
+            const Elem x = elem(e, v);
+            const int i = bi[x.lb], j = bj[x.lb];
+            const double sab = S[x.s], sba = S[(x.lb * v + x.b) * (v + 1) + x.a];
+            double wv, d2;
+            if (i < j) { wv = sab; d2 = 2.0 * sab - sba; }
+            else { wv = x.a <= x.b ? sab : sba; d2 = wv; }
+            mx = fmax(mx, fabs(d2));
+            const double g = proj == 1 ? d2 : 3.0 * wv;
+            const double D = (m.Fmo[i * n + i] + m.Fmo[j * n + j]) -
+                             (m.Fmo[(o + x.a) * n + o + x.a] + m.Fmo[(o + x.b) * n + o + x.b]);
+            const long long f = pair_off(i, x.a, j, x.b, o, v);
+            const double t = m.t2[f] + s2 * g / D;
+            if (push) {
+                h.Ht[(long long)slot * h.L + hoff + e] = t;
+                h.He[(long long)slot * h.L + hoff + e] = g;
+            } else {
+                m.t2[f] = t;
+            }
+        }
+        __syncthreads();                         // (also makes the global writes above visible to the block)
+        if (!push) {   // the mirror half: t2[j][b][i][a] = t2[i][a][j][b], a fastest (DIIS off only)
+            for (int e = threadIdx.x; e < ne; e += NT) {
+                const Elem x = elem(e, v);             // x.a plays b, x.b plays a
+                const int i = bi[x.lb], j = bj[x.lb];
+                if (i < j) m.t2[pair_off(j, x.a, i, x.b, o, v)] = m.t2[pair_off(i, x.b, j, x.a, o, v)];
+            }
         }
     }
-    double r1 = block_red(mx1, true);
-    double r2 = block_red(mx2, true);
-    if (threadIdx.x == 0) {
-        part[((long long)blockIdx.y * nblk + blockIdx.x) * 2 + 0] = r1;
-        part[((long long)blockIdx.y * nblk + blockIdx.x) * 2 + 1] = r2;
+    const double r = block_red(mx, true);
+    if (threadIdx.x == 0) { P[0] = w.u == 0 ? r : 0.0; P[1] = w.u == 0 ? 0.0 : r; }
+    // dots of the new error vector (just written, read back from L2) with every stored one
+    const double *En = h.He + (long long)slot * h.L + hoff;
+    for (int k = 0; k < nvec; ++k) {
+        const double *Ek = h.He + (long long)k * h.L + hoff;
+        double acc = 0.0;
+        for (int e = threadIdx.x; e < ne; e += NT) {
+            double wt = 1.0;
+            if (w.u > 0) {
+                const Elem x = elem(e, v);
+                if (bi[x.lb] == bj[x.lb] && x.a != x.b) wt = 0.5;
+            }
+            const double g = En[e];
+            acc += wt * g * (k == slot ? g : Ek[e]);
+        }
+        const double dk = block_red(acc, false);
+        if (threadIdx.x == 0) P[2 + k] = dk;
     }
-}
-
-__global__ void k_step_finish(const CCMol *mols, const int *active, const double *part, int nblk)
-{
-    const int mol = blockIdx.x;
-    if (active && !active[mol]) return;
-    double a = 0.0, b = 0.0;
-    for (int k = threadIdx.x; k < nblk; k += blockDim.x) {
-        a = fmax(a, part[((long long)mol * nblk + k) * 2 + 0]);
-        b = fmax(b, part[((long long)mol * nblk + k) * 2 + 1]);
-    }
-    a = warp_max(a); b = warp_max(b);
-    if (threadIdx.x == 0) { mols[mol].res[0] = a; mols[mol].res[1] = b; }
 }
 
 // ---------------------------------------------------------------- DIIS
-// gate[mol]: the DIIS step runs while max(|d1|,|d2|) >= gate[mol]. The
-// reference stops mixing once the residual is below the convergence target
-// (there the iteration ends); FP64 iterations use that target, tensor-core
-// iterations (which hand over rather than converge) their hand-over target.
-// Weighted dots of the newest error vector with every stored one. The doubles
-// part is a symmetric pair matrix; the reference's vectors hold only the pairs
-// (ia) <= (jb), so off-diagonal products count 1/2 and diagonal ones 1.
-__global__ void k_diis_dots(const CCMol *mols, const DiisMol *diis, const int *active, const double *gate,
-                            double *part, int nblk)
-{
-    if (skip(active)) return;
-    const CCMol &m = mols[blockIdx.y];
-    const DiisMol &h = diis[blockIdx.y];
-    if (!(fmax(m.res[0], m.res[1]) >= gate[blockIdx.y])) return;      // converged: the reference skips DIIS
-    const long long ov = (long long)m.o * m.v;
-    const int cnt = h.count[0] + 1, n = cnt < h.nd ? cnt : h.nd;
-    const int k = blockIdx.z;                             // stored vector of this block
-    if (k >= n) return;
-    const int slot = h.count[0] % h.nd;
-    const double *en = h.He + (long long)slot * h.L;
-    const double *ek = h.He + (long long)k * h.L;
-    double acc = 0.0;
-    GRID_LOOP(e, h.L) {
-        double w = 1.0;
-        if (e >= ov) {
-            long long f = e - ov, p = f / ov, q = f % ov;
-            w = (p == q) ? 1.0 : 0.5;
-        }
-        acc += w * en[e] * ek[e];
-    }
-    double r = block_red(acc, false);
-    if (threadIdx.x == 0) part[((long long)blockIdx.y * nblk + blockIdx.x) * HX_MAX_DIIS + k] = r;
-}
-
-// Ordered sum of the partial dots into the Gram matrix (slot indexing), then
-// the bordered DIIS system solved by Gaussian elimination with partial
-// pivoting (one thread per molecule). Coefficients go to h.coef[slot].
-__global__ void k_diis_solve(const CCMol *mols, const DiisMol *diis, const int *active, const double *gate,
-                             const double *part, int nblk)
+// One warp per molecule. The maxima of the units give res[0], res[1] (the
+// reference's accuracy(1..2), before the step). gate[mol]: the DIIS step runs
+// while max(|d1|,|d2|) >= gate[mol]. The reference stops mixing once the
+// residual is below the convergence target (there the iteration ends); FP64
+// iterations use that target, tensor-core iterations (which hand over rather
+// than converge) their hand-over target. When it runs, the ordered sums of
+// the units' dots form the Gram row of the new slot and the bordered system
+// is solved by Gaussian elimination with partial pivoting; coef[HX_MAX_DIIS]
+// = vectors to mix (1: none, t = the newest) and coef[HX_MAX_DIIS + 1] = the
+// newest slot.
+__global__ void k_diis_solve(const CCMol *__restrict__ mols, const DiisMol *__restrict__ diis,
+                             const int *__restrict__ active, const int *__restrict__ start, const double *gate,
+                             const double *__restrict__ part, int push)
 {
     const int mol = blockIdx.x;
     if (active && !active[mol]) return;
     const CCMol &m = mols[mol];
+    const int u0 = start[mol], u1 = start[mol + 1];
+    double a = 0.0, b = 0.0;
+    for (int u = u0 + threadIdx.x; u < u1; u += 32) {
+        a = fmax(a, part[(long long)u * HX_PART_STRIDE + 0]);
+        b = fmax(b, part[(long long)u * HX_PART_STRIDE + 1]);
+    }
+    a = warp_max(a);
+    b = warp_max(b);
+    if (threadIdx.x == 0) { m.res[0] = a; m.res[1] = b; }
+    if (!push) return;
     const DiisMol &h = diis[mol];
-    if (!(fmax(m.res[0], m.res[1]) >= gate[mol])) return;
-    const int cnt = h.count[0] + 1, n = cnt < h.nd ? cnt : h.nd;
-    const int slot = h.count[0] % h.nd;
+    const int cnt = h.count[0];
+    const int slot = cnt % h.nd, n = cnt + 1 < h.nd ? cnt + 1 : h.nd;
+    if (!(fmax(a, b) >= gate[mol])) {                  // converged: the reference skips DIIS
+        if (threadIdx.x == 0) { h.coef[HX_MAX_DIIS] = 1.0; h.coef[HX_MAX_DIIS + 1] = slot; }
+        return;
+    }
     __shared__ double g[HX_MAX_DIIS];
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    for (int k = threadIdx.x; k < n; k += 32) {
         double s = 0.0;
-        for (int b = 0; b < nblk; ++b) s += part[((long long)mol * nblk + b) * HX_MAX_DIIS + k];
+        for (int u = u0; u < u1; ++u) s += part[(long long)u * HX_PART_STRIDE + 2 + k];
         g[k] = s;
     }
-    __syncthreads();
+    __syncwarp();
     if (threadIdx.x != 0) return;
     for (int k = 0; k < n; ++k) {
         h.gram[slot * h.nd + k] = g[k];
         h.gram[k * h.nd + slot] = g[k];
     }
-    h.count[0] = cnt;
-    if (n == 1) { h.coef[HX_MAX_DIIS] = 0.0; return; }     // newCCVectors(1) returns early
+    h.count[0] = cnt + 1;
+    h.coef[HX_MAX_DIIS + 1] = slot;
+    h.coef[HX_MAX_DIIS] = 1.0;
+    if (n == 1) return;                                // newCCVectors(1) returns early
     const int nb = n + 1;
     double A[(HX_MAX_DIIS + 1) * (HX_MAX_DIIS + 1)], x[HX_MAX_DIIS + 1];
     for (int p = 0; p < nb; ++p) {
@@ -329,65 +447,106 @@ __global__ void k_diis_solve(const CCMol *mols, const DiisMol *diis, const int *
         for (int c = k + 1; c < nb; ++c) s -= A[k * nb + c] * x[c];
         x[k] = s / A[k * nb + k];
     }
-    for (int k = 0; k < n; ++k) {
-        if (!isfinite(x[k])) { h.coef[HX_MAX_DIIS] = 0.0; return; }   // singular subspace: no mixing
-        h.coef[k] = x[k];
-    }
-    h.coef[HX_MAX_DIIS] = (double)n;     // number of vectors to mix
+    for (int k = 0; k < n; ++k)
+        if (!isfinite(x[k])) return;                   // singular subspace: no mixing
+    for (int k = 0; k < n; ++k) h.coef[k] = x[k];
+    h.coef[HX_MAX_DIIS] = (double)n;
 }
 
-// t = sum_k c_k Ht[k]
-__global__ void k_diis_extrapolate(const CCMol *mols, const DiisMol *diis, const int *active, const double *gate)
+// ---------------------------------------------------------------- amplitudes and energy
+// Element (a, b) of block (i, j), i <= j, counts twice in the full pair sum
+// of energyCC when i < j (it and its mirror) and once on a diagonal block.
+__device__ __forceinline__ double energy_term(const CCMol &m, int i, int j, int a, int b, double t, double t1a,
+                                              double t1b)
 {
-    if (skip(active)) return;
-    const CCMol &m = mols[blockIdx.y];
-    const DiisMol &h = diis[blockIdx.y];
-    if (!(fmax(m.res[0], m.res[1]) >= gate[blockIdx.y])) return;
-    const int n = (int)h.coef[HX_MAX_DIIS];
-    if (n < 2) return;
-    const long long ov = (long long)m.o * m.v;
-    GRID_LOOP(e, h.L) {
-        double s = 0.0;
-        for (int k = 0; k < n; ++k) s += h.coef[k] * h.Ht[(long long)k * h.L + e];
-        if (e < ov) m.t1[e] = s; else m.t2[e - ov] = s;
-    }
+    const double s = m.Lov[pair_off(i, a, j, b, m.o, m.v)] * (t + t1a * t1b);
+    return i < j ? 2.0 * s : s;
 }
 
-// ---------------------------------------------------------------- energy
-// E = 2 sum F_ia t_ia + sum_(ia),(jb) L(ia,jb) (t2 + t1 t1)   (energyCC r-ccsd)
-__global__ void k_energy(const CCMol *mols, const int *active, double *part, int nblk)
+// t = the newest history vector or sum_k c_k Ht[k] (k = 0 .. n-1, slot order)
+__device__ __forceinline__ double combine(const DiisMol &h, int nmix, int slot, long long e)
 {
-    if (skip(active)) return;
-    const CCMol &m = mols[blockIdx.y];
-    const int o = m.o, v = m.v, n = m.N;
-    const long long ov = (long long)o * v;
-    double s1 = 0.0, s2 = 0.0;
-    GRID_LOOP(e, ov + ov * ov) {
-        if (e < ov) {
-            int i = (int)(e / v), a = (int)(e % v);
-            s1 += m.Fmo[i * n + o + a] * m.t1[e];
-        } else {
-            long long f = e - ov, p = f / ov, q = f % ov;
-            s2 += m.Lov[f] * (m.t2[f] + m.t1[p] * m.t1[q]);
+    if (nmix <= 1) return h.Ht[(long long)slot * h.L + e];
+    double s = 0.0;
+    for (int k = 0; k < nmix; ++k) s += h.coef[k] * h.Ht[(long long)k * h.L + e];
+    return s;
+}
+
+// energyCC r-ccsd of the unit: part[0] = sum F_ia t_ia (singles unit),
+// part[1] = the unit's share of sum L (t2 + t1 t1). With DIIS (from != 0) the
+// amplitudes come from the ring (the extrapolation) and are written to t1 and
+// both halves of t2; without, they are read from t1, t2.
+__global__ void __launch_bounds__(NT) k_amplitudes_energy(const CCMol *__restrict__ mols,
+                                                          const DiisMol *__restrict__ diis,
+                                                          const int *__restrict__ active,
+                                                          const int *__restrict__ start, int nmol, int from,
+                                                          double *__restrict__ part)
+{
+    extern __shared__ double sm[];
+    __shared__ int bi[64], bj[64];
+    const Unit w = unit_of(mols, start, nmol, true, bi, bj);
+    if (active && !active[w.mol]) return;
+    const CCMol &m = mols[w.mol];
+    const DiisMol &h = diis[w.mol];
+    const int o = m.o, v = m.v, n = m.N, ov = o * v;
+    const int nmix = from ? (int)h.coef[HX_MAX_DIIS] : 0, slot = from ? (int)h.coef[HX_MAX_DIIS + 1] : 0;
+    double *P = part + (long long)blockIdx.x * HX_PART_STRIDE;
+    double acc = 0.0;
+    if (w.u == 0) {
+        for (int e = threadIdx.x; e < ov; e += NT) {
+            const double t = from ? combine(h, nmix, slot, e) : m.t1[e];
+            if (from) m.t1[e] = t;
+            acc += m.Fmo[(e / v) * n + o + e % v] * t;
+        }
+    } else {
+        // this unit's t1 rows i and j (from the ring: t1 is being written by unit 0)
+        double *T1 = sm + hx_unit_tile(o, v);            // [block][2][v]
+        for (int e = threadIdx.x; e < w.nb * 2 * v; e += NT) {
+            const int lb = e / (2 * v), r = e % (2 * v), a = r % v, row = r < v ? bi[lb] : bj[lb];
+            T1[e] = from ? combine(h, nmix, slot, (long long)row * v + a) : m.t1[row * v + a];
+        }
+        __syncthreads();
+        const int ne = w.nb * v * v;
+        const long long hoff = ov + (long long)w.k0 * v * v;
+        for (int e = threadIdx.x; e < ne; e += NT) {
+            const Elem x = elem(e, v);
+            const int i = bi[x.lb], j = bj[x.lb];
+            const long long f = pair_off(i, x.a, j, x.b, o, v);
+            double t;
+            if (from) {
+                t = combine(h, nmix, slot, hoff + e);
+                m.t2[f] = t;
+                sm[x.s] = t;
+            } else {
+                t = m.t2[f];
+            }
+            acc += energy_term(m, i, j, x.a, x.b, t, T1[x.lb * 2 * v + x.a], T1[x.lb * 2 * v + v + x.b]);
+        }
+        if (from) {
+            __syncthreads();
+            for (int e = threadIdx.x; e < ne; e += NT) {
+                const Elem x = elem(e, v);                 // x.a plays b, x.b plays a
+                const int i = bi[x.lb], j = bj[x.lb];
+                if (i < j) m.t2[pair_off(j, x.a, i, x.b, o, v)] = sm[(x.lb * v + x.b) * (v + 1) + x.a];
+            }
         }
     }
-    double r1 = block_red(s1, false);
-    double r2 = block_red(s2, false);
-    if (threadIdx.x == 0) {
-        part[((long long)blockIdx.y * nblk + blockIdx.x) * 2 + 0] = r1;
-        part[((long long)blockIdx.y * nblk + blockIdx.x) * 2 + 1] = r2;
-    }
+    const double r = block_red(acc, false);
+    if (threadIdx.x == 0) { P[0] = w.u == 0 ? r : 0.0; P[1] = w.u == 0 ? 0.0 : r; }
 }
 
-__global__ void k_energy_finish(const CCMol *mols, const int *active, const double *part, int nblk)
+// E = 2 sum F_ia t_ia + sum_(ia),(jb) L(ia,jb) (t2 + t1 t1)   (energyCC r-ccsd):
+// ordered sums of the units' partials
+__global__ void k_energy_finish(const CCMol *__restrict__ mols, const int *__restrict__ active,
+                                const int *__restrict__ start, const double *__restrict__ part)
 {
     const int mol = blockIdx.x;
     if (active && !active[mol]) return;
     if (threadIdx.x != 0) return;
     double a = 0.0, b = 0.0;
-    for (int k = 0; k < nblk; ++k) {
-        a += part[((long long)mol * nblk + k) * 2 + 0];
-        b += part[((long long)mol * nblk + k) * 2 + 1];
+    for (int u = start[mol]; u < start[mol + 1]; ++u) {
+        a += part[(long long)u * HX_PART_STRIDE + 0];
+        b += part[(long long)u * HX_PART_STRIDE + 1];
     }
     const CCMol &m = mols[mol];
     m.res[2] = 2.0 * a + b + m.eref;
@@ -399,13 +558,12 @@ __global__ void k_energy_finish(const CCMol *mols, const int *active, const doub
 // ---------------------------------------------------------------- set-up
 // Constants after SCF: denominators, ZDO vectors of the undressed ov space,
 // and the reference guess (guessCC r-ccsd, mod_cc.f90:634-650) when asked.
-__global__ void k_setup(const CCMol *mols, const int *active)
+__global__ void k_setup(EW_ARGS)
 {
-    if (skip(active)) return;
-    const CCMol &m = mols[blockIdx.y];
+    EW_PROLOGUE
     const int n = m.N, o = m.o, v = m.v;
     const long long ov = (long long)o * v;
-    GRID_LOOP(e, ov + ov * ov + (long long)n * ov) {
+    EW_LOOP(e, ov + ov * ov + (long long)n * ov) {
         if (e < ov) {
             int i = (int)(e / v), a = (int)(e % v);
             m.D1[e] = m.Fmo[i * n + i] - m.Fmo[(o + a) * n + o + a];
@@ -427,13 +585,12 @@ __global__ void k_setup(const CCMol *mols, const int *active)
 }
 
 // Lov = 2 gov - gov(ab swapped); t1, t2 = reference guess (when guess != 0)
-__global__ void k_setup2(const CCMol *mols, const int *active, int guess)
+__global__ void k_setup2(EW_ARGS, int guess)
 {
-    if (skip(active)) return;
-    const CCMol &m = mols[blockIdx.y];
+    EW_PROLOGUE
     const int n = m.N, o = m.o, v = m.v;
     const long long ov = (long long)o * v;
-    GRID_LOOP(e, ov * ov) {
+    EW_LOOP(e, ov * ov) {
         int b = (int)(e % v);
         long long r = e / v;
         int j = (int)(r % o); r /= o;
@@ -456,80 +613,89 @@ __global__ void k_setup2(const CCMol *mols, const int *active, int guess)
 }  // namespace
 
 // ---------------------------------------------------------------- launchers
-static inline dim3 grid_for(long long work, int nmol, int cap = 4096)
-{
-    long long b = (work + NT - 1) / NT;
-    if (b < 1) b = 1;
-    if (b > cap) b = cap;
-    return dim3((unsigned)b, (unsigned)nmol);
-}
-
-#define LAUNCH_EW(kern, work, ...)                                                   \
-    do {                                                                             \
-        kern<<<grid_for(work, nmol), NT, 0, s>>>(__VA_ARGS__);                       \
-        hx_count_launches(1);                                                        \
-        cudaError_t e_ = cudaGetLastError();                                         \
-        if (e_ != cudaSuccess) return e_;                                            \
+#define LAUNCH_EW(kern, kind, ...)                                                                  \
+    do {                                                                                            \
+        if (S.blocks[kind] > 0)                                                                     \
+            kern<<<(unsigned)S.blocks[kind], NT, 0, s>>>(m, act, S.start[kind], S.nmol, ##__VA_ARGS__); \
+        hx_count_launches(1);                                                                       \
+        cudaError_t e_ = cudaGetLastError();                                                        \
+        if (e_ != cudaSuccess) return e_;                                                           \
     } while (0)
 
-cudaError_t hx_ew_dress_init(const CCMol *m, const int *act, int nmol, long long maxw, cudaStream_t s)
-{ LAUNCH_EW(k_dress_init, maxw, m, act); return cudaSuccess; }
-cudaError_t hx_ew_dress_fock(const CCMol *m, const int *act, int nmol, long long maxw, cudaStream_t s)
-{ LAUNCH_EW(k_dress_fock, maxw, m, act); return cudaSuccess; }
-cudaError_t hx_ew_zdo_products(const CCMol *m, const int *act, int nmol, long long maxw, cudaStream_t s)
-{ LAUNCH_EW(k_zdo_products, maxw, m, act); return cudaSuccess; }
-cudaError_t hx_ew_make_u(const CCMol *m, const int *act, int nmol, long long maxw, cudaStream_t s)
-{ LAUNCH_EW(k_make_u, maxw, m, act); return cudaSuccess; }
-cudaError_t hx_ew_gamma_scale(const CCMol *m, const int *act, int nmol, long long maxw, cudaStream_t s)
-{ LAUNCH_EW(k_gamma_scale, maxw, m, act); return cudaSuccess; }
-cudaError_t hx_ew_fock_blocks(const CCMol *m, const int *act, int nmol, long long maxw, cudaStream_t s)
-{ LAUNCH_EW(k_fock_blocks, maxw, m, act); return cudaSuccess; }
-cudaError_t hx_ew_c_combine(const CCMol *m, const int *act, int nmol, long long maxw, cudaStream_t s)
-{ LAUNCH_EW(k_c_combine, maxw, m, act); return cudaSuccess; }
-cudaError_t hx_ew_assemble(const CCMol *m, const int *act, int nmol, long long maxw, cudaStream_t s)
-{ LAUNCH_EW(k_assemble, maxw, m, act); return cudaSuccess; }
-cudaError_t hx_ew_setup(const CCMol *m, const int *act, int nmol, long long maxw, int guess, cudaStream_t s)
+cudaError_t hx_ew_dress_init(const CCMol *m, const int *act, const HxSched &S, cudaStream_t s)
+{ LAUNCH_EW(k_dress_init, SK_NN); return cudaSuccess; }
+cudaError_t hx_ew_dress_fock(const CCMol *m, const int *act, const HxSched &S, cudaStream_t s)
+{ LAUNCH_EW(k_dress_fock, SK_NN); return cudaSuccess; }
+cudaError_t hx_ew_zdo_products(const CCMol *m, const int *act, const HxSched &S, cudaStream_t s)
+{ LAUNCH_EW(k_zdo_products, SK_ZDO); return cudaSuccess; }
+cudaError_t hx_ew_gamma_scale(const CCMol *m, const int *act, const HxSched &S, cudaStream_t s)
+{ LAUNCH_EW(k_gamma_scale, SK_ONON); return cudaSuccess; }
+cudaError_t hx_ew_fock_blocks(const CCMol *m, const int *act, const HxSched &S, cudaStream_t s)
+{ LAUNCH_EW(k_fock_blocks, SK_FOCK); return cudaSuccess; }
+cudaError_t hx_ew_c_combine(const CCMol *m, const int *act, const HxSched &S, cudaStream_t s)
+{ LAUNCH_EW(k_c_combine, SK_PAIR); return cudaSuccess; }
+cudaError_t hx_ew_setup(const CCMol *m, const int *act, const HxSched &S, cudaStream_t s)
+{ LAUNCH_EW(k_setup, SK_SETUP); return cudaSuccess; }
+cudaError_t hx_ew_setup2(const CCMol *m, const int *act, const HxSched &S, int guess, cudaStream_t s)
+{ LAUNCH_EW(k_setup2, SK_PAIR, guess); return cudaSuccess; }
+
+// dynamic shared memory of the pair-unit kernels (bytes): the largest over the batch
+size_t hx_unit_smem(const int *o, const int *v, int nmol, int kernel)
 {
-    LAUNCH_EW(k_setup, maxw, m, act);
-    return cudaSuccess;
-}
-cudaError_t hx_ew_setup2(const CCMol *m, const int *act, int nmol, long long maxw, int guess, cudaStream_t s)
-{
-    LAUNCH_EW(k_setup2, maxw, m, act, guess);
-    return cudaSuccess;
+    long long mx = 0;
+    for (int k = 0; k < nmol; ++k) {
+        const long long t = hx_unit_tile(o[k], v[k]);
+        long long need = t;                                                 // k_make_u
+        if (kernel == 1) need = t;                                          // k_step_push
+        if (kernel == 2) need = t + 2LL * hx_unit_blocks(v[k]) * v[k];      // k_amplitudes_energy
+        mx = need > mx ? need : mx;
+    }
+    return (size_t)mx * sizeof(double);
 }
 
-cudaError_t hx_step(const CCMol *m, const DiisMol *h, const int *act, int nmol, double s1, double s2,
-                    int use_diis, int proj, double *part, int nblk, cudaStream_t s)
+cudaError_t hx_unit_kernels_init(size_t smem_max)
 {
-    k_step<<<dim3(nblk, nmol), NT, 0, s>>>(m, h, act, s1, s2, use_diis, proj, part, nblk);
-    hx_count_launches(2);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    k_step_finish<<<nmol, 32, 0, s>>>(m, act, part, nblk);
+    cudaError_t e = cudaSuccess;
+    const int b = (int)smem_max;
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_make_u, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_step_push, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_amplitudes_energy, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    return e;
+}
+
+cudaError_t hx_ew_make_u(const CCMol *m, const int *act, const HxSched &S, size_t smem, cudaStream_t s)
+{
+    k_make_u<<<(unsigned)S.blocks[SK_FULL], NT, smem, s>>>(m, act, S.start[SK_FULL], S.nmol);
+    hx_count_launches(1);
     return cudaGetLastError();
 }
 
-cudaError_t hx_diis(const CCMol *m, const DiisMol *h, const int *act, int nmol, const double *gate, double *part,
-                    int nblk, int nd_max, cudaStream_t s)
+// stepCC + pushCCVectors + diisDotProduct + newCCVectors + energyCC of every active molecule
+cudaError_t hx_tail(const CCMol *m, const DiisMol *h, const int *act, const HxSched &S, const size_t smem[2],
+                    double s1, double s2, int proj, int use_diis, const double *gate, double *part, cudaStream_t s)
 {
-    k_diis_dots<<<dim3(nblk, nmol, nd_max), NT, 0, s>>>(m, h, act, gate, part, nblk);
-    hx_count_launches(3);
+    k_step_push<<<(unsigned)S.blocks[SK_UP], NT, smem[0], s>>>(m, h, act, S.start[SK_UP], S.nmol, s1, s2, proj,
+                                                               use_diis, part);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_diis_solve<<<nmol, 32, 0, s>>>(m, h, act, gate, part, nblk);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    k_diis_extrapolate<<<dim3(nblk, nmol), NT, 0, s>>>(m, h, act, gate);
+    k_diis_solve<<<S.nmol, 32, 0, s>>>(m, h, act, S.start[SK_UP], gate, part, use_diis);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    k_amplitudes_energy<<<(unsigned)S.blocks[SK_UP], NT, smem[1], s>>>(m, h, act, S.start[SK_UP], S.nmol, use_diis,
+                                                                       part);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    k_energy_finish<<<S.nmol, 32, 0, s>>>(m, act, S.start[SK_UP], part);
+    hx_count_launches(4);
     return cudaGetLastError();
 }
 
-cudaError_t hx_energy(const CCMol *m, const int *act, int nmol, double *part, int nblk, cudaStream_t s)
+// energyCC of every (active) molecule from its current amplitudes
+cudaError_t hx_energy(const CCMol *m, const DiisMol *h, const int *act, const HxSched &S, size_t smem, double *part,
+                      cudaStream_t s)
 {
-    k_energy<<<dim3(nblk, nmol), NT, 0, s>>>(m, act, part, nblk);
-    hx_count_launches(2);
+    k_amplitudes_energy<<<(unsigned)S.blocks[SK_UP], NT, smem, s>>>(m, h, act, S.start[SK_UP], S.nmol, 0, part);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_energy_finish<<<nmol, 32, 0, s>>>(m, act, part, nblk);
+    k_energy_finish<<<S.nmol, 32, 0, s>>>(m, act, S.start[SK_UP], part);
+    hx_count_launches(2);
     return cudaGetLastError();
 }

@@ -193,10 +193,12 @@ struct hx_ccsd {
     double gate_eps = 0.0;               // convergence target the gates were made for
     double *d_part = nullptr;
     double *d_res = nullptr;             // nmol x 8 iteration results (inside the arena)
-    int nblk = 64;                       // blocks per molecule of the reductions (set at allocation)
+    HxSched sched{};                     // balanced launch schedules of the batch (hx_plan.h)
+    int *d_sched = nullptr;
+    size_t unit_smem[3] = {0, 0, 0};     // dynamic shared memory of the pair-unit kernels
     std::vector<Group> plan;             // GEMM groups of one iteration (in order)
     std::vector<Group> setup_groups;
-    long long maxw_nn = 0, maxw_ov = 0, maxw_pair = 0, maxw_oNoN = 0;
+    long long maxw_oNoN = 0;
     bool initialized = false;
     std::atomic<int> cancel{0};
     // per molecule host results
@@ -465,17 +467,12 @@ static int allocate(hx_ccsd *h)
             m.U = A.take<double>(ov * N); m.UG = A.take<double>(ov * N); m.Vs = A.take<double>((size_t)o * N);
             DiisMol &d = h->diis[mi];
             d.nd = nd > 0 ? nd : 1;
-            d.L = (long long)(ov + pr);
+            d.L = (long long)(ov + (size_t)v * v * o * (o + 1) / 2);   // singles + canonical pair blocks
             d.Ht = nd ? A.take<double>((size_t)nd * d.L) : nullptr;
             d.He = nd ? A.take<double>((size_t)nd * d.L) : nullptr;
             d.gram = A.take<double>((size_t)HX_MAX_DIIS * HX_MAX_DIIS);
-            d.coef = A.take<double>(HX_MAX_DIIS + 1);
+            d.coef = A.take<double>(HX_MAX_DIIS + 2);
             d.count = A.take<int>(1);
-            h->maxw_nn = std::max<long long>(h->maxw_nn, nn);
-            h->maxw_ov = std::max<long long>(h->maxw_ov, ov + v * v + o * o);
-            h->maxw_pair = std::max<long long>(h->maxw_pair, pr + ov);
-            h->maxw_oNoN = std::max<long long>(h->maxw_oNoN, (long long)o * N * o * N);
-            h->maxw_oNoN = std::max<long long>(h->maxw_oNoN, (long long)N * (ov + o * o + v * v));
             h->maxw_oNoN = std::max<long long>(h->maxw_oNoN, (long long)(ov + pr + N * ov));
         }
         double *resblock = A.take<double>((size_t)8 * h->nmol);
@@ -495,11 +492,45 @@ static int allocate(hx_ccsd *h)
     HX_CU(cudaMalloc(&h->d_cc, sizeof(CCMol) * h->nmol));
     HX_CU(cudaMalloc(&h->d_diis, sizeof(DiisMol) * h->nmol));
     HX_CU(cudaMalloc(&h->d_active, sizeof(int) * h->nmol));
-    // reductions: enough blocks per molecule to fill the GPU, capped by the work
-    long long maxpair = 0;
-    for (int mi = 0; mi < h->nmol; ++mi) maxpair = std::max<long long>(maxpair, (long long)h->o[mi] * h->v[mi] * h->o[mi] * h->v[mi]);
-    h->nblk = (int)std::max<long long>(1, std::min<long long>(std::max(1, 1216 / h->nmol), (maxpair + 4095) / 4096));
-    HX_CU(cudaMalloc(&h->d_part, sizeof(double) * std::max<size_t>((size_t)h->nmol * h->nblk * HX_MAX_DIIS, 2 * HX_SCF_GRID_MAX)));
+    // balanced schedules: blocks per molecule in proportion to its work
+    {
+        const int n = h->nmol;
+        std::vector<int> st((size_t)SK_COUNT * (n + 1));
+        h->sched.nmol = n;
+        h->sched.vmax = 0;
+        for (int k = 0; k < SK_COUNT; ++k) {
+            long long acc = 0;
+            for (int mi = 0; mi < n; ++mi) {
+                const long long N = h->N[mi], o = h->o[mi], v = h->v[mi], ov = o * v;
+                long long work = 0;
+                switch (k) {
+                case SK_NN: work = N * N; break;
+                case SK_ZDO: work = N * (ov + o * o + v * v); break;
+                case SK_PAIR: work = ov * ov; break;
+                case SK_ONON: work = o * N * o * N; break;
+                case SK_FOCK: work = ov + v * v + o * o; break;
+                case SK_SETUP: work = ov + ov * ov + N * ov; break;
+                }
+                st[(size_t)k * (n + 1) + mi] = (int)acc;
+                if (k == SK_UP) acc += hx_units((int)o, (int)v, true);
+                else if (k == SK_FULL) acc += hx_units((int)o, (int)v, false);
+                else acc += (work + HX_EW_CHUNK - 1) / HX_EW_CHUNK;
+                if (acc > INT32_MAX / 2) { hx_set_error("batch too large for one launch"); return HX_ERR_ARG; }
+                h->sched.vmax = std::max(h->sched.vmax, (int)v);
+            }
+            st[(size_t)k * (n + 1) + n] = (int)acc;
+            h->sched.blocks[k] = acc;
+        }
+        HX_CU(cudaMalloc(&h->d_sched, sizeof(int) * st.size()));
+        HX_CU(cudaMemcpy(h->d_sched, st.data(), sizeof(int) * st.size(), cudaMemcpyHostToDevice));
+        for (int k = 0; k < SK_COUNT; ++k) h->sched.start[k] = h->d_sched + (size_t)k * (n + 1);
+        for (int kk = 0; kk < 3; ++kk) h->unit_smem[kk] = hx_unit_smem(h->o.data(), h->v.data(), n, kk);
+        const size_t mx = std::max(h->unit_smem[0], std::max(h->unit_smem[1], h->unit_smem[2]));
+        if (mx > 227 * 1024) { hx_set_error("pair units need %zu bytes of shared memory", mx); return HX_ERR_ARG; }
+        HX_CU(hx_unit_kernels_init(mx));
+    }
+    HX_CU(cudaMalloc(&h->d_part, sizeof(double) * std::max<size_t>((size_t)h->sched.blocks[SK_UP] * HX_PART_STRIDE,
+                                                                   2 * HX_SCF_GRID_MAX)));
     for (int ph = 0; ph < PH_COUNT; ++ph) HX_CU(cudaMalloc(&h->d_act_ph[ph], sizeof(int) * h->nmol));
     HX_CU(cudaMalloc(&h->d_gate, sizeof(double) * h->nmol));
     h->gate.assign(h->nmol, 0.0);
@@ -619,7 +650,7 @@ int hx_ccsd_create(const hx_ppp_model *m, const hx_cc_params *p, hx_ccsd **out)
 static int cc_setup(hx_ccsd *h, int guess)
 {
     // Bov0, D1, D2; then G.Bov0, gov = Bov0^T G Bov0; then Lov and the guess
-    HX_CU(hx_ew_setup(h->d_cc, h->d_active, h->nmol, h->maxw_oNoN, guess, h->st));
+    HX_CU(hx_ew_setup(h->d_cc, h->d_active, h->sched, h->st));
     Group g1, g2;
     for (int mi = 0; mi < h->nmol; ++mi) {
         const CCMol &m = h->cc[mi];
@@ -631,7 +662,7 @@ static int cc_setup(hx_ccsd *h, int guess)
     HX_TRY(upload_group(g2));
     HX_CU(hx_tgemm_f64_launch(g1.d, (int)g1.h.size(), g1.tiles, h->d_active, h->st));
     HX_CU(hx_tgemm_f64_launch(g2.d, (int)g2.h.size(), g2.tiles, h->d_active, h->st));
-    HX_CU(hx_ew_setup2(h->d_cc, h->d_active, h->nmol, h->maxw_pair, guess, h->st));
+    HX_CU(hx_ew_setup2(h->d_cc, h->d_active, h->sched, guess, h->st));
     HX_CU(cudaStreamSynchronize(h->st));
     cudaFree(g1.d);
     cudaFree(g2.d);
@@ -724,23 +755,22 @@ int hx_ccsd_init(hx_ccsd *h)
 static int iteration_body(hx_ccsd *h, double eps)
 {
     if (eps != h->gate_eps) { h->gate_eps = eps; HX_TRY(upload_masks(h)); }
-    const int nm = h->nmol;
     auto &P = h->plan;
     int k = 0;
-    HX_CU(hx_ew_dress_init(h->d_cc, h->d_active, nm, h->maxw_nn, h->st));
+    HX_CU(hx_ew_dress_init(h->d_cc, h->d_active, h->sched, h->st));
     HX_TRY(run_group(h, P[k++]));                                    // dress X, Y
     HX_TRY(run_group(h, P[k++]));                                    // Pm
-    HX_CU(hx_ew_dress_fock(h->d_cc, h->d_active, nm, h->maxw_nn, h->st));
+    HX_CU(hx_ew_dress_fock(h->d_cc, h->d_active, h->sched, h->st));
     HX_TRY(run_group(h, P[k++]));                                    // W1 = H2 Y
     HX_TRY(run_group(h, P[k++]));                                    // Fd = X^T W1
-    HX_CU(hx_ew_zdo_products(h->d_cc, h->d_active, nm, h->maxw_oNoN, h->st));
+    HX_CU(hx_ew_zdo_products(h->d_cc, h->d_active, h->sched, h->st));
     HX_TRY(run_group(h, P[k++]));                                    // G B
-    HX_CU(hx_ew_make_u(h->d_cc, h->d_active, nm, h->maxw_pair, h->st));
-    HX_CU(hx_ew_fock_blocks(h->d_cc, h->d_active, nm, h->maxw_ov, h->st));
+    HX_CU(hx_ew_make_u(h->d_cc, h->d_active, h->sched, h->unit_smem[0], h->st));
+    HX_CU(hx_ew_fock_blocks(h->d_cc, h->d_active, h->sched, h->st));
     HX_TRY(run_group(h, P[k++]));                                    // lead
     HX_TRY(run_group(h, P[k++]));                                    // lad_a
     HX_TRY(run_group(h, P[k++]));                                    // lad_b
-    HX_CU(hx_ew_gamma_scale(h->d_cc, h->d_active, nm, h->maxw_oNoN, h->st));
+    HX_CU(hx_ew_gamma_scale(h->d_cc, h->d_active, h->sched, h->st));
     HX_TRY(run_group(h, P[k++]));                                    // lad_d
     HX_TRY(run_group(h, P[k++]));                                    // lad_e
     HX_TRY(run_group(h, P[k++]));                                    // w_d
@@ -750,7 +780,7 @@ static int iteration_body(hx_ccsd *h, double eps)
     HX_TRY(run_group(h, P[k++]));                                    // cint1
     HX_TRY(run_group(h, P[k++]));                                    // cint2
     HX_TRY(run_group(h, P[k++]));                                    // cterm
-    HX_CU(hx_ew_c_combine(h->d_cc, h->d_active, nm, h->maxw_pair, h->st));
+    HX_CU(hx_ew_c_combine(h->d_cc, h->d_active, h->sched, h->st));
     HX_TRY(run_group(h, P[k++]));                                    // dint1
     HX_TRY(run_group(h, P[k++]));                                    // dint2
     HX_TRY(run_group(h, P[k++]));                                    // dint3
@@ -758,17 +788,15 @@ static int iteration_body(hx_ccsd *h, double eps)
     HX_TRY(run_group(h, P[k++]));                                    // F'vv, F'oo
     HX_TRY(run_group(h, P[k++]));                                    // e1
     HX_TRY(run_group(h, P[k++]));                                    // e2
-    HX_CU(hx_ew_assemble(h->d_cc, h->d_active, nm, h->maxw_pair, h->st));
+    // (r2 += X2 + X2 pair-transposed is part of the step below)
     HX_TRY(run_group(h, P[k++]));                                    // singles: u F, U
     HX_TRY(run_group(h, P[k++]));                                    // UG
     HX_TRY(run_group(h, P[k++]));                                    // Vs
     HX_TRY(run_group(h, P[k++]));                                    // r1 += Vs Xv
     HX_TRY(run_group(h, P[k++]));                                    // r1 -= Boo UG
     const int use_diis = h->p.diis_enabled ? 1 : 0;
-    HX_CU(hx_step(h->d_cc, h->d_diis, h->d_active, nm, h->p.t1_step, h->p.t2_step, use_diis, h->p.projection_type,
-                  h->d_part, h->nblk, h->st));
-    if (use_diis) HX_CU(hx_diis(h->d_cc, h->d_diis, h->d_active, nm, h->d_gate, h->d_part, h->nblk, h->p.diis_steps, h->st));
-    HX_CU(hx_energy(h->d_cc, h->d_active, nm, h->d_part, h->nblk, h->st));
+    HX_CU(hx_tail(h->d_cc, h->d_diis, h->d_active, h->sched, h->unit_smem + 1, h->p.t1_step, h->p.t2_step,
+                  h->p.projection_type, use_diis, h->d_gate, h->d_part, h->st));
     return HX_OK;
 }
 
@@ -795,7 +823,7 @@ int hx_ccsd_iterate(hx_ccsd *h, int32_t iteration, double eps, double acc[5])
 int hx_ccsd_energy(hx_ccsd *h, double e[5])
 {
     if (!h || !h->initialized) { hx_set_error("hx_ccsd_energy before hx_ccsd_init"); return HX_ERR_STATE; }
-    HX_CU(hx_energy(h->d_cc, nullptr, h->nmol, h->d_part, h->nblk, h->st));
+    HX_CU(hx_energy(h->d_cc, h->d_diis, nullptr, h->sched, h->unit_smem[2], h->d_part, h->st));
     HX_TRY(fetch_results(h));
     if (e) { e[0] = h->res[2]; e[1] = h->res[3]; e[2] = h->res[4]; e[3] = h->res[5]; e[4] = 0.0; }
     return HX_OK;
@@ -1150,6 +1178,7 @@ void hx_ccsd_destroy(hx_ccsd *h)
     for (int ph = 0; ph < PH_COUNT; ++ph) cudaFree(h->d_act_ph[ph]);
     cudaFree(h->d_gate);
     cudaFree(h->d_part);
+    cudaFree(h->d_sched);
     if (h->st) cudaStreamDestroy(h->st);
     delete h;
 }

@@ -9,21 +9,23 @@ cudaError_t hx_tgemm_f64_launch(const TgemmDesc *d_descs, int n, long long total
 cudaError_t hx_scf_launch(const ScfMol *d_mols, int nmol, int nmax, const ScfParams &p, double *d_gpart,
                           cudaStream_t s);
 
-cudaError_t hx_ew_dress_init(const CCMol *m, const int *act, int nmol, long long maxw, cudaStream_t s);
-cudaError_t hx_ew_dress_fock(const CCMol *m, const int *act, int nmol, long long maxw, cudaStream_t s);
-cudaError_t hx_ew_zdo_products(const CCMol *m, const int *act, int nmol, long long maxw, cudaStream_t s);
-cudaError_t hx_ew_make_u(const CCMol *m, const int *act, int nmol, long long maxw, cudaStream_t s);
-cudaError_t hx_ew_gamma_scale(const CCMol *m, const int *act, int nmol, long long maxw, cudaStream_t s);
-cudaError_t hx_ew_fock_blocks(const CCMol *m, const int *act, int nmol, long long maxw, cudaStream_t s);
-cudaError_t hx_ew_c_combine(const CCMol *m, const int *act, int nmol, long long maxw, cudaStream_t s);
-cudaError_t hx_ew_assemble(const CCMol *m, const int *act, int nmol, long long maxw, cudaStream_t s);
-cudaError_t hx_ew_setup(const CCMol *m, const int *act, int nmol, long long maxw, int guess, cudaStream_t s);
-cudaError_t hx_ew_setup2(const CCMol *m, const int *act, int nmol, long long maxw, int guess, cudaStream_t s);
-cudaError_t hx_step(const CCMol *m, const DiisMol *h, const int *act, int nmol, double s1, double s2,
-                    int use_diis, int proj, double *part, int nblk, cudaStream_t s);
-cudaError_t hx_diis(const CCMol *m, const DiisMol *h, const int *act, int nmol, const double *gate, double *part,
-                    int nblk, int nd_max, cudaStream_t s);
-cudaError_t hx_energy(const CCMol *m, const int *act, int nmol, double *part, int nblk, cudaStream_t s);
+cudaError_t hx_ew_dress_init(const CCMol *m, const int *act, const HxSched &S, cudaStream_t s);
+cudaError_t hx_ew_dress_fock(const CCMol *m, const int *act, const HxSched &S, cudaStream_t s);
+cudaError_t hx_ew_zdo_products(const CCMol *m, const int *act, const HxSched &S, cudaStream_t s);
+cudaError_t hx_ew_gamma_scale(const CCMol *m, const int *act, const HxSched &S, cudaStream_t s);
+cudaError_t hx_ew_fock_blocks(const CCMol *m, const int *act, const HxSched &S, cudaStream_t s);
+cudaError_t hx_ew_c_combine(const CCMol *m, const int *act, const HxSched &S, cudaStream_t s);
+cudaError_t hx_ew_setup(const CCMol *m, const int *act, const HxSched &S, cudaStream_t s);
+cudaError_t hx_ew_setup2(const CCMol *m, const int *act, const HxSched &S, int guess, cudaStream_t s);
+// pair-unit kernels: dynamic shared memory for kernel 0 (make_u), 1 (step and
+// push), 2 (amplitudes and energy); the attribute is raised once to the largest
+size_t hx_unit_smem(const int *o, const int *v, int nmol, int kernel);
+cudaError_t hx_unit_kernels_init(size_t smem_max);
+cudaError_t hx_ew_make_u(const CCMol *m, const int *act, const HxSched &S, size_t smem, cudaStream_t s);
+cudaError_t hx_tail(const CCMol *m, const DiisMol *h, const int *act, const HxSched &S, const size_t smem[2],
+                    double s1, double s2, int proj, int use_diis, const double *gate, double *part, cudaStream_t s);
+cudaError_t hx_energy(const CCMol *m, const DiisMol *h, const int *act, const HxSched &S, size_t smem, double *part,
+                      cudaStream_t s);
 
 // (T) triples (hx_triples.cu): ZDO pair products of the occupied and virtual
 // orbitals, then W, the energy partials and their ordered sum (out[0] = E[4],

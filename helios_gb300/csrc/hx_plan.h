@@ -54,9 +54,14 @@ struct CCMol {
 };
 
 // DIIS history of one molecule: nd slots of the amplitude vector (t1, t2) and
-// of the error vector (d1, 3*Omega2), each of length L = o*v + (o*v)^2, used
-// as a ring (slot = count % nd). gram is nd x nd in slot order; coef holds
-// HX_MAX_DIIS+1 doubles: the mixing coefficients and, last, how many to mix.
+// of the error vector (d1, 3*Omega2 or d2), used as a ring (slot = count % nd).
+// A vector holds what the reference's packed vectors hold, the singles and the
+// pairs (ia) <= (jb), blocked: t1 (o*v), then the v x v blocks [a][b] of the
+// occupied pairs i <= j in row-major order of that triangle, so
+// L = o*v + v*v*o(o+1)/2 (a diagonal block i = j carries both (ia,ib) and
+// (ib,ia), which are equal). gram is nd x nd in slot order; coef holds
+// HX_MAX_DIIS+2 doubles: the mixing coefficients by slot, then how many
+// vectors to mix (1: none, take the newest) and the newest slot.
 struct DiisMol {
     double *Ht, *He, *gram, *coef;
     int *count;
@@ -70,3 +75,42 @@ struct Group {
     TgemmDesc *d = nullptr;
     long long tiles = 0;
 };
+
+// ---------------------------------------------------------------- schedules
+// Launches over a batch give every molecule blocks in proportion to its work
+// (prefix sums of blocks per molecule, `start[nmol + 1]`), so molecules of 8
+// and of 160 sites finish together. Element-wise kinds cover HX_EW_CHUNK
+// elements per block; the pair-unit kinds cover one unit: the singles, or a
+// group of v x v pair blocks (i, j) of about HX_UNIT_ELEMS elements.
+#define HX_EW_CHUNK 2048
+#define HX_UNIT_ELEMS 1024
+#define HX_PART_STRIDE (2 + HX_MAX_DIIS)   // partials per unit: two maxima or sums, then DIIS dots
+
+enum { SK_NN, SK_ZDO, SK_PAIR, SK_ONON, SK_FOCK, SK_SETUP, SK_UP, SK_FULL, SK_COUNT };
+
+struct HxSched {
+    const int *start[SK_COUNT];    // device: first block of each molecule, then the total
+    long long blocks[SK_COUNT];    // host: the total
+    int nmol;
+    int vmax;                      // largest v of the batch (tile size of the pair-unit kernels)
+};
+
+__host__ __device__ inline int hx_unit_blocks(int v)   // v x v blocks per pair unit (1..64)
+{
+    const int g = HX_UNIT_ELEMS / (v * v);
+    return g < 1 ? 1 : (g > 64 ? 64 : g);
+}
+// doubles of shared memory one pair-unit tile takes ([block][a][b], rows of v + 1)
+__host__ __device__ inline long long hx_unit_tile(int o, int v)
+{
+    const long long t = (long long)hx_unit_blocks(v) * v * (v + 1);
+    return t > (long long)o * v ? t : (long long)o * v;      // the singles unit stages o*v values
+}
+// units of a molecule: the singles unit, then the upper-triangle (i <= j)
+// blocks (SK_UP) or all o*o blocks (SK_FULL) in groups of hx_unit_blocks(v)
+__host__ __device__ inline long long hx_units(int o, int v, bool upper)
+{
+    const long long nb = upper ? (long long)o * (o + 1) / 2 : (long long)o * o;
+    const int g = hx_unit_blocks(v);
+    return 1 + (nb + g - 1) / g;
+}
