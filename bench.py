@@ -276,6 +276,18 @@ def run_gb300(args):
                 "tensor_issued_frac_while_in_tc_gemm": tw["gemm_hw_flops"] / (tw["gemm_ms"] * 1e-3 * peak_t)
                 if tw["gemm_ms"] > 0 else None,
                 "tc_gemm_share_of_batch_time": tw["gemm_ms"] * 1e-3 / wsecs if wsecs > 0 else None}
+        # the headline batch again with the default tile shapes instead of the autotuner's table
+        cd = api.CoupledCluster(mols, api.Keywords(bond_alternation=0.1, accuracy=8, precision="mixed", guess=guess,
+                                                   tile_tuning="default"))
+        cd.initCC()
+        cd.solve_batch()
+        cd.initCC()
+        od = cd.solve_batch()
+        td = cd.timing()
+        cd.finalizeCC()
+        sd = (td["init_ms"] + td["solve_ms"]) / 1e3
+        extra["batch"][guess + "_guess"]["default_tiles"] = {
+            "seconds": sd, "molecules_per_s": args.batch / sd, "converged": int((od["status"] == 1).sum())}
         # the same batch on the plain FP64 path (one solve: it has no tensor-core warm-up)
         if args.fp64_compare:
             c64 = api.CoupledCluster(mols, api.Keywords(bond_alternation=0.1, accuracy=8, precision="fp64"))

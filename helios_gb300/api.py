@@ -50,7 +50,7 @@ class CCParams(ctypes.Structure):
                 ("check_stagnation", ctypes.c_int32), ("stagnation_threshold", ctypes.c_double),
                 ("stagnation_after", ctypes.c_int32), ("precision", ctypes.c_int32), ("guess", ctypes.c_int32),
                 ("mixed_switch", ctypes.c_double), ("mixed_patience", ctypes.c_int32),
-                ("mixed_check", ctypes.c_int32)]
+                ("mixed_check", ctypes.c_int32), ("tile_tuning", ctypes.c_int32), ("tile_force", ctypes.c_int32)]
 
 
 class HxError(RuntimeError):
@@ -77,10 +77,54 @@ def library():
                      "hx_ccsd_iterate", "hx_ccsd_energy", "hx_ccsd_solve", "hx_ccsd_solve_batch",
                      "hx_ccsd_get_amplitudes", "hx_ccsd_get_scf", "hx_ccsd_dims", "hx_ccsd_trace",
                      "hx_gemm", "hx_ccsd_timing", "hx_last_error", "hx_ccsd_set_model", "hx_ccsd_training_rows",
-                     "hx_mlp_nparam", "hx_mlp_predict", "hx_mlp_grad", "hx_mlp_train", "hx_ccsd_triples"):
+                     "hx_mlp_nparam", "hx_mlp_predict", "hx_mlp_grad", "hx_mlp_train", "hx_ccsd_triples",
+                     "hx_tile_table", "hx_tile_table_load", "hx_tile_variants", "hx_ccsd_tile_choices"):
             getattr(lib, name).restype = ctypes.c_int
         _lib = lib
+        if os.path.exists(TILE_TABLE_PATH):
+            load_tile_table(read_tile_table(TILE_TABLE_PATH))
     return _lib
+
+
+# ---------------------------------------------------------------- tile autotuner
+TILE_TABLE_PATH = os.path.join(_HERE, "data", "tile_table.json")
+TILE_TUNING = {"table": 0, "tune": 1, "default": 2}
+
+
+def tile_variants(mode: int):
+    """Output tile widths of the candidates of a precision mode (0..3: 3, 4, 5, 7 slices)."""
+    bn = (ctypes.c_int32 * 8)()
+    n = _check(library().hx_tile_variants(int(mode), bn, 8))
+    return [int(bn[k]) for k in range(n)]
+
+
+def tile_table():
+    """The process-wide tile table: list of (mode, group, size class N, size class work, variant)."""
+    n = _check(library().hx_tile_table(None, 0))
+    buf = (ctypes.c_int32 * max(5 * n, 1))()
+    _check(library().hx_tile_table(buf, n))
+    return [tuple(int(buf[5 * k + c]) for c in range(5)) for k in range(n)]
+
+
+def load_tile_table(entries):
+    """Merge entries (mode, group, size class N, size class work, variant) into the tile table."""
+    flat = np.ascontiguousarray(np.asarray(entries, dtype=np.int32).reshape(-1, 5))
+    _check(library().hx_tile_table_load(flat.ctypes.data_as(_c_i), int(flat.shape[0])))
+
+
+def read_tile_table(path):
+    import json
+    with open(path) as f:
+        d = json.load(f)
+    return [tuple(int(x) for x in e) for e in d["entries"]]
+
+
+def write_tile_table(path, entries, note=""):
+    import json
+    entries = sorted(tuple(int(x) for x in e) for e in entries)
+    with open(path, "w") as f:
+        json.dump({"format": "mode, plan group, ceil log2 of the widest N, floor log2 of the multiply-adds, variant",
+                   "note": note, "entries": [list(e) for e in entries]}, f, indent=0)
 
 
 def gemm(A, B, precision="fp64", reps=1):
@@ -174,6 +218,8 @@ class Keywords:
     mixed_switch: float = 1e-3                   # engine: residual where 3-slice hands over to 4-slice
     mixed_patience: int = 3                      # engine: non-improving iterations before the next phase
     mixed_check: str = "emulated"                # engine: convergence checks on "emulated" (7-slice) or "fp64"
+    tile_tuning: str = "table"                   # engine: tensor-core tile shapes "table", "tune" or "default"
+    tile_force: int = -1                         # engine: >= 0 forces one tile candidate in every mode
 
     def to_c(self) -> CCParams:
         p = CCParams()
@@ -201,6 +247,8 @@ class Keywords:
         p.mixed_switch = self.mixed_switch
         p.mixed_patience = self.mixed_patience
         p.mixed_check = {"emulated": 0, "fp64": 1}[self.mixed_check]
+        p.tile_tuning = TILE_TUNING[self.tile_tuning]
+        p.tile_force = int(self.tile_force)
         return p
 
 
@@ -341,6 +389,14 @@ class CoupledCluster:
         return {"init_ms": out[0], "solve_ms": out[1], "gemm_launches": int(out[2]), "gemm_ms": out[3],
                 "gemm_flops": out[4], "gemm_hw_flops": out[5], "device_bytes": int(out[6]),
                 "kernel_launches": int(out[7])}
+
+    def tile_choices(self):
+        """(variants [4, groups] of a mixed handle, milliseconds spent tuning at creation)."""
+        ms = ctypes.c_double()
+        n = _check(library().hx_ccsd_tile_choices(self._h, None, 0, ctypes.byref(ms)))
+        buf = (ctypes.c_int32 * max(n, 1))()
+        _check(library().hx_ccsd_tile_choices(self._h, buf, n, ctypes.byref(ms)))
+        return np.array([buf[k] for k in range(n)], dtype=np.int32).reshape(4, -1) if n else np.zeros((4, 0), np.int32), ms.value
 
     def cancel(self):
         library().hx_ccsd_cancel(self._h)

@@ -588,6 +588,8 @@ void hx_cc_params_default(hx_cc_params *p)
     p->mixed_switch = 1e-3;
     p->mixed_patience = 3;
     p->mixed_check = 0;
+    p->tile_tuning = 0;
+    p->tile_force = -1;
 }
 
 int hx_ccsd_create_batch(const hx_ppp_model *ms, int32_t n, const hx_cc_params *p, hx_ccsd **out)
@@ -598,6 +600,7 @@ int hx_ccsd_create_batch(const hx_ppp_model *ms, int32_t n, const hx_cc_params *
     if (p->diis_enabled && (p->diis_steps < 2 || p->diis_steps > HX_MAX_DIIS)) { hx_set_error("diis-steps outside 2..%d", HX_MAX_DIIS); return HX_ERR_ARG; }
     if (p->precision != HX_PRECISION_FP64 && p->precision != HX_PRECISION_MIXED) { hx_set_error("unknown precision mode"); return HX_ERR_ARG; }
     if (p->mixed_check != 0 && p->mixed_check != 1) { hx_set_error("mixed_check must be 0 (7-slice emulated FP64) or 1 (FP64)"); return HX_ERR_ARG; }
+    if (p->tile_tuning < 0 || p->tile_tuning > 2 || p->tile_force < -1) { hx_set_error("tile_tuning must be 0, 1 or 2 and tile_force >= -1"); return HX_ERR_ARG; }
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) { hx_set_error("no CUDA device"); return HX_ERR_CUDA; }
     hx_ccsd *h = new hx_ccsd();
@@ -634,7 +637,7 @@ int hx_ccsd_create_batch(const hx_ppp_model *ms, int32_t n, const hx_cc_params *
         if (rc < 0) { hx_ccsd_destroy(h); return rc; }
     }
     if (p->precision == HX_PRECISION_MIXED) {
-        rc = tc::create(&h->tce, h->plan, h->st);
+        rc = tc::create(&h->tce, h->plan, h->st, p->tile_tuning, p->tile_force);
         if (rc < 0) { hx_ccsd_destroy(h); return rc; }
     }
     if (cudaStreamSynchronize(h->st) != cudaSuccess) { hx_set_error("set-up failed"); hx_ccsd_destroy(h); return HX_ERR_CUDA; }
@@ -1322,3 +1325,26 @@ int hx_last_error(char *buf, size_t len)
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- tile autotuner
+extern "C" int hx_tile_table(int32_t *entries, int32_t cap) { return tc::table_get(entries, cap); }
+
+extern "C" int hx_tile_table_load(const int32_t *entries, int32_t n)
+{
+    if (n < 0 || (n > 0 && !entries)) { hx_set_error("hx_tile_table_load: bad arguments"); return HX_ERR_ARG; }
+    return tc::table_load(entries, n);
+}
+
+extern "C" int hx_tile_variants(int32_t mode, int32_t *bn, int32_t cap)
+{
+    const int n = tc::variants(mode, bn, cap);
+    if (n < 0) hx_set_error("hx_tile_variants: mode %d outside 0..3", mode);
+    return n;
+}
+
+extern "C" int hx_ccsd_tile_choices(hx_ccsd *h, int32_t *var, int32_t cap, double *tune_ms)
+{
+    if (!h) { hx_set_error("NULL handle"); return HX_ERR_ARG; }
+    if (tune_ms) *tune_ms = tc::tune_ms(h->tce);
+    return h->tce ? tc::choices(h->tce, var, cap) : 0;
+}

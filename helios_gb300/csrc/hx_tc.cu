@@ -42,8 +42,12 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <array>
+#include <chrono>
 #include <climits>
+#include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <vector>
 
@@ -745,6 +749,52 @@ __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restri
     }
 }
 
+// ------------------------------------------------------------------ tile-shape candidates
+// Every precision mode has a few configurations that differ only in the
+// output tile width BN (with the pipeline depth, staging strip and epilogue
+// warps that fit it); slices, slice pairs, exact classes, k-block depth and
+// chunk length are the mode's own, so every candidate forms the same sums.
+// Narrow tiles waste less on the thin operands of small molecules; wide ones
+// reuse each A tile over more columns. The autotuner (choose_variant) picks one
+// per plan group, precision mode and size class.
+using Low64 = Cfg<3, 3, 1, 64, 2, 8, 8, 64, 64>;
+using Low32 = Cfg<3, 3, 1, 32, 3, 8, 4, 64, 64>;
+using Mid48 = Cfg<4, 3, 2, 48, 2, 6, 8, 64, 32>;
+using Mid32 = Cfg<4, 3, 2, 32, 2, 6, 4, 64, 64>;
+using High32 = Cfg<5, 4, 3, 32, 3, 8, 4, 32, 64>;
+using Exact16 = Cfg<7, 6, 5, 16, 3, 6, 4, 32, 32>;
+
+struct Variant {
+    int S, BN, BK, products, smem;
+    cudaError_t (*attr)();
+    void (*launch)(unsigned grid, cudaStream_t s, const TcDesc *d, int nd, long long tiles, const int *act, int *err);
+};
+template <class C>
+static cudaError_t attr_tc()
+{
+    return cudaFuncSetAttribute(tc_gemm<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES);
+}
+template <class C>
+static void launch_tc(unsigned grid, cudaStream_t s, const TcDesc *d, int nd, long long tiles, const int *act, int *err)
+{
+    tc_gemm<C><<<grid, C::NTHREADS, C::SMEM_BYTES, s>>>(d, nd, tiles, act, err);
+}
+template <class C>
+static Variant variant()
+{
+    return Variant{C::S, C::BN, C::BK, C::PRODUCTS, C::SMEM_BYTES, &attr_tc<C>, &launch_tc<C>};
+}
+constexpr int MAX_VARIANTS = 3;
+static const int kNumVariants[4] = {3, 3, 2, 2};
+static const Variant &variant_of(int mode, int k)
+{
+    static const Variant table[4][MAX_VARIANTS] = {{variant<Low>(), variant<Low64>(), variant<Low32>()},
+                                                   {variant<Mid>(), variant<Mid48>(), variant<Mid32>()},
+                                                   {variant<High>(), variant<High32>(), variant<High32>()},
+                                                   {variant<Exact>(), variant<Exact16>(), variant<Exact16>()}};
+    return table[mode][k];
+}
+
 // ------------------------------------------------------------------ host side
 struct PrepList {                    // operands sliced by one pair of launches
     std::vector<PrepDesc> h;
@@ -752,27 +802,28 @@ struct PrepList {                    // operands sliced by one pair of launches
     long long work = 0, rows = 0;
 };
 
-struct SubGroup {
+struct SubGroup {                    // one plan group in one precision mode and tile variant
+    int var = 0;
     std::vector<TcDesc> tcd;         // tensor-core problems
     TcDesc *d_tcd = nullptr;
-    PrepList var, fixed;             // operands sliced every run / once per initialisation
+    PrepList var_ops, fixed;         // operands sliced every run / once per initialisation
+    __nv_bfloat16 *fixed_buf = nullptr;   // slices of the constant operands (persistent)
+    int *fixed_rexp = nullptr;
     int fixed_gen = -1;              // generation the fixed slices were made for
     long long tiles = 0;
-    Group fp64;                       // problems too small for the tensor cores
+    Group fp64;                      // problems too small for the tensor cores
 };
 
-struct Mode {                        // one precision: descriptors of every plan group
-    int S = 0, BN = 0, BK = 64, products = 0, smem = 0;
-    __nv_bfloat16 *fixed = nullptr;  // slices of the constant operands (persistent)
-    int *fixed_rexp = nullptr;
-    std::vector<SubGroup> groups;    // one per plan group, same order
+struct Mode {                        // one precision: one SubGroup per plan group, same order
+    std::vector<SubGroup> groups;
 };
 
 struct Engine {
     __nv_bfloat16 *scratch = nullptr;   // slices of the variable operands (shared by groups and modes)
+    size_t scratch_elems = 0;
     int *rexp = nullptr;
     int *d_err = nullptr;
-    Mode mode[4];                        // 0 = LOW, 1 = MID, 2 = HIGH, 3 = EXACT (3, 4, 6, 7 slices)
+    Mode mode[4];                        // 0 = LOW, 1 = MID, 2 = HIGH, 3 = EXACT (3, 4, 5, 7 slices)
     std::vector<const Group *> keys;
     bool profile = false;
     int generation = 0;
@@ -781,6 +832,7 @@ struct Engine {
     std::vector<cudaEvent_t> pool;
     double tot[4] = {0, 0, 0, 0};
     int nsm = 152;                       // SMs of the device: CTAs of a persistent launch
+    double tune_ms = 0.0;                // time spent timing candidates at creation
 };
 
 static cudaEvent_t take_event(Engine *e)
@@ -876,113 +928,258 @@ static const double kMinTcWork = 1.0e4;
 
 static bool on_tc(const TgemmDesc &t) { return (double)t.batch * t.M * t.N * t.K >= kMinTcWork; }
 
-// Descriptors, tensor maps and slice storage of one precision mode.
-static int build_mode(Engine *e, Mode &md, const std::vector<Group> &plan, size_t var_elems_cap)
+
+static void free_sub(SubGroup &sg)
 {
-    const int S = md.S, BN = md.BN;
+    cudaFree(sg.d_tcd);
+    cudaFree(sg.var_ops.d);
+    cudaFree(sg.fixed.d);
+    cudaFree(sg.fp64.d);
+    cudaFree(sg.fixed_buf);
+    cudaFree(sg.fixed_rexp);
+    sg = SubGroup();
+}
+
+// Slice elements (and padded rows) of a group's variable operands in one variant.
+static void var_need(const Group &g, const Variant &V, size_t &elems, size_t &rows)
+{
+    elems = rows = 0;
+    for (const TgemmDesc &t : g.h) {
+        if (!on_tc(t)) continue;
+        const size_t Kp = rup(t.K, KPAD), Ma = rup(t.M, BM), Nb = rup(t.N, V.BN);
+        if (!t.a_const) { elems += (size_t)V.S * t.batch * Ma * Kp; rows += (size_t)t.batch * Ma; }
+        if (!t.b_const) { elems += (size_t)V.S * t.batch * Nb * Kp; rows += (size_t)t.batch * Nb; }
+    }
+}
+
+// Descriptors, tensor maps and constant-slice storage of one plan group in
+// one precision mode and tile variant.
+static int build_sub(Engine *e, int mode, int var, const Group &g, SubGroup &sg)
+{
+    const Variant &V = variant_of(mode, var);
+    const int S = V.S, BN = V.BN;
+    sg = SubGroup();
+    sg.var = var;
     size_t fneed = 0, frows = 0;
-    for (const Group &g : plan)
-        for (const TgemmDesc &t : g.h) {
-            if (!on_tc(t)) continue;
-            const size_t Kp = rup(t.K, KPAD), Ma = rup(t.M, BM), Nb = rup(t.N, BN);
-            if (t.a_const) { fneed += (size_t)S * t.batch * Ma * Kp; frows += (size_t)t.batch * Ma; }
-            if (t.b_const) { fneed += (size_t)S * t.batch * Nb * Kp; frows += (size_t)t.batch * Nb; }
-        }
-    if ((fneed && cudaMalloc(&md.fixed, fneed * sizeof(__nv_bfloat16)) != cudaSuccess) ||
-        (frows && cudaMalloc(&md.fixed_rexp, frows * sizeof(int)) != cudaSuccess)) {
+    for (const TgemmDesc &t : g.h) {
+        if (!on_tc(t)) continue;
+        const size_t Kp = rup(t.K, KPAD), Ma = rup(t.M, BM), Nb = rup(t.N, BN);
+        if (t.a_const) { fneed += (size_t)S * t.batch * Ma * Kp; frows += (size_t)t.batch * Ma; }
+        if (t.b_const) { fneed += (size_t)S * t.batch * Nb * Kp; frows += (size_t)t.batch * Nb; }
+    }
+    if ((fneed && cudaMalloc(&sg.fixed_buf, fneed * sizeof(__nv_bfloat16)) != cudaSuccess) ||
+        (frows && cudaMalloc(&sg.fixed_rexp, frows * sizeof(int)) != cudaSuccess)) {
         hx_set_error("cudaMalloc of %zu bytes of constant slices failed", fneed * 2 + frows * 4);
         return HX_ERR_NOMEM;
     }
-    size_t foff = 0, froff = 0;
-    for (const Group &g : plan) {
-        SubGroup sg;
-        size_t off = 0, roff = 0;
-        long long tiles = 0;
-        for (const TgemmDesc &t : g.h) {
-            if (!on_tc(t)) { sg.fp64.h.push_back(t); continue; }
-            TcDesc d;
-            memset(&d, 0, sizeof(d));
-            d.batch = t.batch; d.M = t.M; d.N = t.N; d.K = t.K;
-            d.Mp = (int)rup(t.M, BM); d.Np = (int)rup(t.N, BN); d.Kp = (int)rup(t.K, KPAD);
-            d.Mi = t.Mi; d.Ni = t.Ni;
-            for (int k = 0; k < 5; ++k) d.c[k] = t.c[k];
-            d.alpha = t.alpha; d.beta = t.beta; d.C = t.C; d.mol = t.mol;
-            d.tiles_m = d.Mp / BM; d.tiles_n = d.Np / BN;
-            // long K over few output tiles: cut K into slices that fill the GPU
-            const int nkb = d.Kp / md.BK, n64 = d.Kp / KPAD;
-            const long long out_tiles = (long long)d.batch * d.tiles_m * d.tiles_n;
-            int ks = 1;
-            if (t.beta == 1.0 && out_tiles < 152 && n64 >= 16) ks = (int)std::min<long long>((152 + out_tiles - 1) / out_tiles, n64 / 8);
-            d.kb_per = (nkb + ks - 1) / ks;
-            d.ksplit = (nkb + d.kb_per - 1) / d.kb_per;
-            d.tile_start = tiles;
-            tiles += out_tiles * d.ksplit;
-            const size_t asz = (size_t)S * d.batch * d.Mp * d.Kp;
-            const size_t bsz = (size_t)S * d.batch * d.Np * d.Kp;
-            __nv_bfloat16 *abuf, *bbuf;
-            int *aexp, *bexp;
-            if (t.a_const) { abuf = md.fixed + foff; foff += asz; aexp = md.fixed_rexp + froff; froff += (size_t)t.batch * d.Mp; }
-            else { abuf = e->scratch + off; off += asz; aexp = e->rexp + roff; roff += (size_t)t.batch * d.Mp; }
-            if (t.b_const) { bbuf = md.fixed + foff; foff += bsz; bexp = md.fixed_rexp + froff; froff += (size_t)t.batch * d.Np; }
-            else { bbuf = e->scratch + off; off += bsz; bexp = e->rexp + roff; roff += (size_t)t.batch * d.Np; }
-            if (off > var_elems_cap) { hx_set_error("tensor-core scratch overflow"); return HX_ERR_STATE; }
-            int rc = make_map(&d.mapA, abuf, (long long)S * d.batch * d.Mp, d.Kp, BM, md.BK);
-            if (rc == HX_OK) rc = make_map(&d.mapB, bbuf, (long long)S * d.batch * d.Np, d.Kp, BN, md.BK);
-            if (rc < 0) return rc;
-            PrepDesc pa, pb;
-            memset(&pa, 0, sizeof(pa));
-            pa.src = t.A; pa.dst = abuf; pa.batch = t.batch; pa.R = t.M; pa.K = t.K;
-            pa.Rp = d.Mp; pa.Kp = d.Kp; pa.Ri = t.Mi; pa.Ki = t.Ki; pa.mol = t.mol;
-            pa.s[0] = t.a[0]; pa.s[1] = t.a[1]; pa.s[2] = t.a[2]; pa.s[3] = t.a[3]; pa.s[4] = t.a[4];
-            pa.rexp = aexp;
-            d.expA = aexp;
-            pb = pa;
-            pb.src = t.B; pb.dst = bbuf; pb.R = t.N; pb.Rp = d.Np; pb.Ri = t.Ni;
-            pb.s[0] = t.b[0]; pb.s[1] = t.b[1]; pb.s[2] = t.b[2]; pb.s[3] = t.b[3]; pb.s[4] = t.b[4];
-            pb.rexp = bexp;
-            d.expB = bexp;
-            auto add = [&](PrepList &L, PrepDesc p) {
-                p.work_start = L.work;
-                p.row_start = L.rows;
-                p.rfast = prep_rfast(p);
-                L.work += (long long)p.batch * ((p.Rp + PT_R - 1) / PT_R) * (p.Kp / PT_K);
-                L.rows += (long long)p.batch * p.Rp;
-                L.h.push_back(p);
-            };
-            add(t.a_const ? sg.fixed : sg.var, pa);
-            add(t.b_const ? sg.fixed : sg.var, pb);
-            sg.tcd.push_back(d);
+    size_t off = 0, roff = 0, foff = 0, froff = 0;
+    long long tiles = 0;
+    for (const TgemmDesc &t : g.h) {
+        if (!on_tc(t)) { sg.fp64.h.push_back(t); continue; }
+        TcDesc d;
+        memset(&d, 0, sizeof(d));
+        d.batch = t.batch; d.M = t.M; d.N = t.N; d.K = t.K;
+        d.Mp = (int)rup(t.M, BM); d.Np = (int)rup(t.N, BN); d.Kp = (int)rup(t.K, KPAD);
+        d.Mi = t.Mi; d.Ni = t.Ni;
+        for (int k = 0; k < 5; ++k) d.c[k] = t.c[k];
+        d.alpha = t.alpha; d.beta = t.beta; d.C = t.C; d.mol = t.mol;
+        d.tiles_m = d.Mp / BM; d.tiles_n = d.Np / BN;
+        // long K over few output tiles: cut K into slices that fill the GPU
+        const int nkb = d.Kp / V.BK, n64 = d.Kp / KPAD;
+        const long long out_tiles = (long long)d.batch * d.tiles_m * d.tiles_n;
+        int ks = 1;
+        if (t.beta == 1.0 && out_tiles < e->nsm && n64 >= 16)
+            ks = (int)std::min<long long>((e->nsm + out_tiles - 1) / out_tiles, n64 / 8);
+        d.kb_per = (nkb + ks - 1) / ks;
+        d.ksplit = (nkb + d.kb_per - 1) / d.kb_per;
+        d.tile_start = tiles;
+        tiles += out_tiles * d.ksplit;
+        const size_t asz = (size_t)S * d.batch * d.Mp * d.Kp;
+        const size_t bsz = (size_t)S * d.batch * d.Np * d.Kp;
+        __nv_bfloat16 *abuf, *bbuf;
+        int *aexp, *bexp;
+        if (t.a_const) { abuf = sg.fixed_buf + foff; foff += asz; aexp = sg.fixed_rexp + froff; froff += (size_t)t.batch * d.Mp; }
+        else { abuf = e->scratch + off; off += asz; aexp = e->rexp + roff; roff += (size_t)t.batch * d.Mp; }
+        if (t.b_const) { bbuf = sg.fixed_buf + foff; foff += bsz; bexp = sg.fixed_rexp + froff; froff += (size_t)t.batch * d.Np; }
+        else { bbuf = e->scratch + off; off += bsz; bexp = e->rexp + roff; roff += (size_t)t.batch * d.Np; }
+        if (off > e->scratch_elems) { hx_set_error("tensor-core scratch overflow"); return HX_ERR_STATE; }
+        int rc = make_map(&d.mapA, abuf, (long long)S * d.batch * d.Mp, d.Kp, BM, V.BK);
+        if (rc == HX_OK) rc = make_map(&d.mapB, bbuf, (long long)S * d.batch * d.Np, d.Kp, BN, V.BK);
+        if (rc < 0) return rc;
+        PrepDesc pa, pb;
+        memset(&pa, 0, sizeof(pa));
+        pa.src = t.A; pa.dst = abuf; pa.batch = t.batch; pa.R = t.M; pa.K = t.K;
+        pa.Rp = d.Mp; pa.Kp = d.Kp; pa.Ri = t.Mi; pa.Ki = t.Ki; pa.mol = t.mol;
+        pa.s[0] = t.a[0]; pa.s[1] = t.a[1]; pa.s[2] = t.a[2]; pa.s[3] = t.a[3]; pa.s[4] = t.a[4];
+        pa.rexp = aexp;
+        d.expA = aexp;
+        pb = pa;
+        pb.src = t.B; pb.dst = bbuf; pb.R = t.N; pb.Rp = d.Np; pb.Ri = t.Ni;
+        pb.s[0] = t.b[0]; pb.s[1] = t.b[1]; pb.s[2] = t.b[2]; pb.s[3] = t.b[3]; pb.s[4] = t.b[4];
+        pb.rexp = bexp;
+        d.expB = bexp;
+        auto add = [&](PrepList &L, PrepDesc p) {
+            p.work_start = L.work;
+            p.row_start = L.rows;
+            p.rfast = prep_rfast(p);
+            L.work += (long long)p.batch * ((p.Rp + PT_R - 1) / PT_R) * (p.Kp / PT_K);
+            L.rows += (long long)p.batch * p.Rp;
+            L.h.push_back(p);
+        };
+        add(t.a_const ? sg.fixed : sg.var_ops, pa);
+        add(t.b_const ? sg.fixed : sg.var_ops, pb);
+        sg.tcd.push_back(d);
+    }
+    sg.tiles = tiles;
+    if (!sg.tcd.empty()) {
+        if (cudaMalloc(&sg.d_tcd, sizeof(TcDesc) * sg.tcd.size()) != cudaSuccess) {
+            hx_set_error("descriptor allocation failed");
+            return HX_ERR_NOMEM;
         }
-        sg.tiles = tiles;
-        if (!sg.tcd.empty()) {
-            if (cudaMalloc(&sg.d_tcd, sizeof(TcDesc) * sg.tcd.size()) != cudaSuccess) {
+        cudaMemcpy(sg.d_tcd, sg.tcd.data(), sizeof(TcDesc) * sg.tcd.size(), cudaMemcpyHostToDevice);
+        for (PrepList *L : {&sg.var_ops, &sg.fixed}) {
+            if (L->h.empty()) continue;
+            if (cudaMalloc(&L->d, sizeof(PrepDesc) * L->h.size()) != cudaSuccess) {
                 hx_set_error("descriptor allocation failed");
                 return HX_ERR_NOMEM;
             }
-            cudaMemcpy(sg.d_tcd, sg.tcd.data(), sizeof(TcDesc) * sg.tcd.size(), cudaMemcpyHostToDevice);
-            for (PrepList *L : {&sg.var, &sg.fixed}) {
-                if (L->h.empty()) continue;
-                if (cudaMalloc(&L->d, sizeof(PrepDesc) * L->h.size()) != cudaSuccess) {
-                    hx_set_error("descriptor allocation failed");
-                    return HX_ERR_NOMEM;
-                }
-                cudaMemcpy(L->d, L->h.data(), sizeof(PrepDesc) * L->h.size(), cudaMemcpyHostToDevice);
-            }
+            cudaMemcpy(L->d, L->h.data(), sizeof(PrepDesc) * L->h.size(), cudaMemcpyHostToDevice);
         }
-        if (!sg.fp64.h.empty()) {
-            sg.fp64.tiles = hx_tgemm_f64_prepare(sg.fp64.h.data(), (int)sg.fp64.h.size());
-            cudaMalloc(&sg.fp64.d, sizeof(TgemmDesc) * sg.fp64.h.size());
-            cudaMemcpy(sg.fp64.d, sg.fp64.h.data(), sizeof(TgemmDesc) * sg.fp64.h.size(), cudaMemcpyHostToDevice);
-        } else {
-            sg.fp64.d = nullptr;
-            sg.fp64.tiles = 0;
+    }
+    if (!sg.fp64.h.empty()) {
+        sg.fp64.tiles = hx_tgemm_f64_prepare(sg.fp64.h.data(), (int)sg.fp64.h.size());
+        if (cudaMalloc(&sg.fp64.d, sizeof(TgemmDesc) * sg.fp64.h.size()) != cudaSuccess) {
+            hx_set_error("descriptor allocation failed");
+            return HX_ERR_NOMEM;
         }
-        md.groups.push_back(std::move(sg));
+        cudaMemcpy(sg.fp64.d, sg.fp64.h.data(), sizeof(TgemmDesc) * sg.fp64.h.size(), cudaMemcpyHostToDevice);
     }
     return HX_OK;
 }
 
-int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s)
+// One plan group in its mode and variant: slice the operands (the constant
+// ones once per initialisation), then the persistent tcgen05 GEMM.
+static cudaError_t run_sub(Engine *e, SubGroup &sg, int mode, const int *d_active, cudaStream_t s)
+{
+    const Variant &V = variant_of(mode, sg.var);
+    if (sg.fp64.tiles > 0) {
+        cudaError_t r = hx_tgemm_f64_launch(sg.fp64.d, (int)sg.fp64.h.size(), sg.fp64.tiles, d_active, s);
+        if (r != cudaSuccess) return r;
+    }
+    if (sg.tiles == 0) return cudaSuccess;
+    cudaError_t r = cudaSuccess;
+    // constant slices are made once per initialisation, for every molecule
+    // (molecules enter a mode at different iterations)
+    if (sg.fixed_gen != e->generation) {
+        if ((r = prep_launch(sg.fixed.d, (int)sg.fixed.h.size(), sg.fixed.work, sg.fixed.rows, V.S, nullptr, s)) != cudaSuccess)
+            return r;
+        sg.fixed_gen = e->generation;
+    }
+    if ((r = prep_launch(sg.var_ops.d, (int)sg.var_ops.h.size(), sg.var_ops.work, sg.var_ops.rows, V.S, d_active, s)) !=
+        cudaSuccess)
+        return r;
+    hx_count_launches(1);
+    Engine::Pending pend{};
+    if (e->profile) {
+        pend.a = take_event(e);
+        pend.b = take_event(e);
+        for (const TcDesc &d : sg.tcd) {
+            pend.flops += 2.0 * d.batch * (double)d.M * d.N * d.K;
+            pend.hwflops += 2.0 * d.batch * (double)d.Mp * d.Np * d.Kp * V.products;
+        }
+        cudaEventRecord(pend.a, s);
+    }
+    // persistent: one CTA per SM (shared memory allows one), each looping over tiles
+    const unsigned grid = (unsigned)std::min<long long>(sg.tiles, e->nsm);
+    V.launch(grid, s, sg.d_tcd, (int)sg.tcd.size(), sg.tiles, d_active, e->d_err);
+    r = cudaGetLastError();
+    if (e->profile) {
+        cudaEventRecord(pend.b, s);
+        e->pending.push_back(pend);
+    }
+    return r;
+}
+
+// ------------------------------------------------------------------ autotuner
+// The tile variant of each (precision mode, plan group, size class): size
+// class = (ceil log2 of the widest output column count N, floor log2 of the
+// group's multiply-adds). Choices live in one process-wide table, filled from
+// a shipped table (hx_tile_table_load) or by timing every candidate on the
+// handle's own contraction shapes at creation (tuning = 1, on a table miss).
+using TileKey = std::array<int, 4>;
+static std::mutex g_tile_mu;
+static std::map<TileKey, int> g_tile_table;
+
+static TileKey tile_key(int mode, int gi, const Group &g)
+{
+    long long maxn = 0;
+    double work = 0.0;
+    for (const TgemmDesc &t : g.h) {
+        if (!on_tc(t)) continue;
+        maxn = std::max<long long>(maxn, t.N);
+        work += (double)t.batch * t.M * t.N * t.K;
+    }
+    int nb = 0;
+    while ((1LL << nb) < maxn) ++nb;
+    return TileKey{mode, gi, nb, work > 0.0 ? (int)std::floor(std::log2(work)) : 0};
+}
+
+// Time every candidate of one group (one warm-up run that also slices the
+// constant operands, then the mean of three runs, CUDA events on s) and
+// return the fastest; *ms gets the time spent.
+static int tune_group(Engine *e, int mode, const Group &g, cudaStream_t s, int *best, double *spent)
+{
+    *best = 0;
+    float best_ms = 1e30f;
+    cudaEvent_t a, b;
+    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
+        hx_set_error("autotuner: cudaEventCreate failed");
+        return HX_ERR_CUDA;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    int rc = HX_OK;
+    for (int v = 0; v < kNumVariants[mode] && rc == HX_OK; ++v) {
+        SubGroup sg;
+        rc = build_sub(e, mode, v, g, sg);
+        if (rc == HX_OK && sg.tiles == 0) { free_sub(sg); break; }
+        cudaError_t ce = cudaSuccess;
+        if (rc == HX_OK) ce = run_sub(e, sg, mode, nullptr, s);
+        if (rc == HX_OK && ce == cudaSuccess) ce = cudaEventRecord(a, s);
+        for (int r = 0; r < 3 && rc == HX_OK && ce == cudaSuccess; ++r) ce = run_sub(e, sg, mode, nullptr, s);
+        if (rc == HX_OK && ce == cudaSuccess) ce = cudaEventRecord(b, s);
+        if (rc == HX_OK && ce == cudaSuccess) ce = cudaEventSynchronize(b);
+        float ms = 0.f;
+        if (rc == HX_OK && ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, a, b);
+        free_sub(sg);
+        if (rc == HX_OK && ce != cudaSuccess) { hx_set_error("autotuner: %s", cudaGetErrorString(ce)); rc = HX_ERR_CUDA; }
+        if (rc == HX_OK && error_word(e) != 0) { hx_set_error("autotuner: a tensor-core wait timed out"); rc = HX_ERR_KERNEL; }
+        if (rc == HX_OK && ms < best_ms) { best_ms = ms; *best = v; }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    *spent += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
+}
+
+static int choose_variant(Engine *e, int mode, int gi, const Group &g, cudaStream_t s, int tuning, int force)
+{
+    if (force >= 0) return std::min(force, kNumVariants[mode] - 1);
+    const TileKey key = tile_key(mode, gi, g);
+    if (tuning != 2) {
+        std::lock_guard<std::mutex> lock(g_tile_mu);
+        auto it = g_tile_table.find(key);
+        if (it != g_tile_table.end()) return std::min(it->second, kNumVariants[mode] - 1);
+    }
+    if (tuning != 1) return 0;
+    int best = 0;
+    const int rc = tune_group(e, mode, g, s, &best, &e->tune_ms);
+    if (rc < 0) return rc;
+    std::lock_guard<std::mutex> lock(g_tile_mu);
+    g_tile_table[key] = best;
+    return best;
+}
+
+int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s, int tuning, int force)
 {
     *out = nullptr;
     Engine *e = new Engine();
@@ -993,25 +1190,16 @@ int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s)
         hx_set_error("cannot query the device's multiprocessor count");
         return HX_ERR_CUDA;
     }
-    e->mode[0].BK = Low::BK; e->mode[1].BK = Mid::BK; e->mode[2].BK = High::BK; e->mode[3].BK = Exact::BK;
-    e->mode[0].S = Low::S; e->mode[0].BN = Low::BN; e->mode[0].products = Low::PRODUCTS; e->mode[0].smem = Low::SMEM_BYTES;
-    e->mode[1].S = Mid::S; e->mode[1].BN = Mid::BN; e->mode[1].products = Mid::PRODUCTS; e->mode[1].smem = Mid::SMEM_BYTES;
-    e->mode[2].S = High::S; e->mode[2].BN = High::BN; e->mode[2].products = High::PRODUCTS; e->mode[2].smem = High::SMEM_BYTES;
-    e->mode[3].S = Exact::S; e->mode[3].BN = Exact::BN; e->mode[3].products = Exact::PRODUCTS; e->mode[3].smem = Exact::SMEM_BYTES;
-    // variable operands share one scratch: the largest group of either mode
+    // variable operands share one scratch: the largest group of any mode and variant
     size_t need = 0, need_rows = 0;
-    for (const Mode &md : e->mode)
-        for (const Group &g : plan) {
-            size_t gneed = 0, grows = 0;
-            for (const TgemmDesc &t : g.h) {
-                if (!on_tc(t)) continue;
-                const size_t Kp = rup(t.K, KPAD), Ma = rup(t.M, BM), Nb = rup(t.N, md.BN);
-                if (!t.a_const) { gneed += (size_t)md.S * t.batch * Ma * Kp; grows += (size_t)t.batch * Ma; }
-                if (!t.b_const) { gneed += (size_t)md.S * t.batch * Nb * Kp; grows += (size_t)t.batch * Nb; }
+    for (int md = 0; md < 4; ++md)
+        for (int v = 0; v < kNumVariants[md]; ++v)
+            for (const Group &g : plan) {
+                size_t ge, gr;
+                var_need(g, variant_of(md, v), ge, gr);
+                need = std::max(need, ge);
+                need_rows = std::max(need_rows, gr);
             }
-            need = std::max(need, gneed);
-            need_rows = std::max(need_rows, grows);
-        }
     if ((need && cudaMalloc(&e->scratch, need * sizeof(__nv_bfloat16)) != cudaSuccess) ||
         (need_rows && cudaMalloc(&e->rexp, need_rows * sizeof(int)) != cudaSuccess) ||
         cudaMalloc(&e->d_err, sizeof(int)) != cudaSuccess) {
@@ -1019,20 +1207,26 @@ int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s)
         destroy(e);
         return HX_ERR_NOMEM;
     }
+    e->scratch_elems = need;
     cudaMemsetAsync(e->d_err, 0, sizeof(int), s);
-    for (Mode &md : e->mode) {
-        int rc = build_mode(e, md, plan, need);
-        if (rc < 0) { destroy(e); return rc; }
-    }
+    for (int md = 0; md < 4; ++md)
+        for (int v = 0; v < kNumVariants[md]; ++v)
+            if (variant_of(md, v).attr() != cudaSuccess) {
+                destroy(e);
+                hx_set_error("cannot reserve shared memory for tc_gemm");
+                return HX_ERR_CUDA;
+            }
+    for (int md = 0; md < 4; ++md)
+        for (size_t gi = 0; gi < plan.size(); ++gi) {
+            int var = choose_variant(e, md, (int)gi, plan[gi], s, tuning, force);
+            if (var < 0) { destroy(e); return var; }
+            SubGroup sg;
+            int rc = build_sub(e, md, var, plan[gi], sg);
+            e->mode[md].groups.push_back(std::move(sg));
+            if (rc < 0) { destroy(e); return rc; }
+        }
     for (const Group &g : plan) e->keys.push_back(&g);
-    if (cudaFuncSetAttribute(tc_gemm<Low>, cudaFuncAttributeMaxDynamicSharedMemorySize, Low::SMEM_BYTES) != cudaSuccess ||
-        cudaFuncSetAttribute(tc_gemm<Mid>, cudaFuncAttributeMaxDynamicSharedMemorySize, Mid::SMEM_BYTES) != cudaSuccess ||
-        cudaFuncSetAttribute(tc_gemm<High>, cudaFuncAttributeMaxDynamicSharedMemorySize, High::SMEM_BYTES) != cudaSuccess ||
-        cudaFuncSetAttribute(tc_gemm<Exact>, cudaFuncAttributeMaxDynamicSharedMemorySize, Exact::SMEM_BYTES) != cudaSuccess) {
-        destroy(e);
-        hx_set_error("cannot reserve shared memory for tc_gemm");
-        return HX_ERR_CUDA;
-    }
+    ++e->generation;                  // tuning runs made constant slices of zeros: make them again
     *out = e;
     return HX_OK;
 }
@@ -1043,47 +1237,8 @@ cudaError_t run_group(Engine *e, const TgemmDesc *descs, int n, const int *d_act
     for (size_t k = 0; k < e->keys.size(); ++k)
         if (e->keys[k]->h.data() == descs) { gi = (int)k; break; }
     if (gi < 0 || mode < 0 || mode > 3) return cudaErrorInvalidValue;
-    Mode &md = e->mode[mode];
-    SubGroup &sg = md.groups[gi];
-    if (sg.fp64.tiles > 0) {
-        cudaError_t r = hx_tgemm_f64_launch(sg.fp64.d, (int)sg.fp64.h.size(), sg.fp64.tiles, d_active, s);
-        if (r != cudaSuccess) return r;
-    }
-    if (sg.tiles == 0) return cudaSuccess;
-    cudaError_t r = cudaSuccess;
-    // constant slices of this mode are made once per initialisation, for every
-    // molecule (molecules enter a mode at different iterations)
-    if (sg.fixed_gen != e->generation) {
-        if ((r = prep_launch(sg.fixed.d, (int)sg.fixed.h.size(), sg.fixed.work, sg.fixed.rows, md.S, nullptr, s)) != cudaSuccess)
-            return r;
-        sg.fixed_gen = e->generation;
-    }
-    if ((r = prep_launch(sg.var.d, (int)sg.var.h.size(), sg.var.work, sg.var.rows, md.S, d_active, s)) != cudaSuccess)
-        return r;
-    hx_count_launches(1);
-    Engine::Pending pend{};
-    if (e->profile) {
-        pend.a = take_event(e);
-        pend.b = take_event(e);
-        for (const TcDesc &d : sg.tcd) {
-            pend.flops += 2.0 * d.batch * (double)d.M * d.N * d.K;
-            pend.hwflops += 2.0 * d.batch * (double)d.Mp * d.Np * d.Kp * md.products;
-        }
-        cudaEventRecord(pend.a, s);
-    }
-    // persistent: one CTA per SM (shared memory allows one), each looping over tiles
-    const unsigned grid = (unsigned)std::min<long long>(sg.tiles, e->nsm);
-    const int nd = (int)sg.tcd.size();
-    if (mode == 0) tc_gemm<Low><<<grid, Low::NTHREADS, Low::SMEM_BYTES, s>>>(sg.d_tcd, nd, sg.tiles, d_active, e->d_err);
-    else if (mode == 1) tc_gemm<Mid><<<grid, Mid::NTHREADS, Mid::SMEM_BYTES, s>>>(sg.d_tcd, nd, sg.tiles, d_active, e->d_err);
-    else if (mode == 2) tc_gemm<High><<<grid, High::NTHREADS, High::SMEM_BYTES, s>>>(sg.d_tcd, nd, sg.tiles, d_active, e->d_err);
-    else tc_gemm<Exact><<<grid, Exact::NTHREADS, Exact::SMEM_BYTES, s>>>(sg.d_tcd, nd, sg.tiles, d_active, e->d_err);
-    r = cudaGetLastError();
-    if (e->profile) {
-        cudaEventRecord(pend.b, s);
-        e->pending.push_back(pend);
-    }
-    return r;
+    (void)n;
+    return run_sub(e, e->mode[mode].groups[gi], mode, d_active, s);
 }
 
 int error_word(Engine *e)
@@ -1093,19 +1248,22 @@ int error_word(Engine *e)
     return v;
 }
 
+int choices(Engine *e, int *var, int cap)
+{
+    const int ng = e ? (int)e->keys.size() : 0;
+    for (int md = 0; md < 4; ++md)
+        for (int gi = 0; gi < ng; ++gi)
+            if (var && md * ng + gi < cap) var[md * ng + gi] = e->mode[md].groups[gi].var;
+    return 4 * ng;
+}
+
+double tune_ms(Engine *e) { return e ? e->tune_ms : 0.0; }
+
 void destroy(Engine *e)
 {
     if (!e) return;
-    for (Mode &md : e->mode) {
-        for (auto &g : md.groups) {
-            cudaFree(g.d_tcd);
-            cudaFree(g.var.d);
-            cudaFree(g.fixed.d);
-            if (g.fp64.d) cudaFree(g.fp64.d);
-        }
-        cudaFree(md.fixed);
-        cudaFree(md.fixed_rexp);
-    }
+    for (Mode &md : e->mode)
+        for (auto &g : md.groups) free_sub(g);
     for (auto &p : e->pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
     for (auto x : e->pool) cudaEventDestroy(x);
     cudaFree(e->scratch);
@@ -1114,6 +1272,39 @@ void destroy(Engine *e)
     delete e;
 }
 
+int table_get(int *entries, int cap)
+{
+    std::lock_guard<std::mutex> lock(g_tile_mu);
+    int k = 0;
+    for (const auto &kv : g_tile_table) {
+        if (entries && k < cap)
+            for (int c = 0; c < 4; ++c) entries[5 * k + c] = kv.first[c];
+        if (entries && k < cap) entries[5 * k + 4] = kv.second;
+        ++k;
+    }
+    return k;
+}
+
+int table_load(const int *entries, int n)
+{
+    std::lock_guard<std::mutex> lock(g_tile_mu);
+    for (int k = 0; k < n; ++k) {
+        const int *x = entries + 5 * k;
+        if (x[0] < 0 || x[0] > 3 || x[4] < 0 || x[4] >= kNumVariants[x[0]]) {
+            hx_set_error("tile table entry %d: mode %d, variant %d out of range", k, x[0], x[4]);
+            return HX_ERR_ARG;
+        }
+        g_tile_table[TileKey{x[0], x[1], x[2], x[3]}] = x[4];
+    }
+    return HX_OK;
+}
+
+int variants(int mode, int *bn, int cap)
+{
+    if (mode < 0 || mode > 3) return HX_ERR_ARG;
+    for (int k = 0; k < kNumVariants[mode] && bn && k < cap; ++k) bn[k] = variant_of(mode, k).BN;
+    return kNumVariants[mode];
+}
 }  // namespace tc
 
 // ------------------------------------------------------------------ allocation-free single GEMM

@@ -106,6 +106,16 @@ typedef struct hx_cc_params {
     int32_t mixed_check;          /* mixed precision: the iterations that may declare
                                      convergence: 0 = 7-slice tensor-core contractions that
                                      emulate FP64 (default), 1 = FP64 on the CUDA cores */
+    int32_t tile_tuning;          /* mixed precision, tensor-core tile shapes per (precision
+                                     mode, contraction group, size class): 0 = from the tile
+                                     table (hx_tile_table_load), the default shape where it
+                                     has no entry (default); 1 = the same, but a missing entry
+                                     is found by timing every candidate on this handle's own
+                                     contractions when it is created, and added to the table;
+                                     2 = the default shapes */
+    int32_t tile_force;           /* >= 0: candidate tile_force of every precision mode (the
+                                     last one where a mode has fewer); -1 (default): as
+                                     tile_tuning says */
 } hx_cc_params;
 
 typedef struct hx_ccsd hx_ccsd;
@@ -267,6 +277,24 @@ int hx_gemm(const double *A, const double *B, double *C, int32_t M, int32_t N, i
 #define HX_NOALLOC_MAX_DIM 512
 int hx_gemm_noalloc(const double *A, const double *B, double *C, int32_t M, int32_t N, int32_t K,
                     int32_t precision, void *stream);
+
+/* ---- Tensor-core tile autotuner (no counterpart in the reference). Every
+ * precision mode of the exact-slice GEMM has a few candidate tile widths
+ * (hx_tile_variants); they form the same sums in the same order and differ
+ * in speed only. The process-wide tile table maps (mode, contraction group,
+ * size class N, size class work) to a candidate: entries of 5 int32 values.
+ * hx_tile_table copies up to cap entries and returns how many there are;
+ * hx_tile_table_load merges n entries (a table measured on the GB300 ships
+ * with the Python front end). */
+int hx_tile_table(int32_t *entries, int32_t cap);
+int hx_tile_table_load(const int32_t *entries, int32_t n);
+/* Output tile widths (BN) of mode's candidates (mode 0..3: 3, 4, 5, 7
+ * slices); returns their number. */
+int hx_tile_variants(int32_t mode, int32_t *bn, int32_t cap);
+/* The candidate each (mode, group) of a mixed-precision handle runs,
+ * var[mode * groups + group]; *tune_ms (if not NULL) = milliseconds its
+ * creation spent timing candidates. Returns 4 * groups (0 for FP64 handles). */
+int hx_ccsd_tile_choices(hx_ccsd *h, int32_t *var, int32_t cap, double *tune_ms);
 
 /* Copy the message of the last error (thread-local) into buf; returns its length. */
 int hx_last_error(char *buf, size_t len);

@@ -41,6 +41,7 @@ def test_default_parameters_are_helios_defaults(lib):
     assert p.stagnation_threshold == 60.0
     # engine keys after the reference's: mixed-precision ladder defaults
     assert p.mixed_switch == 1e-3 and p.mixed_patience == 3 and p.mixed_check == 0
+    assert p.tile_tuning == 0 and p.tile_force == -1
 
 
 def test_keywords_potentiate_like_the_reference(lib):
@@ -57,6 +58,36 @@ def test_create_rejects_bad_input_without_a_gpu_call(lib):
     assert lib.hx_ccsd_create_batch(None, 0, ctypes.byref(p), ctypes.byref(h)) == -100
     buf = ctypes.create_string_buffer(256)
     assert lib.hx_last_error(buf, 256) > 0
+
+
+def test_tile_table_selection_logic(lib, tmp_path):
+    # the autotuner's table on the host (no GPU call): candidates per mode, merging,
+    # range checks, the shipped file format, and the keywords that steer it
+    from helios_gb300 import api
+    widths = [api.tile_variants(m) for m in range(4)]
+    assert [w[0] for w in widths] == [96, 80, 64, 32]            # the defaults come first
+    assert all(len(w) >= 2 and sorted(w, reverse=True) == w for w in widths)
+    assert lib.hx_tile_variants(4, None, 0) == -100
+    before = dict(((e[0], e[1], e[2], e[3]), e[4]) for e in api.tile_table())
+    api.load_tile_table([(0, 900, 7, 20, 1), (3, 901, 4, 10, 1)])
+    api.load_tile_table([(0, 900, 7, 20, 2)])                     # a later entry replaces an earlier one
+    got = dict(((e[0], e[1], e[2], e[3]), e[4]) for e in api.tile_table())
+    assert got[(0, 900, 7, 20)] == 2 and got[(3, 901, 4, 10)] == 1
+    assert {k: v for k, v in got.items() if k[1] < 900} == before
+    with pytest.raises(api.HxError):
+        api.load_tile_table([(2, 902, 3, 3, len(widths[2]))])      # no such candidate
+    with pytest.raises(api.HxError):
+        api.load_tile_table([(4, 903, 3, 3, 0)])                   # no such mode
+    path = str(tmp_path / "t.json")
+    api.write_tile_table(path, [(1, 2, 3, 4, 1), (0, 1, 2, 3, 0)])
+    assert api.read_tile_table(path) == [(0, 1, 2, 3, 0), (1, 2, 3, 4, 1)]
+    p = api.Keywords(tile_tuning="tune", tile_force=2).to_c()
+    assert p.tile_tuning == 1 and p.tile_force == 2
+    assert api.Keywords(tile_tuning="default").to_c().tile_tuning == 2
+    if os.path.exists(api.TILE_TABLE_PATH):                        # the shipped table is valid and loaded
+        shipped = api.read_tile_table(api.TILE_TABLE_PATH)
+        assert shipped and all(0 <= e[4] < len(widths[e[0]]) for e in shipped)
+        assert set((e[0], e[1], e[2], e[3]) for e in shipped) <= set(got)
 
 
 def _is_perfect_matching(mol):
