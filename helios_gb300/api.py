@@ -122,9 +122,10 @@ def read_tile_table(path):
 def write_tile_table(path, entries, note=""):
     import json
     entries = sorted(tuple(int(x) for x in e) for e in entries)
-    with open(path, "w") as f:
-        json.dump({"format": "mode, plan group, ceil log2 of the widest N, floor log2 of the multiply-adds, variant",
-                   "note": note, "entries": [list(e) for e in entries]}, f, indent=0)
+    head = json.dumps({"format": "mode, plan group, ceil log2 of the widest N, floor log2 of the multiply-adds, variant",
+                       "note": note})
+    with open(path, "w") as f:       # one entry per line
+        f.write(head[:-1] + ', "entries": [\n' + ",\n".join(json.dumps(list(e)) for e in entries) + "\n]}\n")
 
 
 def gemm(A, B, precision="fp64", reps=1):
