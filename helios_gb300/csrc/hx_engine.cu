@@ -1187,10 +1187,51 @@ void hx_ccsd_destroy(hx_ccsd *h)
 }
 
 // (T) of molecule mol from its current amplitudes (hx_triples.cu has the
-// formulas). The integrals come from the site basis: (ck|jl) = C_ck^T G C_jl
-// and (bd|ai) = (G C_ai)^T C_bd as GEMMs; X = (bd|ai) t_kj^cd - (ck|jl) t_il^ab
-// as two GEMMs over [(i a b)][(k c j)] on the FP64 CUDA-core kernel; X and
-// W take o^3 v^3 doubles each, allocated for the call.
+// formulas), over the occupied triples i <= j <= k. The integrals come from
+// the site basis: I1[i][a][b][d] = (ai|bd) = (G C_ai)^T C_bd and J[k][c][j][l]
+// = (ck|jl) = C_ck^T G C_jl, FP64 GEMMs once per call. The triples are taken
+// in slabs (one i, a range of j, every k >= j), each within a byte budget
+// (a few GB whatever the molecule): for a slab W_ijk^abc is formed directly as
+// the six pair permutations of X, twelve GEMMs of (v^2 x v x v) and
+// (v^2 x v x o) per (i, j), batched over k, on the 7-slice tensor-core GEMM
+// (an emulated FP64 product, as accurate as the FP64 one), then the energy
+// kernel sums the slab's triples. Memory is O(o v^3) for the integrals plus
+// the slab, not O(o^3 v^3).
+namespace {
+// one of the twelve permutation terms for a fixed (i, j): batch over k = j .. o-1
+TgemmDesc triples_term(int t, const CCMol &m, const double *I1, const double *J, double *Wj, int i, int j)
+{
+    const int o = m.o, v = m.v, nk = o - j, M = v * v;
+    const long long vvv = (long long)v * v * v, vov = (long long)v * o * v, voo = (long long)v * o * o;
+    const long long vv = (long long)v * v, ov = (long long)o * v, oo = (long long)o * o;
+    const double *T2 = m.t2;
+    // output W[k - j][a][b][c]: C strides (m outer, m inner, n outer, n inner, batch)
+    // Where A does not depend on k (P1, P2, P3, P5) k joins the columns, n = (k - j, x),
+    // so the large operand is sliced once; P4 and P6 keep k as a batch index.
+    const int NK = nk * v;
+    switch (t) {
+    // P1 = X(ia, jb, kc): m = (a, b), n = (k, c)
+    case 0: return tg(I1 + i * vvv, T2 + j * vov + j * v, Wj, 1, M, NK, v, v, v, v, {vv, v, 0, 1, 0}, {vov, ov, 0, 1, 0}, {vv, v, vvv, 1, 0}, 1.0, 0.0, 0);
+    case 1: return tg(T2 + i * vov, J + j * voo + j * o, Wj, 1, M, NK, o, v, v, o, {ov, 1, 0, v, 0}, {voo, oo, 0, 1, 0}, {vv, v, vvv, 1, 0}, -1.0, 1.0, 0);
+    // P2 = X(ia, kc, jb): m = (a, c), n = (k, b)
+    case 2: return tg(I1 + i * vvv, T2 + j * vov + j * v, Wj, 1, M, NK, v, v, v, v, {vv, v, 0, 1, 0}, {v, ov, 0, 1, 0}, {vv, 1, vvv, v, 0}, 1.0, 1.0, 0);
+    case 3: return tg(T2 + i * vov, J + j * voo + j * o, Wj, 1, M, NK, o, v, v, o, {ov, 1, 0, v, 0}, {o, oo, 0, 1, 0}, {vv, 1, vvv, v, 0}, -1.0, 1.0, 0);
+    // P3 = X(jb, ia, kc): m = (b, a), n = (k, c)
+    case 4: return tg(I1 + j * vvv, T2 + j * vov + i * v, Wj, 1, M, NK, v, v, v, v, {vv, v, 0, 1, 0}, {vov, ov, 0, 1, 0}, {v, vv, vvv, 1, 0}, 1.0, 1.0, 0);
+    case 5: return tg(T2 + j * vov, J + j * voo + i * o, Wj, 1, M, NK, o, v, v, o, {ov, 1, 0, v, 0}, {voo, oo, 0, 1, 0}, {v, vv, vvv, 1, 0}, -1.0, 1.0, 0);
+    // P4 = X(kc, ia, jb): m = (c, a), n = b, batch k
+    case 6: return tg(I1 + j * vvv, T2 + j * vov + i * v, Wj, nk, M, v, v, v, v, v, {vv, v, 0, 1, vvv}, {0, ov, 0, 1, 0}, {1, vv, 0, v, vvv}, 1.0, 1.0, 0);
+    case 7: return tg(T2 + j * vov, J + j * voo + i * o, Wj, nk, M, v, o, v, v, o, {ov, 1, 0, v, vov}, {0, oo, 0, 1, 0}, {1, vv, 0, v, vvv}, -1.0, 1.0, 0);
+    // P5 = X(jb, kc, ia): m = (b, c), n = (k, a)
+    case 8: return tg(I1 + j * vvv, T2 + i * vov + j * v, Wj, 1, M, NK, v, v, v, v, {vv, v, 0, 1, 0}, {v, ov, 0, 1, 0}, {v, 1, vvv, vv, 0}, 1.0, 1.0, 0);
+    case 9: return tg(T2 + j * vov, J + i * voo + j * o, Wj, 1, M, NK, o, v, v, o, {ov, 1, 0, v, 0}, {o, oo, 0, 1, 0}, {v, 1, vvv, vv, 0}, -1.0, 1.0, 0);
+    // P6 = X(kc, jb, ia): m = (c, b), n = a, batch k
+    case 10: return tg(I1 + j * vvv, T2 + i * vov + j * v, Wj, nk, M, v, v, v, v, v, {vv, v, 0, 1, vvv}, {0, ov, 0, 1, 0}, {1, v, 0, vv, vvv}, 1.0, 1.0, 0);
+    default: return tg(T2 + j * vov, J + i * voo + j * o, Wj, nk, M, v, o, v, v, o, {ov, 1, 0, v, vov}, {0, oo, 0, 1, 0}, {1, v, 0, vv, vvv}, -1.0, 1.0, 0);
+    }
+}
+}  // namespace
+
 int hx_ccsd_triples(hx_ccsd *h, int32_t mol, double e[4])
 {
     if (!h || !h->initialized) { hx_set_error("hx_ccsd_triples before hx_ccsd_init"); return HX_ERR_STATE; }
@@ -1198,29 +1239,53 @@ int hx_ccsd_triples(hx_ccsd *h, int32_t mol, double e[4])
     if (h->scf_failed[mol]) { hx_set_error("hx_ccsd_triples: the SCF of molecule %d did not converge", mol); return HX_ERR_SCF; }
     const CCMol &m = h->cc[mol];
     const int N = m.N, o = m.o, v = m.v;
-    const long long ov = (long long)o * v, o3 = (long long)o * o * o, n3 = o3 * v * v * v;
-    const size_t nX = (size_t)n3, nI1 = (size_t)ov * v * v, nJ = (size_t)ov * o * o;
-    const size_t nBvv = (size_t)N * v * v, nBoo = (size_t)N * o * o, npart = 2 * (size_t)o3;
-    const size_t elems = 2 * nX + nI1 + nJ + nBvv + 2 * nBoo + npart + 2;
+    const long long ov = (long long)o * v, vvv = (long long)v * v * v;
+    const size_t nI1 = (size_t)ov * v * v, nJ = (size_t)ov * o * o;
+    const size_t nBvv = (size_t)N * v * v, nBoo = (size_t)N * o * o;
+    // slab budget: W (v^3 doubles per triple) plus the 7-slice bf16 copies of the
+    // operands a k-batched term (P4, P6) slices per triple (14 B per element of a
+    // v^2 x K tile, K padded to 64)
+    const double per_pair = 8.0 * vvv + 14.0 * ((v * v + 127) / 128 * 128) * (double)((v + 63) / 64 * 64);
     size_t fre = 0, tot = 0;
     HX_CU(cudaMemGetInfo(&fre, &tot));
-    if ((double)elems * sizeof(double) > 0.9 * (double)fre) {
-        hx_set_error("hx_ccsd_triples: N = %d needs %.1f GB of device memory for X and W (o^3 v^3 doubles each), "
-                     "%.1f GB are free", N, elems * 8.0 / 1e9, fre / 1e9);
+    const double fixed_bytes = 8.0 * (nI1 + nJ + nBvv + 2 * nBoo);
+    const double budget = std::min(24e9, 0.5 * ((double)fre - fixed_bytes));
+    const long long max_pairs = (long long)(budget / per_pair);
+    if (max_pairs < o) {
+        hx_set_error("hx_ccsd_triples: N = %d needs about %.1f GB of device memory for one slab of triples, "
+                     "%.1f GB are free", N, (fixed_bytes + o * per_pair) / 1e9, fre / 1e9);
         return HX_ERR_NOMEM;
     }
+    // slabs: (i, j0, j1) with sum_{j0 <= j < j1} (o - j) <= max_pairs
+    struct Slab { int i, j0, j1; long long pairs; };
+    std::vector<Slab> slabs;
+    long long maxp = 0;
+    for (int i = 0; i < o; ++i)
+        for (int j0 = i; j0 < o;) {
+            int j1 = j0;
+            long long p = 0;
+            while (j1 < o && p + (o - j1) <= max_pairs) { p += o - j1; ++j1; }
+            slabs.push_back({i, j0, j1, p});
+            maxp = std::max(maxp, p);
+            j0 = j1;
+        }
+    const size_t nW = (size_t)maxp * vvv;
+    const size_t elems = nI1 + nJ + nBvv + 2 * nBoo + nW + 2 * (size_t)maxp + 2 * slabs.size();
     double *buf = nullptr;
+    int2 *d_pairs = nullptr;
     HX_CU(cudaMalloc(&buf, elems * sizeof(double)));
-    double *X = buf, *W = X + nX, *I1 = W + nX, *J = I1 + nI1, *Bvv0 = J + nJ, *Boo0 = Bvv0 + nBvv,
-           *GBoo0 = Boo0 + nBoo, *part = GBoo0 + nBoo, *out = part + npart;
-    std::vector<Group> gs(5);
+    if (cudaMalloc(&d_pairs, sizeof(int2) * (size_t)maxp) != cudaSuccess) {
+        cudaFree(buf);
+        hx_set_error("hx_ccsd_triples: allocation failed");
+        return HX_ERR_NOMEM;
+    }
+    double *I1 = buf, *J = I1 + nI1, *Bvv0 = J + nJ, *Boo0 = Bvv0 + nBvv, *GBoo0 = Boo0 + nBoo, *W = GBoo0 + nBoo,
+           *part = W + nW, *out = part + 2 * maxp;
+    std::vector<Group> gs(3);
     const long long oo = (long long)o * o, vv = (long long)v * v;
     gs[0].h.push_back(tg(m.G, Boo0, GBoo0, 1, N, (int)oo, N, N, (int)oo, N, {0, N, 0, 1, 0}, {0, 1, 0, oo, 0}, {0, oo, 0, 1, 0}, 1.0, 0.0, mol));
     gs[1].h.push_back(tg(m.Bov0, GBoo0, J, 1, (int)ov, (int)oo, N, (int)ov, (int)oo, N, {0, 1, 0, ov, 0}, {0, 1, 0, oo, 0}, {0, oo, 0, 1, 0}, 1.0, 0.0, mol));
     gs[2].h.push_back(tg(m.GBov0, Bvv0, I1, 1, (int)ov, (int)vv, N, (int)ov, (int)vv, N, {0, 1, 0, ov, 0}, {0, 1, 0, vv, 0}, {0, vv, 0, 1, 0}, 1.0, 0.0, mol));
-    const long long ncol = (long long)o * v * o;
-    gs[3].h.push_back(tg(I1, m.t2, X, 1, (int)(ov * v), (int)ncol, v, v, o, v, {vv, v, 0, 1, 0}, {ov, v, 0, 1, 0}, {v * ncol, ncol, o, 1, 0}, 1.0, 0.0, mol));
-    gs[4].h.push_back(tg(m.t2, J, X, 1, (int)(ov * v), (int)ncol, o, v, o, o, {ov, 1, 0, v, 0}, {oo, o, 0, 1, 0}, {v * ncol, ncol, o, 1, 0}, -1.0, 1.0, mol));
     int rc = HX_OK;
     cudaError_t ce = hx_triples_pairs(m.Cmo, N, o, Bvv0, Boo0, h->st);
     for (auto &g : gs) {
@@ -1228,19 +1293,48 @@ int hx_ccsd_triples(hx_ccsd *h, int32_t mol, double e[4])
         rc = upload_group(g);
         if (rc == HX_OK) ce = hx_tgemm_f64_launch(g.d, (int)g.h.size(), g.tiles, nullptr, h->st);
     }
-    if (ce == cudaSuccess && rc == HX_OK) ce = hx_triples_energy(X, W, m.t1, m.gov, m.Fmo, N, o, part, out, h->st);
-    double r[2] = {0.0, 0.0};
-    if (ce == cudaSuccess && rc == HX_OK) ce = cudaMemcpyAsync(r, out, sizeof(r), cudaMemcpyDeviceToHost, h->st);
+    std::vector<int2> pairs;
+    for (size_t si = 0; si < slabs.size() && rc == HX_OK && ce == cudaSuccess; ++si) {
+        const Slab &sl = slabs[si];
+        std::vector<Group> plan(12);
+        pairs.clear();
+        for (int j = sl.j0; j < sl.j1; ++j) {
+            double *Wj = W + (long long)pairs.size() * vvv;
+            for (int t = 0; t < 12; ++t) plan[t].h.push_back(triples_term(t, m, I1, J, Wj, sl.i, j));
+            for (int k = j; k < o; ++k) pairs.push_back(make_int2(j, k));
+        }
+        tc::Engine *te = nullptr;
+        rc = tc::create(&te, plan, h->st, 2, 0, 3);      // the 7-slice (emulated FP64) mode only
+        for (int t = 0; t < 12 && rc == HX_OK && ce == cudaSuccess; ++t)
+            ce = tc::run_group(te, plan[t].h.data(), (int)plan[t].h.size(), nullptr, h->st, 3);
+        if (rc == HX_OK && ce == cudaSuccess)
+            ce = cudaMemcpyAsync(d_pairs, pairs.data(), sizeof(int2) * pairs.size(), cudaMemcpyHostToDevice, h->st);
+        if (rc == HX_OK && ce == cudaSuccess)
+            ce = hx_triples_energy(W, d_pairs, (int)pairs.size(), sl.i, m.t1, m.gov, m.Fmo, N, o, part, out + 2 * si,
+                                   h->st);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(h->st);   // the pair list is pageable host memory
+        if (rc == HX_OK && ce == cudaSuccess && te && tc::error_word(te)) {
+            hx_set_error("hx_ccsd_triples: a tensor-core wait timed out");
+            rc = HX_ERR_KERNEL;
+        }
+        tc::destroy(te);
+    }
+    std::vector<double> r(2 * slabs.size(), 0.0);
+    if (ce == cudaSuccess && rc == HX_OK)
+        ce = cudaMemcpyAsync(r.data(), out, sizeof(double) * r.size(), cudaMemcpyDeviceToHost, h->st);
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(h->st);
     for (auto &g : gs) if (g.d) cudaFree(g.d);
     cudaFree(buf);
+    cudaFree(d_pairs);
     if (rc != HX_OK) return rc;
     if (ce != cudaSuccess) { hx_set_error("hx_ccsd_triples: %s", cudaGetErrorString(ce)); return HX_ERR_CUDA; }
+    double e4 = 0.0, e5 = 0.0;
+    for (size_t si = 0; si < slabs.size(); ++si) { e4 += r[2 * si]; e5 += r[2 * si + 1]; }
     if (e) {
-        e[0] = r[0] + r[1];      // (T) = E[4] + E[5] (spin-orbital textbook sign)
-        e[1] = r[0];
-        e[2] = r[1];
-        e[3] = -(r[0] + r[1]);   // the reference's triples term c1 + c2 (+ c3 = 0 for canonical RHF)
+        e[0] = e4 + e5;          // (T) = E[4] + E[5] (spin-orbital textbook sign)
+        e[1] = e4;
+        e[2] = e5;
+        e[3] = -(e4 + e5);       // the reference's triples term c1 + c2 (+ c3 = 0 for canonical RHF)
     }
     return HX_OK;
 }

@@ -28,8 +28,10 @@ cudaError_t hx_energy(const CCMol *m, const DiisMol *h, const int *act, const Hx
                       cudaStream_t s);
 
 // (T) triples (hx_triples.cu): ZDO pair products of the occupied and virtual
-// orbitals, then W, the energy partials and their ordered sum (out[0] = E[4],
-// out[1] = E[5]) from X = [(i a b)][(k c j)].
+// orbitals; the energy partials of a slab of triples (i, j, k) for one i, the
+// pairs (j, k) listed in `pairs`, and their ordered sum (out[0] = E[4],
+// out[1] = E[5] of the slab, each triple weighted by its permutations).
 cudaError_t hx_triples_pairs(const double *C, int N, int o, double *Bvv0, double *Boo0, cudaStream_t s);
-cudaError_t hx_triples_energy(const double *X, double *W, const double *t1, const double *gov, const double *Fmo,
-                              int N, int o, double *part, double *out, cudaStream_t s);
+cudaError_t hx_triples_energy(const double *W, const int2 *pairs, int npairs, int i, const double *t1,
+                              const double *gov, const double *Fmo, int N, int o, double *part, double *out,
+                              cudaStream_t s);

@@ -1179,7 +1179,7 @@ static int choose_variant(Engine *e, int mode, int gi, const Group &g, cudaStrea
     return best;
 }
 
-int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s, int tuning, int force)
+int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s, int tuning, int force, int only_mode)
 {
     *out = nullptr;
     Engine *e = new Engine();
@@ -1193,7 +1193,7 @@ int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s, int tun
     // variable operands share one scratch: the largest group of any mode and variant
     size_t need = 0, need_rows = 0;
     for (int md = 0; md < 4; ++md)
-        for (int v = 0; v < kNumVariants[md]; ++v)
+        for (int v = 0; v < kNumVariants[md] && (only_mode < 0 || md == only_mode); ++v)
             for (const Group &g : plan) {
                 size_t ge, gr;
                 var_need(g, variant_of(md, v), ge, gr);
@@ -1218,6 +1218,7 @@ int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s, int tun
             }
     for (int md = 0; md < 4; ++md)
         for (size_t gi = 0; gi < plan.size(); ++gi) {
+            if (only_mode >= 0 && md != only_mode) { e->mode[md].groups.emplace_back(); continue; }
             int var = choose_variant(e, md, (int)gi, plan[gi], s, tuning, force);
             if (var < 0) { destroy(e); return var; }
             SubGroup sg;

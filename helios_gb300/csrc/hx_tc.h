@@ -9,8 +9,10 @@ struct Engine;
 // operand). Tile variants: force >= 0 takes candidate `force` of every mode;
 // otherwise tuning 0 looks each (mode, group, size class) up in the tile
 // table and takes the default on a miss, 1 times every candidate on a miss
-// (and records the winner), 2 takes the defaults.
-int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s, int tuning = 2, int force = -1);
+// (and records the winner), 2 takes the defaults. only_mode >= 0 builds that
+// precision mode alone (the others have no groups to run).
+int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s, int tuning = 2, int force = -1,
+           int only_mode = -1);
 // Run one plan group on the tensor cores: slice the operands, tcgen05 GEMM,
 // FP64 epilogue. mode 0 = LOW (3 slices, about 2^-24 of the row maxima),
 // 1 = MID (4 slices, about 2^-32), 2 = HIGH (5 slices, about 2^-35), 3 =

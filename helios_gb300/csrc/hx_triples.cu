@@ -1,16 +1,17 @@
-// (T) triples correction of a converged closed-shell CCSD (FP64, HBM bound).
+// (T) triples correction of a converged closed-shell CCSD: the energy kernels.
 //
 // The spin-adapted form of the perturbative triples on spatial orbitals:
-//   X_ijk^abc = sum_d (bd|ai) t_kj^cd - sum_l (ck|jl) t_il^ab     (two GEMMs)
+//   X_ijk^abc = sum_d (bd|ai) t_kj^cd - sum_l (ck|jl) t_il^ab
 //   W_ijk^abc = X summed over the six simultaneous permutations of the pairs
-//               (ia), (jb), (kc)                                    (k_t_sym)
+//               (ia), (jb), (kc): twelve GEMMs per block of triples on the
+//               tensor cores (hx_ccsd_triples in hx_engine.cu)
 //   Z_ijk^abc = (jb|kc) t_i^a + (ia|kc) t_j^b + (ia|jb) t_k^c
 //   Y_ijk^abc = 4 W_abc + W_bca + W_cab - 2 W_acb - 2 W_bac - 2 W_cba  (ijk fixed)
 //   E[4] = sum W Y / (3 D),  E[5] = sum Z Y / (3 D),  D = e_i+e_j+e_k-e_a-e_b-e_c
-// (k_t_energy). E[4] + E[5] equals the spin-orbital (T) of the connected and
-// disconnected triples amplitudes. X is stored [(i a b)][(k c j)], W and the
-// energy run over [(i j k)][(a b c)]: one block per occupied triple, its
-// threads over the v^3 virtual triples (32-bit index arithmetic inside).
+// (k_t_energy), over the triples i <= j <= k, each weighted by its number of
+// distinct permutations. E[4] + E[5] equals the spin-orbital (T) of the
+// connected and disconnected triples amplitudes. One block per occupied
+// triple, its threads over the v^3 virtual triples (32-bit index arithmetic).
 #include <algorithm>
 
 #include "hx_common.cuh"
@@ -44,36 +45,22 @@ __global__ void k_t_pairs(const double *__restrict__ C, int N, int o, double *__
     }
 }
 
-// W[(ijk)][(abc)] = sum over the six pair permutations of X
-__global__ void __launch_bounds__(TNT) k_t_sym(const double *__restrict__ X, double *__restrict__ W, int o, int v)
+// Per-block partials of E[4] and E[5] for one triple (i, j, k), i <= j <= k:
+// the block's W_ijk^abc (v^3, [a][b][c]) sits in the slab at pair `blockIdx.x`;
+// the triple counts w = 6, 3 or 1 times (its distinct permutations: the
+// energy of a triple is unchanged by a simultaneous permutation of (ia),
+// (jb), (kc)).
+__global__ void __launch_bounds__(TNT) k_t_energy(const double *__restrict__ W, const int2 *__restrict__ pairs, int i,
+                                                  const double *__restrict__ t1, const double *__restrict__ gov,
+                                                  const double *__restrict__ Fmo, int N, int o, int v,
+                                                  double *__restrict__ part)
 {
-    const int ijk = blockIdx.x;
-    const int k = ijk % o, j = (ijk / o) % o, i = ijk / (o * o);
-    const int v3 = v * v * v;
-    const long long ncol = (long long)o * v * o;
-    // X(pair1, pair2, pair3) with pairs (p, x): row ((p1 v + x1) v + x2), column (p3 v + x3) o + p2
-    auto Xp = [&](int p1, int x1, int p2, int x2, int p3, int x3) {
-        return X[((long long)(p1 * v + x1) * v + x2) * ncol + (long long)(p3 * v + x3) * o + p2];
-    };
-    double *Wb = W + (long long)ijk * v3;
-    for (int abc = threadIdx.x; abc < v3; abc += TNT) {
-        const int c = abc % v, b = (abc / v) % v, a = abc / (v * v);
-        Wb[abc] = Xp(i, a, j, b, k, c) + Xp(i, a, k, c, j, b) + Xp(j, b, i, a, k, c)
-                + Xp(k, c, i, a, j, b) + Xp(j, b, k, c, i, a) + Xp(k, c, j, b, i, a);
-    }
-}
-
-// per-block partial sums of E[4] and E[5]
-__global__ void __launch_bounds__(TNT) k_t_energy(const double *__restrict__ W, const double *__restrict__ t1,
-                                                  const double *__restrict__ gov, const double *__restrict__ Fmo,
-                                                  int N, int o, int v, double *__restrict__ part)
-{
-    const int ijk = blockIdx.x;
-    const int k = ijk % o, j = (ijk / o) % o, i = ijk / (o * o);
+    const int j = pairs[blockIdx.x].x, k = pairs[blockIdx.x].y;
     const int v2 = v * v, v3 = v2 * v;
     const long long ov = (long long)o * v;
-    const double *Wb = W + (long long)ijk * v3;
+    const double *Wb = W + (long long)blockIdx.x * v3;
     const double eijk = Fmo[(long long)i * N + i] + Fmo[(long long)j * N + j] + Fmo[(long long)k * N + k];
+    const double wt = (i == j && j == k) ? 1.0 : ((i == j || j == k) ? 3.0 : 6.0);
     double e4 = 0.0, e5 = 0.0;
     for (int abc = threadIdx.x; abc < v3; abc += TNT) {
         const int c = abc % v, b = (abc / v) % v, a = abc / v2;
@@ -95,8 +82,8 @@ __global__ void __launch_bounds__(TNT) k_t_energy(const double *__restrict__ W, 
     if (threadIdx.x == 0) {
         double s4 = 0.0, s5 = 0.0;
         for (int w = 0; w < TNT / 32; ++w) { s4 += sh[0][w]; s5 += sh[1][w]; }
-        part[2 * (long long)blockIdx.x] = s4;
-        part[2 * (long long)blockIdx.x + 1] = s5;
+        part[2 * (long long)blockIdx.x] = wt * s4;
+        part[2 * (long long)blockIdx.x + 1] = wt * s5;
     }
 }
 
@@ -127,18 +114,15 @@ cudaError_t hx_triples_pairs(const double *C, int N, int o, double *Bvv0, double
     return cudaGetLastError();
 }
 
-cudaError_t hx_triples_energy(const double *X, double *W, const double *t1, const double *gov, const double *Fmo,
-                              int N, int o, double *part, double *out, cudaStream_t s)
+cudaError_t hx_triples_energy(const double *W, const int2 *pairs, int npairs, int i, const double *t1,
+                              const double *gov, const double *Fmo, int N, int o, double *part, double *out,
+                              cudaStream_t s)
 {
     const int v = N - o;
-    const unsigned nb = (unsigned)((long long)o * o * o);
-    k_t_sym<<<nb, TNT, 0, s>>>(X, W, o, v);
+    k_t_energy<<<(unsigned)npairs, TNT, 0, s>>>(W, pairs, i, t1, gov, Fmo, N, o, v, part);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_t_energy<<<nb, TNT, 0, s>>>(W, t1, gov, Fmo, N, o, v, part);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    k_t_final<<<1, 32, 0, s>>>(part, nb, out);
-    hx_count_launches(3);
+    k_t_final<<<1, 32, 0, s>>>(part, npairs, out);
+    hx_count_launches(2);
     return cudaGetLastError();
 }
