@@ -216,8 +216,10 @@ int hx_ccsd_trace(hx_ccsd *h, int32_t mol, double *out, int32_t cap);
  * (connected triples), e[2] = E[5] (disconnected), e[3] = the reference's
  * triples term c1 + c2 + c3, which is -(T): its c1 multiplies amp^2 by
  * D = F_aa + F_bb + F_cc - F_ii - F_jj - F_kk > 0, and c3 (a term in F_kc)
- * vanishes for canonical RHF orbitals. Needs 2 o^3 v^3 doubles of device
- * memory for the call (HX_ERR_NOMEM when they are not free). */
+ * vanishes for canonical RHF orbitals. The triples i <= j <= k are taken in
+ * slabs on the 7-slice (FP64-emulating) tensor-core GEMM; the call allocates
+ * O(o v^3) doubles plus one slab (at most about 24 GB) and returns
+ * HX_ERR_NOMEM when not even one slab fits. */
 int hx_ccsd_triples(hx_ccsd *h, int32_t mol, double e[4]);
 
 /* Engine utility with no counterpart in the reference: device timing.
