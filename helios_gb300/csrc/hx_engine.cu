@@ -220,7 +220,20 @@ struct hx_ccsd {
     std::vector<long long> dcount;
     std::vector<std::vector<int>> slot_phase;
     std::vector<std::array<double, PH_COUNT>> ph_end;
-    int *d_act_ph[PH_COUNT] = {};
+    int *d_act_ph[PH_COUNT] = {};        // one launch mask per phase, contiguous ([phase][molecule])
+    // device-side iterator of solve_all (hx_control.cu)
+    CtlMol *d_ctl = nullptr;
+    double *d_trace = nullptr;           // [molecule][trace_cap][5]
+    int trace_cap = 0;
+    int *d_remaining = nullptr, *d_cancel = nullptr, *d_occ = nullptr;   // one block: [0], [1], [2..6]
+    unsigned long long *d_t0 = nullptr;
+    int *h_pinned = nullptr;             // pinned mirror of that block: [0] molecules still running,
+                                         // [1] the stop request, [2..6] molecules per phase next
+    bool device_ctl = false;             // solve_all: the device decides phases and masks
+    bool capturing = false;              // iteration_body is being captured: phases become conditional nodes
+    bool profiling = false;              // per-launch GEMM timing: iterations are launched one by one
+    cudaStream_t st2 = nullptr;          // captures the bodies of the conditional nodes
+    PhaseConditions cond{};
     std::vector<std::vector<std::array<double, 5>>> trace;
     // device time of the last hx_ccsd_init and solve (events on st)
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -273,6 +286,36 @@ static int upload_group(Group &g)
     return HX_OK;
 }
 
+// While an iteration is captured: a conditional (if) node on phase ph's
+// condition is added to the capture, and body(s2) is captured into its graph.
+template <class F>
+static int with_condition(hx_ccsd *h, int ph, F body)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    const cudaGraphEdgeData *edges = nullptr;
+    size_t nd = 0;
+    HX_CU(cudaStreamGetCaptureInfo(h->st, &cs, nullptr, &g, &deps, &edges, &nd));
+    alignas(cudaGraphNodeParams) unsigned char raw[sizeof(cudaGraphNodeParams)] = {};   // (no default constructor)
+    cudaGraphNodeParams &np = *reinterpret_cast<cudaGraphNodeParams *>(raw);
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h->cond.h[ph];
+    np.conditional.type = cudaGraphCondTypeIf;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    HX_CU(cudaGraphAddNode(&node, g, deps, edges, nd, &np));
+    HX_CU(cudaStreamUpdateCaptureDependencies(h->st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    HX_CU(cudaStreamBeginCaptureToGraph(h->st2, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                        cudaStreamCaptureModeThreadLocal));
+    const cudaError_t e = body(h->st2);
+    cudaGraph_t out = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(h->st2, &out);
+    HX_CU(e);
+    HX_CU(e2);
+    return HX_OK;
+}
+
 // Each molecule runs the group in its current phase: the tensor-core modes
 // on tcgen05, FP64 on the CUDA-core kernel; one launch per phase in use, with
 // that phase's mask (every launch skips the molecules that are not its own).
@@ -283,6 +326,18 @@ static int run_group(hx_ccsd *h, Group &g)
         int n[PH_COUNT] = {};
         for (int mi = 0; mi < h->nmol; ++mi)
             if (h->active[mi]) ++n[h->phase[mi]];
+        if (h->device_ctl && h->capturing) {
+            // each phase's launches become the body of a conditional node that
+            // runs only when some molecule is in that phase this iteration
+            for (int ph = PH_LOW; ph >= PH_FP64; --ph)
+                HX_TRY(with_condition(h, ph, [&](cudaStream_t s2) {
+                    if (ph == PH_FP64) return hx_tgemm_f64_launch(g.d, (int)g.h.size(), g.tiles, h->d_act_ph[PH_FP64], s2);
+                    return tc::run_group(h->tce, g.h.data(), (int)g.h.size(), h->d_act_ph[ph], s2, tc_mode(ph));
+                }));
+            return HX_OK;
+        }
+        if (h->device_ctl)                       // the phases the device counted for this iteration
+            for (int ph = 0; ph < PH_COUNT; ++ph) n[ph] = h->h_pinned[2 + ph];
         for (int ph = PH_LOW; ph >= PH_EXACT; --ph) {
             if (!n[ph]) continue;
             cudaError_t e = tc::run_group(h->tce, g.h.data(), (int)g.h.size(), h->d_act_ph[ph], h->st, tc_mode(ph));
@@ -531,7 +586,15 @@ static int allocate(hx_ccsd *h)
     }
     HX_CU(cudaMalloc(&h->d_part, sizeof(double) * std::max<size_t>((size_t)h->sched.blocks[SK_UP] * HX_PART_STRIDE,
                                                                    2 * HX_SCF_GRID_MAX)));
-    for (int ph = 0; ph < PH_COUNT; ++ph) HX_CU(cudaMalloc(&h->d_act_ph[ph], sizeof(int) * h->nmol));
+    HX_CU(cudaMalloc(&h->d_act_ph[0], sizeof(int) * PH_COUNT * h->nmol));
+    for (int ph = 1; ph < PH_COUNT; ++ph) h->d_act_ph[ph] = h->d_act_ph[0] + (size_t)ph * h->nmol;
+    HX_CU(cudaMalloc(&h->d_ctl, sizeof(CtlMol) * h->nmol));
+    HX_CU(cudaMalloc(&h->d_remaining, 8 * sizeof(int)));
+    h->d_cancel = h->d_remaining + 1;
+    h->d_occ = h->d_remaining + 2;
+    HX_CU(cudaMalloc(&h->d_t0, sizeof(unsigned long long)));
+    HX_CU(cudaHostAlloc((void **)&h->h_pinned, 8 * sizeof(int), cudaHostAllocDefault));
+    HX_CU(cudaStreamCreateWithFlags(&h->st2, cudaStreamNonBlocking));
     HX_CU(cudaMalloc(&h->d_gate, sizeof(double) * h->nmol));
     h->gate.assign(h->nmol, 0.0);
     h->active.assign(h->nmol, 1);
@@ -757,7 +820,7 @@ int hx_ccsd_init(hx_ccsd *h)
 // One iterationCC for every active molecule (no host synchronisation).
 static int iteration_body(hx_ccsd *h, double eps)
 {
-    if (eps != h->gate_eps) { h->gate_eps = eps; HX_TRY(upload_masks(h)); }
+    if (!h->device_ctl && eps != h->gate_eps) { h->gate_eps = eps; HX_TRY(upload_masks(h)); }
     auto &P = h->plan;
     int k = 0;
     HX_CU(hx_ew_dress_init(h->d_cc, h->d_active, h->sched, h->st));
@@ -848,30 +911,6 @@ static void diis_mirror_reset(hx_ccsd *h, int mi)
 // reused by later pushes as usual.
 static const double kPurge = 0.1;
 
-static int diis_purge(hx_ccsd *h, int mi, double a)
-{
-    const int nd = h->diis[mi].nd;
-    const int valid = (int)std::min<long long>(h->dcount[mi], nd);
-    std::vector<int> drop;
-    for (int ph = PH_HIGH; ph < PH_COUNT; ++ph) {        // EXACT and FP64 vectors are never purged
-        if (!(h->ph_end[mi][ph] > 0.0) || !(a < kPurge * h->ph_end[mi][ph])) continue;
-        for (int k = 0; k < valid; ++k)
-            if (h->slot_phase[mi][k] == ph) drop.push_back(k);
-        h->ph_end[mi][ph] = -1.0;
-    }
-    if (drop.empty()) return HX_OK;
-    std::vector<double> g((size_t)nd * nd);
-    HX_CU(cudaMemcpyAsync(g.data(), h->diis[mi].gram, sizeof(double) * g.size(), cudaMemcpyDeviceToHost, h->st));
-    HX_CU(cudaStreamSynchronize(h->st));
-    for (int p : drop) {
-        for (int q = 0; q < nd; ++q) g[(size_t)p * nd + q] = g[(size_t)q * nd + p] = 0.0;
-        g[(size_t)p * nd + p] = 1e100;
-        h->slot_phase[mi][p] = -1;
-    }
-    HX_CU(cudaMemcpyAsync(h->diis[mi].gram, g.data(), sizeof(double) * g.size(), cudaMemcpyHostToDevice, h->st));
-    HX_CU(cudaStreamSynchronize(h->st));
-    return HX_OK;
-}
 
 // The iterator (gIterator.f90:88-210) over every active molecule. In mixed
 // precision a molecule walks down a ladder of phases:
@@ -898,108 +937,186 @@ static int diis_purge(hx_ccsd *h, int mi, double a)
 static const double kMidSpan = 1e-3;
 static const int kMaxFp64Returns = 3;
 
+// The iterator runs on the device (k_control, after every iteration). The
+// host uploads each molecule's iterator state and captures one iteration as a
+// CUDA graph: first a node that sets each phase's condition from the number
+// of molecules in it, then every contraction group with one conditional node
+// per phase (its launches masked per molecule), the element-wise kernels,
+// the tail and k_control. The host replays the graph and reads the number of
+// molecules still running every kPoll iterations; a stop request
+// (hx_ccsd_cancel) reaches the device at the next read. Replays after the
+// last molecule stopped find every phase empty and do almost nothing. With
+// per-launch GEMM timing on (hx_ccsd_timing) the iterations are launched one
+// by one instead (the timing events belong to the host's launches), each with
+// the phases the device counted for it.
+static const int kPoll = 4;
+
 static int solve_all(hx_ccsd *h, int maxiter, double eps)
 {
     const bool mixed = h->tce != nullptr;
-    const int check_ph = h->p.mixed_check == 1 ? PH_FP64 : PH_EXACT;
+    const int n = h->nmol;
     int remaining = 0;
-    for (int mi = 0; mi < h->nmol; ++mi) {
+    std::vector<CtlMol> c(n);
+    for (int mi = 0; mi < n; ++mi) {
         remaining += h->active[mi];
         h->phase[mi] = mixed ? PH_LOW : PH_FP64;
-        h->stall[mi] = 0;
-        h->best[mi] = 1e300;
-        h->fin_scale[mi] = 1.0;
-        h->fp_returns[mi] = 0;
+        h->fin_scale[mi] = 1.0;                  // (the first iteration's DIIS gates)
+        CtlMol &x = c[mi];
+        memset(&x, 0, sizeof(x));
+        x.iteration = h->rules[mi].iteration;
+        x.successful = h->rules[mi].successful;
+        x.current = h->rules[mi].current;
+        x.status = h->status[mi];
+        x.active = h->active[mi];
+        x.phase = h->phase[mi];
+        x.best = 1e300;
+        x.fin_scale = 1.0;
+        x.dcount = h->dcount[mi];
+        for (int k = 0; k < HX_MAX_DIIS; ++k)
+            x.slot_phase[k] = (signed char)(k < (int)h->slot_phase[mi].size() ? h->slot_phase[mi][k] : -1);
+        for (int k = 0; k < PH_COUNT; ++k) x.ph_end[k] = h->ph_end[mi][k];
         h->trace[mi].clear();
     }
     h->gate_eps = eps;
     HX_TRY(upload_masks(h));
-    const auto t0 = std::chrono::steady_clock::now();
-    HX_CU(cudaEventRecord(h->ev[2], h->st));
-    while (remaining > 0) {
-        HX_TRY(iteration_body(h, eps));
-        HX_TRY(fetch_results(h));
-        if (h->tce) tc::collect(h->tce, h->prof);
-        const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-        if (h->tce && tc::error_word(h->tce) != 0) {
-            hx_set_error("a tensor-core kernel timed out waiting (code %d)", tc::error_word(h->tce));
-            return HX_ERR_KERNEL;
-        }
-        bool changed = false;
-        const bool cancel = h->cancel.exchange(0) != 0;
-        for (int mi = 0; mi < h->nmol; ++mi) {
-            if (!h->active[mi]) continue;
-            const double *r = &h->res[(size_t)mi * 8];
-            const double a = std::max(r[0], r[1]);
-            const int ph = h->phase[mi];
-            h->trace[mi].push_back({r[0], r[1], r[2], secs, (double)ph});
-            if (h->p.diis_enabled && a >= h->gate[mi]) {  // the step pushed (t, error) into the ring
-                const int nd = h->diis[mi].nd;
-                h->slot_phase[mi][(size_t)(h->dcount[mi] % nd)] = ph;
-                ++h->dcount[mi];
-            }
-            if (mixed) HX_TRY(diis_purge(h, mi, a));
-            if (ph >= PH_HIGH && !cancel) {
-                // tensor-core phases never claim convergence: they hand over
-                if (a < h->best[mi]) { h->best[mi] = a; h->stall[mi] = 0; } else ++h->stall[mi];
-                const double fin = kHighMargin * h->fin_scale[mi] * eps;
-                const double below = ph == PH_LOW ? h->p.mixed_switch : ph == PH_MID ? kMidSpan * h->p.mixed_switch : 0.0;
-                const bool stalled = h->stall[mi] >= h->p.mixed_patience;
-                int next = ph;
-                if (a < fin) next = check_ph;
-                else if (a < below || stalled) next = ph == PH_HIGH ? check_ph : ph - 1;
-                Rules &R = h->rules[mi];
-                int s = R.update(next != ph ? std::max(a, eps * 2) : a, h->p, maxiter, eps, false);
-                if (s == HX_DIVERGED || s == HX_STAGNATED || s == HX_FAILED_MAXITER) {
-                    h->status[mi] = s; h->active[mi] = 0; --remaining; changed = true;
-                } else if (next != ph) {
-                    h->phase[mi] = next;
-                    h->stall[mi] = 0;
-                    h->best[mi] = 1e300;
-                    changed = true;
-                    h->ph_end[mi][ph] = a;
-                    // HIGH stalled above its hand-over target: its floor is above
-                    // it, so the check phase iterates on instead of sending the
-                    // molecule back
-                    if (ph == PH_HIGH && a >= fin) h->fp_returns[mi] = kMaxFp64Returns;
-                    if (stalled && a >= fin && ph != PH_HIGH) {          // LOW or MID
-                        HX_CU(cudaMemsetAsync(h->diis[mi].count, 0, sizeof(int), h->st));
-                        diis_mirror_reset(h, mi);
-                    }
-                }
-                continue;
-            }
-            int s = h->rules[mi].update(a, h->p, maxiter, eps, cancel);
-            if (s != 0) {
-                h->status[mi] = s;
-                h->active[mi] = 0;
-                --remaining;
-                changed = true;
-            } else if (mixed && h->fp_returns[mi] < kMaxFp64Returns) {
-                // the check did not confirm convergence: more 5-slice
-                // iterations to a 10x tighter target, then check again
-                h->phase[mi] = PH_HIGH;
-                h->fin_scale[mi] *= 0.1;
-                ++h->fp_returns[mi];
-                h->stall[mi] = 0;
-                h->best[mi] = 1e300;
-                changed = true;
-            } else if (mixed && ph == PH_EXACT) {
-                if (a < h->best[mi]) { h->best[mi] = a; h->stall[mi] = 0; }
-                else if (++h->stall[mi] >= h->p.mixed_patience) {
-                    h->phase[mi] = PH_FP64;
-                    h->stall[mi] = 0;
-                    changed = true;
-                }
-            }
-        }
-        if (changed) HX_TRY(upload_masks(h));
+    const int cap = (int)std::min<long long>((long long)maxiter + 1, 10000);
+    if (cap > h->trace_cap) {
+        cudaFree(h->d_trace);
+        h->d_trace = nullptr;
+        h->trace_cap = 0;
+        HX_CU(cudaMalloc(&h->d_trace, sizeof(double) * 5 * (size_t)cap * n));
+        h->trace_cap = cap;
     }
+    CtlParams P;
+    memset(&P, 0, sizeof(P));
+    P.nmol = n; P.maxiter = maxiter; P.mixed = mixed; P.check_ph = h->p.mixed_check == 1 ? PH_FP64 : PH_EXACT;
+    P.patience = h->p.mixed_patience; P.max_returns = kMaxFp64Returns; P.diis_enabled = h->p.diis_enabled;
+    P.check_div = h->p.check_divergence; P.check_stag = h->p.check_stagnation; P.stag_after = h->p.stagnation_after;
+    P.trace_cap = h->trace_cap; P.eps = eps; P.mixed_switch = h->p.mixed_switch; P.mid_span = kMidSpan;
+    P.high_margin = kHighMargin; P.purge = kPurge; P.div_thr = h->p.divergence_threshold;
+    P.stag_thr = h->p.stagnation_threshold;
+    HX_CU(cudaMemcpyAsync(h->d_ctl, c.data(), sizeof(CtlMol) * n, cudaMemcpyHostToDevice, h->st));
+    h->h_pinned[0] = remaining;
+    h->h_pinned[1] = 0;
+    for (int ph = 0; ph < PH_COUNT; ++ph) h->h_pinned[2 + ph] = 0;
+    for (int mi = 0; mi < n; ++mi)
+        if (h->active[mi]) ++h->h_pinned[2 + h->phase[mi]];
+    HX_CU(cudaMemcpyAsync(h->d_remaining, h->h_pinned, 8 * sizeof(int), cudaMemcpyHostToDevice, h->st));
+    if (h->tce) HX_CU(tc::prepare_fixed(h->tce, h->st));
+    h->cancel.store(0);
+    HX_CU(cudaEventRecord(h->ev[2], h->st));
+    HX_CU(hx_control_start(h->d_t0, h->st));
+    auto control = [&]() {
+        return hx_control(h->d_cc, h->d_diis, h->d_ctl, P, h->d_cancel, h->d_t0, h->d_active,
+                          mixed ? h->d_act_ph[0] : nullptr, h->d_gate, h->d_trace, h->d_remaining, h->d_occ, h->st);
+    };
+    h->device_ctl = true;
+    const bool graph = !h->profiling;
+    cudaGraphExec_t exec = nullptr;
+    long long nodes = 0;
+    int rc = HX_OK;
+    if (graph) {
+        const long long before = g_launches.load();
+        cudaGraph_t gr = nullptr;
+        cudaError_t ce = cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal);
+        if (ce == cudaSuccess) {
+            cudaStreamCaptureStatus cs;
+            cudaGraph_t g = nullptr;
+            ce = cudaStreamGetCaptureInfo(h->st, &cs, nullptr, &g);
+            for (int ph = 0; ph < PH_COUNT && ce == cudaSuccess; ++ph)
+                ce = cudaGraphConditionalHandleCreate(&h->cond.h[ph], g, 0, 0);
+            if (ce == cudaSuccess) ce = hx_phase_conditions(h->d_occ, h->cond, h->st);
+            h->capturing = true;
+            if (ce == cudaSuccess) rc = iteration_body(h, eps);
+            h->capturing = false;
+            if (ce == cudaSuccess && rc == HX_OK) ce = control();
+            const cudaError_t ce2 = cudaStreamEndCapture(h->st, &gr);
+            if (ce == cudaSuccess) ce = ce2;
+        }
+        if (rc == HX_OK && ce == cudaSuccess) ce = cudaGraphInstantiate(&exec, gr, 0);
+        if (gr) cudaGraphDestroy(gr);
+        nodes = g_launches.load() - before;
+        g_launches.fetch_sub(nodes);                 // captured, not run: counted per replay below
+        if (rc == HX_OK && ce != cudaSuccess) {
+            hx_set_error("capturing the iteration: %s", cudaGetErrorString(ce));
+            rc = HX_ERR_CUDA;
+        }
+    }
+    long long launched = 0;
+    const int poll = graph ? kPoll : 1;
+    while (rc == HX_OK) {
+        for (int k = 0; k < poll && rc == HX_OK; ++k, ++launched) {
+            if (graph) {
+                const cudaError_t ce = cudaGraphLaunch(exec, h->st);
+                if (ce != cudaSuccess) { hx_set_error("graph launch: %s", cudaGetErrorString(ce)); rc = HX_ERR_CUDA; }
+                hx_count_launches((int)nodes);
+            } else {
+                // launched one by one: the phases counted at the last read run
+                // (h_pinned[2..6]); the device counts the next ones from zero
+                if (cudaMemsetAsync(h->d_occ, 0, PH_COUNT * sizeof(int), h->st) != cudaSuccess) {
+                    hx_set_error("solve: cudaMemsetAsync failed");
+                    rc = HX_ERR_CUDA;
+                }
+                if (rc == HX_OK) rc = iteration_body(h, eps);
+                if (rc == HX_OK && control() != cudaSuccess) { hx_set_error("iterator kernel launch failed"); rc = HX_ERR_CUDA; }
+            }
+        }
+        if (rc != HX_OK) break;
+        cudaError_t ce = cudaMemcpyAsync(h->h_pinned, h->d_remaining, (graph ? 1 : 8) * sizeof(int),
+                                         cudaMemcpyDeviceToHost, h->st);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(h->st);
+        if (ce != cudaSuccess) { hx_set_error("solve: %s", cudaGetErrorString(ce)); rc = HX_ERR_CUDA; break; }
+        if (h->tce) {
+            tc::collect(h->tce, h->prof);
+            if (tc::error_word(h->tce) != 0) {
+                hx_set_error("a tensor-core kernel timed out waiting (code %d)", tc::error_word(h->tce));
+                rc = HX_ERR_KERNEL;
+                break;
+            }
+        }
+        if (h->h_pinned[0] <= 0) break;
+        if (h->cancel.exchange(0)) {
+            h->h_pinned[1] = 1;
+            ce = cudaMemcpyAsync(h->d_cancel, h->h_pinned + 1, sizeof(int), cudaMemcpyHostToDevice, h->st);
+            if (ce != cudaSuccess) { hx_set_error("solve: %s", cudaGetErrorString(ce)); rc = HX_ERR_CUDA; break; }
+        }
+        if (launched > (long long)maxiter + 2 * kPoll + 8) {
+            hx_set_error("the device iterator did not stop after %lld iterations", launched);
+            rc = HX_ERR_STATE;
+        }
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    h->device_ctl = false;
+    if (rc < 0) { cudaStreamSynchronize(h->st); return rc; }
     HX_CU(cudaEventRecord(h->ev[3], h->st));
     HX_CU(cudaEventSynchronize(h->ev[3]));
     cudaEventElapsedTime(&h->solve_ms, h->ev[2], h->ev[3]);
+    // the iterator's state and traces back to the host mirrors
+    HX_CU(cudaMemcpy(c.data(), h->d_ctl, sizeof(CtlMol) * n, cudaMemcpyDeviceToHost));
+    int maxnt = 0;
+    for (int mi = 0; mi < n; ++mi) maxnt = std::max(maxnt, c[mi].ntrace);
+    std::vector<double> tr((size_t)n * maxnt * 5);
+    if (maxnt > 0)
+        HX_CU(cudaMemcpy2D(tr.data(), sizeof(double) * 5 * maxnt, h->d_trace, sizeof(double) * 5 * h->trace_cap,
+                           sizeof(double) * 5 * maxnt, n, cudaMemcpyDeviceToHost));
+    for (int mi = 0; mi < n; ++mi) {
+        const CtlMol &x = c[mi];
+        h->rules[mi].iteration = x.iteration;
+        h->rules[mi].successful = x.successful;
+        h->rules[mi].current = x.current;
+        h->status[mi] = x.status;
+        h->dcount[mi] = x.dcount;
+        for (int k = 0; k < (int)h->slot_phase[mi].size(); ++k) h->slot_phase[mi][k] = k < HX_MAX_DIIS ? x.slot_phase[k] : -1;
+        for (int k = 0; k < PH_COUNT; ++k) h->ph_end[mi][k] = x.ph_end[k];
+        for (int t = 0; t < x.ntrace; ++t) {
+            const double *row = &tr[((size_t)mi * maxnt + t) * 5];
+            h->trace[mi].push_back({row[0], row[1], row[2], row[3], row[4]});
+        }
+    }
+    HX_TRY(fetch_results(h));
+    if (h->tce) tc::collect(h->tce, h->prof);
     // keep every molecule addressable for getters / energy after the solve
-    for (int mi = 0; mi < h->nmol; ++mi) { h->active[mi] = !h->scf_failed[mi]; h->phase[mi] = PH_FP64; }
+    for (int mi = 0; mi < n; ++mi) { h->active[mi] = !h->scf_failed[mi]; h->phase[mi] = PH_FP64; }
     HX_TRY(upload_masks(h));
     return HX_OK;
 }
@@ -1106,6 +1223,7 @@ int hx_ccsd_timing(hx_ccsd *h, double out[8], int32_t profile)
     if (!h) { hx_set_error("NULL handle"); return HX_ERR_ARG; }
     if (profile >= 0) {
         if (h->tce) tc::set_profile(h->tce, profile != 0);
+        h->profiling = profile != 0;
         if (profile) { for (int k = 0; k < 4; ++k) h->prof[k] = 0.0; g_launches.store(0); }
     }
     if (out) {
@@ -1178,7 +1296,13 @@ void hx_ccsd_destroy(hx_ccsd *h)
     cudaFree(h->d_cc);
     cudaFree(h->d_diis);
     cudaFree(h->d_active);
-    for (int ph = 0; ph < PH_COUNT; ++ph) cudaFree(h->d_act_ph[ph]);
+    cudaFree(h->d_act_ph[0]);
+    cudaFree(h->d_ctl);
+    cudaFree(h->d_trace);
+    cudaFree(h->d_remaining);
+    cudaFree(h->d_t0);
+    if (h->h_pinned) cudaFreeHost(h->h_pinned);
+    if (h->st2) cudaStreamDestroy(h->st2);
     cudaFree(h->d_gate);
     cudaFree(h->d_part);
     cudaFree(h->d_sched);

@@ -35,3 +35,17 @@ cudaError_t hx_triples_pairs(const double *C, int N, int o, double *Bvv0, double
 cudaError_t hx_triples_energy(const double *W, const int2 *pairs, int npairs, int i, const double *t1,
                               const double *gov, const double *Fmo, int N, int o, double *part, double *out,
                               cudaStream_t s);
+
+// Device-side iterator (hx_control.cu): record the solve's start time; after an
+// iteration apply the stop rules and the phase ladder, write the next
+// iteration's masks (act_ph may be NULL for FP64 handles) and count the
+// molecules still running (remaining) and per next phase (occ[5]); in a
+// captured iteration, set each phase's conditional node from occ and clear occ.
+struct PhaseConditions {
+    cudaGraphConditionalHandle h[5];
+};
+cudaError_t hx_control_start(unsigned long long *d_t0, cudaStream_t s);
+cudaError_t hx_control(const CCMol *mols, const DiisMol *diis, CtlMol *ctl, const CtlParams &P, const int *cancel_flag,
+                       const unsigned long long *t0, int *active, int *act_ph, double *gate, double *trace,
+                       int *remaining, int *occ, cudaStream_t s);
+cudaError_t hx_phase_conditions(int *occ, const PhaseConditions &c, cudaStream_t s);

@@ -114,3 +114,21 @@ __host__ __device__ inline long long hx_units(int o, int v, bool upper)
     const int g = hx_unit_blocks(v);
     return 1 + (nb + g - 1) / g;
 }
+
+// ---------------------------------------------------------------- device-side iterator
+// The state of the iterator (gIterator.f90:88-210) and of the mixed-precision
+// phase ladder of one molecule, kept on the device so that a solve runs
+// without a host round trip per iteration (k_control, hx_control.cu).
+struct CtlMol {
+    int iteration, successful, status, active, phase, stall, fp_returns, ntrace;
+    long long dcount;                  // DIIS pushes so far
+    double current, best, fin_scale;
+    double ph_end[5];                  // residual at which each phase ended (0 not ended, -1 purged)
+    signed char slot_phase[HX_MAX_DIIS];   // phase that produced each DIIS slot (-1 empty or purged)
+};
+
+struct CtlParams {
+    int nmol, maxiter, mixed, check_ph, patience, max_returns, diis_enabled;
+    int check_div, check_stag, stag_after, trace_cap;
+    double eps, mixed_switch, mid_span, high_margin, purge, div_thr, stag_thr;
+};

@@ -1242,6 +1242,20 @@ cudaError_t run_group(Engine *e, const TgemmDesc *descs, int n, const int *d_act
     return run_sub(e, e->mode[mode].groups[gi], mode, d_active, s);
 }
 
+cudaError_t prepare_fixed(Engine *e, cudaStream_t s)
+{
+    if (!e) return cudaSuccess;
+    for (int md = 0; md < 4; ++md)
+        for (SubGroup &sg : e->mode[md].groups) {
+            if (sg.tiles == 0 || sg.fixed_gen == e->generation) continue;
+            const cudaError_t r = prep_launch(sg.fixed.d, (int)sg.fixed.h.size(), sg.fixed.work, sg.fixed.rows,
+                                              variant_of(md, sg.var).S, nullptr, s);
+            if (r != cudaSuccess) return r;
+            sg.fixed_gen = e->generation;
+        }
+    return cudaSuccess;
+}
+
 int error_word(Engine *e)
 {
     int v = 0;

@@ -19,6 +19,10 @@ int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s, int tun
 // EXACT (7 slices: an FP64 GEMM emulated, as accurate as the FP64 product).
 cudaError_t run_group(Engine *e, const TgemmDesc *descs, int n, const int *d_active, cudaStream_t s, int mode);
 void destroy(Engine *e);
+// Slice the constant operands of every group and mode now (they are
+// otherwise sliced on a group's first run after an initialisation), so that
+// a captured iteration holds no one-off work.
+cudaError_t prepare_fixed(Engine *e, cudaStream_t s);
 // Device error word of the tensor-core kernels (0 = no wait timed out).
 int error_word(Engine *e);
 // Live timing of the tcgen05 GEMM launches (CUDA events on the launching
