@@ -39,7 +39,7 @@ __device__ int rules_update(CtlMol &c, double acc, const CtlParams &P, bool canc
 }
 
 __global__ void k_control(const CCMol *__restrict__ mols, const DiisMol *__restrict__ diis, CtlMol *__restrict__ ctl,
-                          CtlParams P, const int *__restrict__ cancel_flag, const unsigned long long *__restrict__ t0,
+                          CtlParams P, const volatile int *cancel_flag, const unsigned long long *__restrict__ t0,
                           int *__restrict__ active, int *__restrict__ act_ph, double *__restrict__ gate,
                           double *__restrict__ trace, int *__restrict__ remaining, int *__restrict__ occ)
 {
@@ -138,15 +138,32 @@ __global__ void k_control_start(unsigned long long *t0) { *t0 = gtimer(); }
 
 // First node of a captured iteration: each phase's conditional body runs only
 // if some molecule is in that phase (counted by the last iteration's
-// k_control); the counts start again from zero.
-__global__ void k_phase_conditions(int *occ, PhaseConditions c)
+// k_control); the counts start again from zero, and runs[p] counts the
+// iterations in which phase p ran.
+// (one handle per conditional node; entries with phase < 0 are unused)
+__global__ void k_phase_conditions(int *occ, const PhaseCondition *hs, int n, int *runs)
 {
-    for (int p = 0; p < 5; ++p) {
-        cudaGraphSetConditional(c.h[p], occ[p] > 0 ? 1u : 0u);
-        occ[p] = 0;
-    }
+    unsigned int on[5];
+    for (int p = 0; p < 5; ++p) { on[p] = occ[p] > 0 ? 1u : 0u; occ[p] = 0; runs[p] += (int)on[p]; }
+    for (int k = 0; k < n; ++k)
+        if (hs[k].phase >= 0) cudaGraphSetConditional(hs[k].handle, on[hs[k].phase]);
+}
+
+// Last node of the loop body: run the body again while a molecule is still
+// running, and never more than cap times (count is cleared before the launch).
+__global__ void k_loop_condition(const int *remaining, cudaGraphConditionalHandle loop, int *count, int cap)
+{
+    const int n = ++*count;
+    cudaGraphSetConditional(loop, (*remaining > 0 && n < cap) ? 1u : 0u);
 }
 }  // namespace
+
+cudaError_t hx_loop_condition(const int *remaining, cudaGraphConditionalHandle loop, int *count, int cap, cudaStream_t s)
+{
+    k_loop_condition<<<1, 1, 0, s>>>(remaining, loop, count, cap);
+    hx_count_launches(1);
+    return cudaGetLastError();
+}
 
 cudaError_t hx_control_start(unsigned long long *d_t0, cudaStream_t s)
 {
@@ -155,14 +172,14 @@ cudaError_t hx_control_start(unsigned long long *d_t0, cudaStream_t s)
     return cudaGetLastError();
 }
 
-cudaError_t hx_phase_conditions(int *occ, const PhaseConditions &c, cudaStream_t s)
+cudaError_t hx_phase_conditions(int *occ, const PhaseCondition *hs, int n, int *runs, cudaStream_t s)
 {
-    k_phase_conditions<<<1, 1, 0, s>>>(occ, c);
+    k_phase_conditions<<<1, 1, 0, s>>>(occ, hs, n, runs);
     hx_count_launches(1);
     return cudaGetLastError();
 }
 
-cudaError_t hx_control(const CCMol *mols, const DiisMol *diis, CtlMol *ctl, const CtlParams &P, const int *cancel_flag,
+cudaError_t hx_control(const CCMol *mols, const DiisMol *diis, CtlMol *ctl, const CtlParams &P, const volatile int *cancel_flag,
                        const unsigned long long *t0, int *active, int *act_ph, double *gate, double *trace,
                        int *remaining, int *occ, cudaStream_t s)
 {

@@ -225,15 +225,22 @@ struct hx_ccsd {
     CtlMol *d_ctl = nullptr;
     double *d_trace = nullptr;           // [molecule][trace_cap][5]
     int trace_cap = 0;
-    int *d_remaining = nullptr, *d_cancel = nullptr, *d_occ = nullptr;   // one block: [0], [1], [2..6]
+    int *d_remaining = nullptr, *d_occ = nullptr, *d_loops = nullptr;   // one block: [0], [2..6], [7],
+    int *d_runs = nullptr;                                              // [8..12] iterations per phase
+    long long phase_nodes[5] = {};       // kernels captured in each phase's conditional bodies
+    int *d_cancel = nullptr;             // device address of h_pinned[8] (mapped host memory)
     unsigned long long *d_t0 = nullptr;
-    int *h_pinned = nullptr;             // pinned mirror of that block: [0] molecules still running,
-                                         // [1] the stop request, [2..6] molecules per phase next
+    int *h_pinned = nullptr;             // pinned, mapped: [0..7] mirror of that block ([0] molecules
+                                         // still running, [2..6] per phase next), [8] the stop request
+                                         // (read by the device)
     bool device_ctl = false;             // solve_all: the device decides phases and masks
     bool capturing = false;              // iteration_body is being captured: phases become conditional nodes
     bool profiling = false;              // per-launch GEMM timing: iterations are launched one by one
     cudaStream_t st2 = nullptr;          // captures the bodies of the conditional nodes
-    PhaseConditions cond{};
+    // conditional handles of a captured iteration, one per conditional node
+    // (a plan group's launches of one phase), made as the nodes are captured
+    std::vector<PhaseCondition> cond;
+    PhaseCondition *d_cond = nullptr;    // room for one per (plan group, phase)
     std::vector<std::vector<std::array<double, 5>>> trace;
     // device time of the last hx_ccsd_init and solve (events on st)
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -300,7 +307,13 @@ static int with_condition(hx_ccsd *h, int ph, F body)
     alignas(cudaGraphNodeParams) unsigned char raw[sizeof(cudaGraphNodeParams)] = {};   // (no default constructor)
     cudaGraphNodeParams &np = *reinterpret_cast<cudaGraphNodeParams *>(raw);
     np.type = cudaGraphNodeTypeConditional;
-    np.conditional.handle = h->cond.h[ph];
+    PhaseCondition pc;
+    memset(&pc, 0, sizeof(pc));
+    pc.phase = ph;
+    HX_CU(cudaGraphConditionalHandleCreate(&pc.handle, g, 0, 0));
+    if (h->cond.size() >= h->plan.size() * PH_COUNT) { hx_set_error("too many conditional nodes"); return HX_ERR_STATE; }
+    h->cond.push_back(pc);
+    np.conditional.handle = pc.handle;
     np.conditional.type = cudaGraphCondTypeIf;
     np.conditional.size = 1;
     cudaGraphNode_t node;
@@ -308,7 +321,9 @@ static int with_condition(hx_ccsd *h, int ph, F body)
     HX_CU(cudaStreamUpdateCaptureDependencies(h->st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
     HX_CU(cudaStreamBeginCaptureToGraph(h->st2, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
                                         cudaStreamCaptureModeThreadLocal));
+    const long long before = g_launches.load();
     const cudaError_t e = body(h->st2);
+    h->phase_nodes[ph] += g_launches.load() - before;
     cudaGraph_t out = nullptr;
     const cudaError_t e2 = cudaStreamEndCapture(h->st2, &out);
     HX_CU(e);
@@ -329,7 +344,7 @@ static int run_group(hx_ccsd *h, Group &g)
         if (h->device_ctl && h->capturing) {
             // each phase's launches become the body of a conditional node that
             // runs only when some molecule is in that phase this iteration
-            for (int ph = PH_LOW; ph >= PH_FP64; --ph)
+            for (int ph = 0; ph < PH_COUNT; ++ph)
                 HX_TRY(with_condition(h, ph, [&](cudaStream_t s2) {
                     if (ph == PH_FP64) return hx_tgemm_f64_launch(g.d, (int)g.h.size(), g.tiles, h->d_act_ph[PH_FP64], s2);
                     return tc::run_group(h->tce, g.h.data(), (int)g.h.size(), h->d_act_ph[ph], s2, tc_mode(ph));
@@ -589,11 +604,18 @@ static int allocate(hx_ccsd *h)
     HX_CU(cudaMalloc(&h->d_act_ph[0], sizeof(int) * PH_COUNT * h->nmol));
     for (int ph = 1; ph < PH_COUNT; ++ph) h->d_act_ph[ph] = h->d_act_ph[0] + (size_t)ph * h->nmol;
     HX_CU(cudaMalloc(&h->d_ctl, sizeof(CtlMol) * h->nmol));
-    HX_CU(cudaMalloc(&h->d_remaining, 8 * sizeof(int)));
-    h->d_cancel = h->d_remaining + 1;
+    HX_CU(cudaMalloc(&h->d_remaining, 16 * sizeof(int)));
     h->d_occ = h->d_remaining + 2;
+    h->d_loops = h->d_remaining + 7;
+    h->d_runs = h->d_remaining + 8;
     HX_CU(cudaMalloc(&h->d_t0, sizeof(unsigned long long)));
-    HX_CU(cudaHostAlloc((void **)&h->h_pinned, 8 * sizeof(int), cudaHostAllocDefault));
+    HX_CU(cudaHostAlloc((void **)&h->h_pinned, 16 * sizeof(int), cudaHostAllocMapped));
+    memset(h->h_pinned, 0, 16 * sizeof(int));
+    {
+        int *dp = nullptr;
+        HX_CU(cudaHostGetDevicePointer((void **)&dp, h->h_pinned, 0));
+        h->d_cancel = dp + 8;
+    }
     HX_CU(cudaStreamCreateWithFlags(&h->st2, cudaStreamNonBlocking));
     HX_CU(cudaMalloc(&h->d_gate, sizeof(double) * h->nmol));
     h->gate.assign(h->nmol, 0.0);
@@ -938,19 +960,18 @@ static const double kMidSpan = 1e-3;
 static const int kMaxFp64Returns = 3;
 
 // The iterator runs on the device (k_control, after every iteration). The
-// host uploads each molecule's iterator state and captures one iteration as a
-// CUDA graph: first a node that sets each phase's condition from the number
-// of molecules in it, then every contraction group with one conditional node
-// per phase (its launches masked per molecule), the element-wise kernels,
-// the tail and k_control. The host replays the graph and reads the number of
-// molecules still running every kPoll iterations; a stop request
-// (hx_ccsd_cancel) reaches the device at the next read. Replays after the
-// last molecule stopped find every phase empty and do almost nothing. With
-// per-launch GEMM timing on (hx_ccsd_timing) the iterations are launched one
-// by one instead (the timing events belong to the host's launches), each with
-// the phases the device counted for it.
-static const int kPoll = 4;
-
+// host uploads each molecule's iterator state and builds one CUDA graph for
+// the whole solve: a conditional while node whose body is one captured
+// iteration -- a node that sets each phase's condition from the number of
+// molecules in that phase, every contraction group with one conditional node
+// per phase (its launches masked per molecule), the element-wise kernels, the
+// tail, k_control, and a node that continues the loop while a molecule is
+// still running (at most maxiter + 8 times, so the loop always ends). The
+// host launches it once and waits. A stop request (hx_ccsd_cancel) is a word
+// of mapped host memory that k_control reads every iteration. With per-launch
+// GEMM timing on (hx_ccsd_timing) the iterations are launched one by one
+// instead (the timing events belong to the host's launches), each with the
+// phases the device counted for it.
 static int solve_all(hx_ccsd *h, int maxiter, double eps)
 {
     const bool mixed = h->tce != nullptr;
@@ -998,12 +1019,14 @@ static int solve_all(hx_ccsd *h, int maxiter, double eps)
     HX_CU(cudaMemcpyAsync(h->d_ctl, c.data(), sizeof(CtlMol) * n, cudaMemcpyHostToDevice, h->st));
     h->h_pinned[0] = remaining;
     h->h_pinned[1] = 0;
+    reinterpret_cast<volatile int *>(h->h_pinned)[8] = 0;
     for (int ph = 0; ph < PH_COUNT; ++ph) h->h_pinned[2 + ph] = 0;
     for (int mi = 0; mi < n; ++mi)
         if (h->active[mi]) ++h->h_pinned[2 + h->phase[mi]];
     HX_CU(cudaMemcpyAsync(h->d_remaining, h->h_pinned, 8 * sizeof(int), cudaMemcpyHostToDevice, h->st));
     if (h->tce) HX_CU(tc::prepare_fixed(h->tce, h->st));
     h->cancel.store(0);
+    HX_CU(cudaMemsetAsync(h->d_loops, 0, 6 * sizeof(int), h->st));      // the loop count and runs[5]
     HX_CU(cudaEventRecord(h->ev[2], h->st));
     HX_CU(hx_control_start(h->d_t0, h->st));
     auto control = [&]() {
@@ -1017,53 +1040,115 @@ static int solve_all(hx_ccsd *h, int maxiter, double eps)
     int rc = HX_OK;
     if (graph) {
         const long long before = g_launches.load();
+        // one graph for the whole solve: a while node whose body is one
+        // iteration (the phase-condition node, every group with one conditional
+        // node per phase, the tail, k_control, then the loop condition)
         cudaGraph_t gr = nullptr;
-        cudaError_t ce = cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal);
-        if (ce == cudaSuccess) {
-            cudaStreamCaptureStatus cs;
-            cudaGraph_t g = nullptr;
-            ce = cudaStreamGetCaptureInfo(h->st, &cs, nullptr, &g);
-            for (int ph = 0; ph < PH_COUNT && ce == cudaSuccess; ++ph)
-                ce = cudaGraphConditionalHandleCreate(&h->cond.h[ph], g, 0, 0);
-            if (ce == cudaSuccess) ce = hx_phase_conditions(h->d_occ, h->cond, h->st);
-            h->capturing = true;
-            if (ce == cudaSuccess) rc = iteration_body(h, eps);
-            h->capturing = false;
-            if (ce == cudaSuccess && rc == HX_OK) ce = control();
-            const cudaError_t ce2 = cudaStreamEndCapture(h->st, &gr);
-            if (ce == cudaSuccess) ce = ce2;
+        const char *step = "cudaGraphCreate";
+        cudaError_t ce = cudaGraphCreate(&gr, 0);
+        const int ncond = (int)(h->plan.size() * PH_COUNT);
+        h->cond.clear();
+        for (int ph = 0; ph < PH_COUNT; ++ph) h->phase_nodes[ph] = 0;
+        if (ce == cudaSuccess && mixed && !h->d_cond) {
+            step = "cudaMalloc";
+            ce = cudaMalloc(&h->d_cond, sizeof(PhaseCondition) * ncond);
         }
-        if (rc == HX_OK && ce == cudaSuccess) ce = cudaGraphInstantiate(&exec, gr, 0);
+        cudaGraphConditionalHandle loop = 0;
+        cudaGraph_t body = nullptr;
+        if (ce == cudaSuccess) {
+            step = "the loop's conditional handle";
+            ce = cudaGraphConditionalHandleCreate(&loop, gr, 1, cudaGraphCondAssignDefault);
+        }
+        if (ce == cudaSuccess) {
+            step = "the while node";
+            alignas(cudaGraphNodeParams) unsigned char raw[sizeof(cudaGraphNodeParams)] = {};
+            cudaGraphNodeParams &np = *reinterpret_cast<cudaGraphNodeParams *>(raw);
+            np.type = cudaGraphNodeTypeConditional;
+            np.conditional.handle = loop;
+            np.conditional.type = cudaGraphCondTypeWhile;
+            np.conditional.size = 1;
+            cudaGraphNode_t wnode;
+            ce = cudaGraphAddNode(&wnode, gr, nullptr, nullptr, 0, &np);
+            if (ce == cudaSuccess) body = np.conditional.phGraph_out[0];
+        }
+        if (ce == cudaSuccess) {
+            step = "cudaStreamBeginCaptureToGraph";
+            ce = cudaStreamBeginCaptureToGraph(h->st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+            if (ce == cudaSuccess) {
+                if (mixed) {
+                    step = "the phase-condition kernel";
+                    ce = hx_phase_conditions(h->d_occ, h->d_cond, ncond, h->d_runs, h->st);
+                }
+                h->capturing = true;
+                if (ce == cudaSuccess) rc = iteration_body(h, eps);
+                h->capturing = false;
+                if (ce == cudaSuccess && rc == HX_OK) { step = "the control kernel"; ce = control(); }
+                if (ce == cudaSuccess && rc == HX_OK) {
+                    step = "the loop-condition kernel";
+                    ce = hx_loop_condition(h->d_remaining, loop, h->d_loops, maxiter + 8, h->st);
+                }
+                cudaGraph_t out = nullptr;
+                const cudaError_t ce2 = cudaStreamEndCapture(h->st, &out);
+                if (ce == cudaSuccess && ce2 != cudaSuccess) { step = "cudaStreamEndCapture"; ce = ce2; }
+            }
+        }
+        if (rc == HX_OK && ce == cudaSuccess && mixed) {
+            // the handles the capture made, read by the first node at run time
+            step = "cudaMemcpy of the conditional handles";
+            std::vector<PhaseCondition> all(ncond);
+            memset(all.data(), 0, sizeof(PhaseCondition) * ncond);
+            for (int k = 0; k < ncond; ++k) all[k].phase = k < (int)h->cond.size() ? h->cond[k].phase : -1;
+            for (size_t k = 0; k < h->cond.size(); ++k) all[k].handle = h->cond[k].handle;
+            ce = cudaMemcpy(h->d_cond, all.data(), sizeof(PhaseCondition) * ncond, cudaMemcpyHostToDevice);
+        }
+        if (rc == HX_OK && ce == cudaSuccess) { step = "cudaGraphInstantiate"; ce = cudaGraphInstantiate(&exec, gr, 0); }
         if (gr) cudaGraphDestroy(gr);
         nodes = g_launches.load() - before;
         g_launches.fetch_sub(nodes);                 // captured, not run: counted per replay below
         if (rc == HX_OK && ce != cudaSuccess) {
-            hx_set_error("capturing the iteration: %s", cudaGetErrorString(ce));
+            hx_set_error("capturing the iteration (%s): %s", step, cudaGetErrorString(ce));
             rc = HX_ERR_CUDA;
         }
     }
     long long launched = 0;
-    const int poll = graph ? kPoll : 1;
-    while (rc == HX_OK) {
-        for (int k = 0; k < poll && rc == HX_OK; ++k, ++launched) {
-            if (graph) {
-                const cudaError_t ce = cudaGraphLaunch(exec, h->st);
-                if (ce != cudaSuccess) { hx_set_error("graph launch: %s", cudaGetErrorString(ce)); rc = HX_ERR_CUDA; }
-                hx_count_launches((int)nodes);
-            } else {
-                // launched one by one: the phases counted at the last read run
-                // (h_pinned[2..6]); the device counts the next ones from zero
-                if (cudaMemsetAsync(h->d_occ, 0, PH_COUNT * sizeof(int), h->st) != cudaSuccess) {
-                    hx_set_error("solve: cudaMemsetAsync failed");
-                    rc = HX_ERR_CUDA;
-                }
-                if (rc == HX_OK) rc = iteration_body(h, eps);
-                if (rc == HX_OK && control() != cudaSuccess) { hx_set_error("iterator kernel launch failed"); rc = HX_ERR_CUDA; }
+    if (graph && rc == HX_OK) {
+        // the whole solve is one launch; the host waits for it
+        cudaError_t ce = cudaGraphLaunch(exec, h->st);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(h->st);
+        if (ce != cudaSuccess) { hx_set_error("solve graph: %s", cudaGetErrorString(ce)); rc = HX_ERR_CUDA; }
+        // kernels run: every iteration's unconditional ones, and each phase's
+        // bodies in the iterations that phase ran
+        int lr[6] = {0, 0, 0, 0, 0, 0};
+        if (rc == HX_OK && cudaMemcpy(lr, h->d_loops, sizeof(lr), cudaMemcpyDeviceToHost) == cudaSuccess) {
+            long long cond_nodes = 0, run = 0;
+            for (int ph = 0; ph < PH_COUNT; ++ph) { cond_nodes += h->phase_nodes[ph]; run += h->phase_nodes[ph] * lr[1 + ph]; }
+            hx_count_launches((int)((nodes - cond_nodes) * lr[0] + run));
+        }
+        const int loops = lr[0];
+        if (rc == HX_OK && h->tce) {
+            tc::collect(h->tce, h->prof);
+            if (tc::error_word(h->tce) != 0) {
+                hx_set_error("a tensor-core kernel timed out waiting (code %d)", tc::error_word(h->tce));
+                rc = HX_ERR_KERNEL;
             }
         }
+        if (rc == HX_OK && loops >= maxiter + 8) {
+            hx_set_error("the device iterator did not stop after %d iterations", loops);
+            rc = HX_ERR_STATE;
+        }
+    }
+    while (!graph && rc == HX_OK) {
+        // launched one by one: the phases counted at the last read run
+        // (h_pinned[2..6]); the device counts the next ones from zero
+        if (cudaMemsetAsync(h->d_occ, 0, PH_COUNT * sizeof(int), h->st) != cudaSuccess) {
+            hx_set_error("solve: cudaMemsetAsync failed");
+            rc = HX_ERR_CUDA;
+        }
+        if (rc == HX_OK) rc = iteration_body(h, eps);
+        if (rc == HX_OK && control() != cudaSuccess) { hx_set_error("iterator kernel launch failed"); rc = HX_ERR_CUDA; }
+        ++launched;
         if (rc != HX_OK) break;
-        cudaError_t ce = cudaMemcpyAsync(h->h_pinned, h->d_remaining, (graph ? 1 : 8) * sizeof(int),
-                                         cudaMemcpyDeviceToHost, h->st);
+        cudaError_t ce = cudaMemcpyAsync(h->h_pinned, h->d_remaining, 8 * sizeof(int), cudaMemcpyDeviceToHost, h->st);
         if (ce == cudaSuccess) ce = cudaStreamSynchronize(h->st);
         if (ce != cudaSuccess) { hx_set_error("solve: %s", cudaGetErrorString(ce)); rc = HX_ERR_CUDA; break; }
         if (h->tce) {
@@ -1075,12 +1160,7 @@ static int solve_all(hx_ccsd *h, int maxiter, double eps)
             }
         }
         if (h->h_pinned[0] <= 0) break;
-        if (h->cancel.exchange(0)) {
-            h->h_pinned[1] = 1;
-            ce = cudaMemcpyAsync(h->d_cancel, h->h_pinned + 1, sizeof(int), cudaMemcpyHostToDevice, h->st);
-            if (ce != cudaSuccess) { hx_set_error("solve: %s", cudaGetErrorString(ce)); rc = HX_ERR_CUDA; break; }
-        }
-        if (launched > (long long)maxiter + 2 * kPoll + 8) {
+        if (launched > (long long)maxiter + 8) {
             hx_set_error("the device iterator did not stop after %lld iterations", launched);
             rc = HX_ERR_STATE;
         }
@@ -1239,7 +1319,10 @@ int hx_ccsd_timing(hx_ccsd *h, double out[8], int32_t profile)
 
 void hx_ccsd_cancel(hx_ccsd *h)
 {
-    if (h) h->cancel.store(1);
+    if (!h) return;
+    h->cancel.store(1);
+    // a running solve's control kernel reads this mapped word every iteration
+    if (h->h_pinned) reinterpret_cast<volatile int *>(h->h_pinned)[8] = 1;
 }
 
 int hx_ccsd_set_model(hx_ccsd *h, const float *params)
@@ -1298,6 +1381,7 @@ void hx_ccsd_destroy(hx_ccsd *h)
     cudaFree(h->d_active);
     cudaFree(h->d_act_ph[0]);
     cudaFree(h->d_ctl);
+    cudaFree(h->d_cond);
     cudaFree(h->d_trace);
     cudaFree(h->d_remaining);
     cudaFree(h->d_t0);

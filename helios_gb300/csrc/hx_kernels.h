@@ -40,12 +40,17 @@ cudaError_t hx_triples_energy(const double *W, const int2 *pairs, int npairs, in
 // iteration apply the stop rules and the phase ladder, write the next
 // iteration's masks (act_ph may be NULL for FP64 handles) and count the
 // molecules still running (remaining) and per next phase (occ[5]); in a
-// captured iteration, set each phase's conditional node from occ and clear occ.
-struct PhaseConditions {
-    cudaGraphConditionalHandle h[5];
+// captured iteration, set the conditional node of each entry of hs from the
+// count of its phase (entries with phase < 0 are skipped), clear occ and add
+// one to runs[p] for every phase p that runs.
+struct PhaseCondition {
+    cudaGraphConditionalHandle handle;
+    int phase, pad_;
 };
 cudaError_t hx_control_start(unsigned long long *d_t0, cudaStream_t s);
-cudaError_t hx_control(const CCMol *mols, const DiisMol *diis, CtlMol *ctl, const CtlParams &P, const int *cancel_flag,
+cudaError_t hx_control(const CCMol *mols, const DiisMol *diis, CtlMol *ctl, const CtlParams &P, const volatile int *cancel_flag,
                        const unsigned long long *t0, int *active, int *act_ph, double *gate, double *trace,
                        int *remaining, int *occ, cudaStream_t s);
-cudaError_t hx_phase_conditions(int *occ, const PhaseConditions &c, cudaStream_t s);
+cudaError_t hx_phase_conditions(int *occ, const PhaseCondition *hs, int n, int *runs, cudaStream_t s);
+// Last node of a solve's loop body: keep looping while molecules run, at most cap times.
+cudaError_t hx_loop_condition(const int *remaining, cudaGraphConditionalHandle loop, int *count, int cap, cudaStream_t s);
