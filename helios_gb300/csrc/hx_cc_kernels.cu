@@ -120,15 +120,17 @@ __global__ void k_zdo_products(EW_ARGS)
     }
 }
 
-// Ts[i][mu][j][nu] *= G[mu][nu]
+// Ts[i][mu][j][nu] *= G[mu][nu]  (a molecule's o N o N < 2^32 elements: 32-bit index arithmetic)
 __global__ void k_gamma_scale(EW_ARGS)
 {
     EW_PROLOGUE
-    const int n = m.N, o = m.o;
-    EW_LOOP(e, (long long)o * n * o * n) {
-        int nu = (int)(e % n);
-        int mu = (int)((e / ((long long)n * o)) % n);
-        m.Ts[e] *= m.G[mu * n + nu];
+    const unsigned n = (unsigned)m.N, no = n * (unsigned)m.o;
+    double *__restrict__ Ts = m.Ts;
+    const double *__restrict__ G = m.G;
+    EW_LOOP(e, (long long)no * no) {
+        const unsigned x = (unsigned)e;
+        const unsigned nu = x % n, mu = (x / no) % n;
+        Ts[e] *= G[mu * n + nu];
     }
 }
 
@@ -155,14 +157,13 @@ __global__ void k_fock_blocks(EW_ARGS)
 __global__ void k_c_combine(EW_ARGS)
 {
     EW_PROLOGUE
-    const int o = m.o, v = m.v;
+    const unsigned o = (unsigned)m.o, v = (unsigned)m.v;
+    const double *__restrict__ Cp = m.Cp;
+    double *__restrict__ X2 = m.X2;
     EW_LOOP(e, (long long)o * v * o * v) {
-        int b = (int)(e % v);
-        long long r = e / v;
-        int j = (int)(r % o); r /= o;
-        int a = (int)(r % v);
-        int i = (int)(r / v);
-        m.X2[e] = 0.5 * m.Cp[e] + m.Cp[(((long long)j * v + a) * o + i) * v + b];
+        const unsigned x = (unsigned)e;                  // o^2 v^2 < 2^32
+        const unsigned b = x % v, r = x / v, j = r % o, r2 = r / o, a = r2 % v, i = r2 / v;
+        X2[e] = 0.5 * Cp[e] + Cp[((j * v + a) * o + i) * v + b];
     }
 }
 
@@ -210,24 +211,36 @@ __device__ __forceinline__ Unit unit_of(const CCMol *mols, const int *start, int
     return w;
 }
 
-// element e of a unit -> block lb, row a, column b; padded shared-memory index
-struct Elem {
-    int lb, a, b, s;
-};
-__device__ __forceinline__ Elem elem(int e, int v)
-{
-    Elem x;
-    const int vv = v * v;
-    x.lb = e / vv;
-    const int r = e - x.lb * vv;
-    x.a = r / v;
-    x.b = r - x.a * v;
-    x.s = (x.lb * v + x.a) * (v + 1) + x.b;
-    return x;
-}
 __device__ __forceinline__ long long pair_off(int i, int a, int j, int b, int o, int v)
 {
     return (((long long)i * v + a) * o + j) * v + b;
+}
+
+// Tile loops of a unit: warp w walks the rows (block lb, row a) of the unit's
+// tile, its lanes the columns b, so global reads and writes run along b (one
+// division per row, none per element); shared-memory index of (lb, a, b) is
+// (lb v + a)(v + 1) + b.
+#define ROW_LOOP(nrows) for (int row_ = threadIdx.x >> 5; row_ < (nrows); row_ += NT / 32)
+#define COL_LOOP(b, v) for (int b = threadIdx.x & 31; b < (v); b += 32)
+
+// K sums over the block at once (two barriers); valid in thread 0
+template <int K>
+__device__ __forceinline__ void block_sum_n(double (&x)[K])
+{
+    __shared__ double sh[K][NT / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) x[k] = warp_sum(x[k]);
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < K; ++k) sh[k][w] = x[k];
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        x[k] = (threadIdx.x < NT / 32) ? sh[k][threadIdx.x] : 0.0;
+        if (w == 0) x[k] = warp_sum(x[k]);
+    }
 }
 
 // u[i][a][j][b] = 2 t[i][a][j][b] - t[i][b][j][a]  (SK_FULL units)
@@ -239,16 +252,23 @@ __global__ void __launch_bounds__(NT) k_make_u(const CCMol *__restrict__ mols, c
     const Unit w = unit_of(mols, start, nmol, false, bi, bj);
     if ((active && !active[w.mol]) || w.u == 0) return;
     const CCMol &m = mols[w.mol];
-    const int o = m.o, v = m.v, ne = w.nb * v * v;
-    for (int e = threadIdx.x; e < ne; e += NT) {
-        const Elem x = elem(e, v);
-        sm[x.s] = m.t2[pair_off(bi[x.lb], x.a, bj[x.lb], x.b, o, v)];
+    const int o = m.o, v = m.v, nrows = w.nb * v;
+    const double *__restrict__ t2 = m.t2;
+    double *__restrict__ u = m.u;
+#pragma unroll 4
+    ROW_LOOP(nrows) {
+        const int lb = row_ / v, a = row_ - lb * v;
+        const double *src = t2 + pair_off(bi[lb], a, bj[lb], 0, o, v);
+        double *srow = sm + (lb * v + a) * (v + 1);
+        COL_LOOP(b, v) srow[b] = src[b];
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < ne; e += NT) {
-        const Elem x = elem(e, v);
-        const double tt = sm[(x.lb * v + x.b) * (v + 1) + x.a];
-        m.u[pair_off(bi[x.lb], x.a, bj[x.lb], x.b, o, v)] = 2.0 * sm[x.s] - tt;
+#pragma unroll 4
+    ROW_LOOP(nrows) {
+        const int lb = row_ / v, a = row_ - lb * v;
+        double *dst = u + pair_off(bi[lb], a, bj[lb], 0, o, v);
+        const double *srow = sm + (lb * v + a) * (v + 1);
+        COL_LOOP(b, v) dst[b] = 2.0 * srow[b] - sm[(lb * v + b) * (v + 1) + a];
     }
 }
 
@@ -261,10 +281,11 @@ __global__ void __launch_bounds__(NT) k_make_u(const CCMol *__restrict__ mols, c
 //     (F_aa + F_bb) (the grouping the set-up uses, so (ia,jb) and (jb,ia)
 //     round alike).
 // push = 1: (t, g) go into the ring slot count % nd and part gets the dots of
-// g with every stored error vector (weights as the reference's packed dots:
-// 1, or 1/2 for the two mirror elements (a, b) != (b, a) of a diagonal
-// block); t2 itself is written by k_extrapolate. push = 0 (no DIIS): t1 and
-// both halves of t2 are written here. part[0], part[1] = max|d1|, max|d2|.
+// g with every stored error vector. The error vector keeps the pair (ia, ib)
+// of a diagonal block once (a <= b; the mirror element is stored as 0), so a
+// plain dot is the reference's packed dot over (ia) <= (jb); t2 itself is
+// written by k_amplitudes_energy. push = 0 (no DIIS): t1 and both halves of t2 are
+// written here. part[0], part[1] = max|d1|, max|d2|.
 __global__ void __launch_bounds__(NT) k_step_push(const CCMol *__restrict__ mols, const DiisMol *__restrict__ diis,
                                                   const int *__restrict__ active, const int *__restrict__ start,
                                                   int nmol, double s1, double s2, int proj, int push,
@@ -280,12 +301,14 @@ __global__ void __launch_bounds__(NT) k_step_push(const CCMol *__restrict__ mols
     double *P = part + (long long)blockIdx.x * HX_PART_STRIDE;
     const int cnt = push ? h.count[0] : 0;
     const int slot = push ? cnt % h.nd : 0, nvec = push ? min(cnt + 1, h.nd) : 0;
+    const double *__restrict__ Fmo = m.Fmo;
+    double *__restrict__ t2 = m.t2;
+    const double *__restrict__ X2 = m.X2;
     double *S = sm;                              // the assembled residual of the unit's blocks
     double mx = 0.0;
     long long hoff;
-    int ne;
+    const int nrows = w.nb * v;
     if (w.u == 0) {
-        ne = ov;
         hoff = 0;
         for (int e = threadIdx.x; e < ov; e += NT) {
             const double d = m.r1[e];
@@ -295,103 +318,124 @@ __global__ void __launch_bounds__(NT) k_step_push(const CCMol *__restrict__ mols
             else m.t1[e] = t;
         }
     } else {
-        ne = w.nb * v * v;
         hoff = ov + (long long)w.k0 * v * v;
-        // S = r2 + (X2 + X2[q][p]): element (a, b) of block (i, j) takes
-        // X2[j][b][i][a], read with a fastest (coalesced) and added at the
-        // transposed tile position
-        for (int e = threadIdx.x; e < ne; e += NT) {
-            const Elem x = elem(e, v);
-            S[x.s] = m.X2[pair_off(bi[x.lb], x.a, bj[x.lb], x.b, o, v)];
+        // S = r2 + (X2 + X2[q][p]): element (a, b) of block (i, j) takes X2[j][b][i][a],
+        // read along a (coalesced) and added at the transposed tile position
+#pragma unroll 4
+        ROW_LOOP(nrows) {
+            const int lb = row_ / v, a = row_ - lb * v;
+            const double *src = X2 + pair_off(bi[lb], a, bj[lb], 0, o, v);
+            double *srow = S + (lb * v + a) * (v + 1);
+            COL_LOOP(b, v) srow[b] = src[b];
         }
         __syncthreads();
-        for (int e = threadIdx.x; e < ne; e += NT) {
-            const Elem x = elem(e, v);                 // x.a plays b, x.b plays a
-            S[(x.lb * v + x.b) * (v + 1) + x.a] += m.X2[pair_off(bj[x.lb], x.a, bi[x.lb], x.b, o, v)];
+#pragma unroll 4
+        ROW_LOOP(nrows) {
+            const int lb = row_ / v, x = row_ - lb * v;              // x plays b
+            const double *src = X2 + pair_off(bj[lb], x, bi[lb], 0, o, v);
+            COL_LOOP(y, v) S[(lb * v + y) * (v + 1) + x] += src[y];  // y plays a
         }
         __syncthreads();
-        for (int e = threadIdx.x; e < ne; e += NT) {
-            const Elem x = elem(e, v);
-            S[x.s] = m.r2[pair_off(bi[x.lb], x.a, bj[x.lb], x.b, o, v)] + S[x.s];
+#pragma unroll 4
+        ROW_LOOP(nrows) {
+            const int lb = row_ / v, a = row_ - lb * v;
+            const double *src = m.r2 + pair_off(bi[lb], a, bj[lb], 0, o, v);
+            double *srow = S + (lb * v + a) * (v + 1);
+            COL_LOOP(b, v) srow[b] = src[b] + srow[b];
         }
         __syncthreads();
-        for (int e = threadIdx.x; e < ne; e += NT) {
-            const Elem x = elem(e, v);
-            const int i = bi[x.lb], j = bj[x.lb];
-            const double sab = S[x.s], sba = S[(x.lb * v + x.b) * (v + 1) + x.a];
-            double wv, d2;
-            if (i < j) { wv = sab; d2 = 2.0 * sab - sba; }
-            else { wv = x.a <= x.b ? sab : sba; d2 = wv; }
-            mx = fmax(mx, fabs(d2));
-            const double g = proj == 1 ? d2 : 3.0 * wv;
-            const double D = (m.Fmo[i * n + i] + m.Fmo[j * n + j]) -
-                             (m.Fmo[(o + x.a) * n + o + x.a] + m.Fmo[(o + x.b) * n + o + x.b]);
-            const long long f = pair_off(i, x.a, j, x.b, o, v);
-            const double t = m.t2[f] + s2 * g / D;
-            if (push) {
-                h.Ht[(long long)slot * h.L + hoff + e] = t;
-                h.He[(long long)slot * h.L + hoff + e] = g;
-            } else {
-                m.t2[f] = t;
+        ROW_LOOP(nrows) {
+            const int lb = row_ / v, a = row_ - lb * v, i = bi[lb], j = bj[lb];
+            const double fij = Fmo[i * n + i] + Fmo[j * n + j], faa = Fmo[(o + a) * n + o + a];
+            const double *srow = S + (lb * v + a) * (v + 1);
+            double *trow = t2 + pair_off(i, a, j, 0, o, v);
+            const long long hrow = hoff + (long long)(lb * v + a) * v;
+            COL_LOOP(b, v) {
+                const double sab = srow[b], sba = S[(lb * v + b) * (v + 1) + a];
+                double wv, d2;
+                if (i < j) { wv = sab; d2 = 2.0 * sab - sba; }
+                else { wv = a <= b ? sab : sba; d2 = wv; }
+                mx = fmax(mx, fabs(d2));
+                const double g = proj == 1 ? d2 : 3.0 * wv;
+                const double D = fij - (faa + Fmo[(o + b) * n + o + b]);
+                const double t = trow[b] + s2 * g / D;
+                if (push) {
+                    h.Ht[(long long)slot * h.L + hrow + b] = t;
+                    // a diagonal block holds (ia, ib) and (ib, ia), the same pair: the
+                    // error vector keeps it once (a <= b), so plain dots of stored error
+                    // vectors are the reference's packed dots
+                    h.He[(long long)slot * h.L + hrow + b] = (i == j && a > b) ? 0.0 : g;
+                } else {
+                    trow[b] = t;
+                }
             }
         }
         __syncthreads();                         // (also makes the global writes above visible to the block)
         if (!push) {   // the mirror half: t2[j][b][i][a] = t2[i][a][j][b], a fastest (DIIS off only)
-            for (int e = threadIdx.x; e < ne; e += NT) {
-                const Elem x = elem(e, v);             // x.a plays b, x.b plays a
-                const int i = bi[x.lb], j = bj[x.lb];
-                if (i < j) m.t2[pair_off(j, x.a, i, x.b, o, v)] = m.t2[pair_off(i, x.b, j, x.a, o, v)];
+            ROW_LOOP(nrows) {
+                const int lb = row_ / v, x = row_ - lb * v, i = bi[lb], j = bj[lb];   // x plays b
+                if (i < j) {
+                    double *dst = t2 + pair_off(j, x, i, 0, o, v);
+                    COL_LOOP(y, v) dst[y] = t2[pair_off(i, y, j, x, o, v)];
+                }
             }
         }
     }
     const double r = block_red(mx, true);
     if (threadIdx.x == 0) { P[0] = w.u == 0 ? r : 0.0; P[1] = w.u == 0 ? 0.0 : r; }
-    // dots of the new error vector (just written, read back from L2) with every stored one
+    // dots of the new error vector (just written, read back from L2) with every
+    // stored one over the unit's contiguous stretch of the ring, eight stored
+    // vectors per pass
+    const int ne = w.u == 0 ? ov : w.nb * v * v;
     const double *En = h.He + (long long)slot * h.L + hoff;
-    for (int k = 0; k < nvec; ++k) {
-        const double *Ek = h.He + (long long)k * h.L + hoff;
-        double acc = 0.0;
+    for (int k0 = 0; k0 < nvec; k0 += 8) {
+        double acc[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        const double *Ek[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) Ek[q] = h.He + (long long)(k0 + q < nvec ? k0 + q : slot) * h.L + hoff;
+#pragma unroll 2
         for (int e = threadIdx.x; e < ne; e += NT) {
-            double wt = 1.0;
-            if (w.u > 0) {
-                const Elem x = elem(e, v);
-                if (bi[x.lb] == bj[x.lb] && x.a != x.b) wt = 0.5;
-            }
             const double g = En[e];
-            acc += wt * g * (k == slot ? g : Ek[e]);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) acc[q] += g * Ek[q][e];
         }
-        const double dk = block_red(acc, false);
-        if (threadIdx.x == 0) P[2 + k] = dk;
+        block_sum_n<8>(acc);
+        if (threadIdx.x == 0)
+            for (int q = 0; q < 8 && k0 + q < nvec; ++q) P[2 + k0 + q] = acc[q];
     }
 }
 
 // ---------------------------------------------------------------- DIIS
-// One warp per molecule. The maxima of the units give res[0], res[1] (the
+// One block per molecule. The maxima of the units give res[0], res[1] (the
 // reference's accuracy(1..2), before the step). gate[mol]: the DIIS step runs
 // while max(|d1|,|d2|) >= gate[mol]. The reference stops mixing once the
 // residual is below the convergence target (there the iteration ends); FP64
 // iterations use that target, tensor-core iterations (which hand over rather
-// than converge) their hand-over target. When it runs, the ordered sums of
-// the units' dots form the Gram row of the new slot and the bordered system
-// is solved by Gaussian elimination with partial pivoting; coef[HX_MAX_DIIS]
-// = vectors to mix (1: none, t = the newest) and coef[HX_MAX_DIIS + 1] = the
-// newest slot.
-__global__ void k_diis_solve(const CCMol *__restrict__ mols, const DiisMol *__restrict__ diis,
-                             const int *__restrict__ active, const int *__restrict__ start, const double *gate,
-                             const double *__restrict__ part, int push)
+// than converge) their hand-over target. When it runs, the units' dots
+// summed in a fixed order (strided per thread, then a fixed tree) form the
+// Gram row of the new slot and the bordered system is solved by Gaussian
+// elimination with partial pivoting; coef[HX_MAX_DIIS] = vectors to mix (1:
+// none, t = the newest) and coef[HX_MAX_DIIS + 1] = the newest slot.
+__global__ void __launch_bounds__(NT) k_diis_solve(const CCMol *__restrict__ mols, const DiisMol *__restrict__ diis,
+                                                   const int *__restrict__ active, const int *__restrict__ start,
+                                                   const double *gate, const double *__restrict__ part, int push)
 {
     const int mol = blockIdx.x;
     if (active && !active[mol]) return;
     const CCMol &m = mols[mol];
     const int u0 = start[mol], u1 = start[mol + 1];
+    __shared__ double ab[2];
     double a = 0.0, b = 0.0;
-    for (int u = u0 + threadIdx.x; u < u1; u += 32) {
+    for (int u = u0 + threadIdx.x; u < u1; u += NT) {
         a = fmax(a, part[(long long)u * HX_PART_STRIDE + 0]);
         b = fmax(b, part[(long long)u * HX_PART_STRIDE + 1]);
     }
-    a = warp_max(a);
-    b = warp_max(b);
-    if (threadIdx.x == 0) { m.res[0] = a; m.res[1] = b; }
+    a = block_red(a, true);
+    b = block_red(b, true);
+    if (threadIdx.x == 0) { m.res[0] = a; m.res[1] = b; ab[0] = a; ab[1] = b; }
+    __syncthreads();
+    a = ab[0];
+    b = ab[1];
     if (!push) return;
     const DiisMol &h = diis[mol];
     const int cnt = h.count[0];
@@ -401,47 +445,64 @@ __global__ void k_diis_solve(const CCMol *__restrict__ mols, const DiisMol *__re
         return;
     }
     __shared__ double g[HX_MAX_DIIS];
-    for (int k = threadIdx.x; k < n; k += 32) {
-        double s = 0.0;
-        for (int u = u0; u < u1; ++u) s += part[(long long)u * HX_PART_STRIDE + 2 + k];
-        g[k] = s;
-    }
-    __syncwarp();
-    if (threadIdx.x != 0) return;
     for (int k = 0; k < n; ++k) {
-        h.gram[slot * h.nd + k] = g[k];
-        h.gram[k * h.nd + slot] = g[k];
+        double s = 0.0;
+        for (int u = u0 + threadIdx.x; u < u1; u += NT) s += part[(long long)u * HX_PART_STRIDE + 2 + k];
+        s = block_red(s, false);
+        if (threadIdx.x == 0) g[k] = s;
     }
-    h.count[0] = cnt + 1;
-    h.coef[HX_MAX_DIIS + 1] = slot;
-    h.coef[HX_MAX_DIIS] = 1.0;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < n; ++k) {
+            h.gram[slot * h.nd + k] = g[k];
+            h.gram[k * h.nd + slot] = g[k];
+        }
+        h.count[0] = cnt + 1;
+        h.coef[HX_MAX_DIIS + 1] = slot;
+        h.coef[HX_MAX_DIIS] = 1.0;
+    }
     if (n == 1) return;                                // newCCVectors(1) returns early
+    // the bordered system [B 1; 1 0] c = e by Gaussian elimination with partial
+    // pivoting in shared memory: pivot search and back substitution in one
+    // thread, the row updates in parallel (each row's operations in the same
+    // order as a serial elimination)
+    constexpr int MB = HX_MAX_DIIS + 1;
+    __shared__ double A[MB * MB], x[MB];
+    __shared__ int piv_s;
     const int nb = n + 1;
-    double A[(HX_MAX_DIIS + 1) * (HX_MAX_DIIS + 1)], x[HX_MAX_DIIS + 1];
-    for (int p = 0; p < nb; ++p) {
-        for (int q = 0; q < nb; ++q) {
-            double val;
-            if (p == n && q == n) val = 0.0;
-            else if (p == n || q == n) val = 1.0;
-            else val = h.gram[p * h.nd + q];
-            A[p * nb + q] = val;
-        }
-        x[p] = (p == n) ? 1.0 : 0.0;
+    __syncthreads();
+    for (int e = threadIdx.x; e < nb * nb; e += NT) {
+        const int p = e / nb, q = e % nb;
+        double val;
+        if (p == n && q == n) val = 0.0;
+        else if (p == n || q == n) val = 1.0;
+        else val = h.gram[p * h.nd + q];
+        A[p * nb + q] = val;
     }
+    for (int p = threadIdx.x; p < nb; p += NT) x[p] = (p == n) ? 1.0 : 0.0;
+    __syncthreads();
     for (int k = 0; k < nb; ++k) {
-        int piv = k;
-        for (int r = k + 1; r < nb; ++r)
-            if (fabs(A[r * nb + k]) > fabs(A[piv * nb + k])) piv = r;
-        if (piv != k) {
-            for (int c = 0; c < nb; ++c) { double t = A[k * nb + c]; A[k * nb + c] = A[piv * nb + c]; A[piv * nb + c] = t; }
-            double t = x[k]; x[k] = x[piv]; x[piv] = t;
+        if (threadIdx.x == 0) {
+            int piv = k;
+            for (int r = k + 1; r < nb; ++r)
+                if (fabs(A[r * nb + k]) > fabs(A[piv * nb + k])) piv = r;
+            piv_s = piv;
         }
-        for (int r = k + 1; r < nb; ++r) {
-            double f = A[r * nb + k] / A[k * nb + k];
+        __syncthreads();
+        const int piv = piv_s;
+        if (piv != k) {
+            for (int c = threadIdx.x; c < nb; c += NT) { double t = A[k * nb + c]; A[k * nb + c] = A[piv * nb + c]; A[piv * nb + c] = t; }
+            if (threadIdx.x == 0) { double t = x[k]; x[k] = x[piv]; x[piv] = t; }
+        }
+        __syncthreads();
+        for (int r = k + 1 + threadIdx.x; r < nb; r += NT) {
+            const double f = A[r * nb + k] / A[k * nb + k];
             for (int c = k; c < nb; ++c) A[r * nb + c] -= f * A[k * nb + c];
             x[r] -= f * x[k];
         }
+        __syncthreads();
     }
+    if (threadIdx.x != 0) return;
     for (int k = nb - 1; k >= 0; --k) {
         double s = x[k];
         for (int c = k + 1; c < nb; ++c) s -= A[k * nb + c] * x[c];
@@ -454,28 +515,12 @@ __global__ void k_diis_solve(const CCMol *__restrict__ mols, const DiisMol *__re
 }
 
 // ---------------------------------------------------------------- amplitudes and energy
-// Element (a, b) of block (i, j), i <= j, counts twice in the full pair sum
-// of energyCC when i < j (it and its mirror) and once on a diagonal block.
-__device__ __forceinline__ double energy_term(const CCMol &m, int i, int j, int a, int b, double t, double t1a,
-                                              double t1b)
-{
-    const double s = m.Lov[pair_off(i, a, j, b, m.o, m.v)] * (t + t1a * t1b);
-    return i < j ? 2.0 * s : s;
-}
-
-// t = the newest history vector or sum_k c_k Ht[k] (k = 0 .. n-1, slot order)
-__device__ __forceinline__ double combine(const DiisMol &h, int nmix, int slot, long long e)
-{
-    if (nmix <= 1) return h.Ht[(long long)slot * h.L + e];
-    double s = 0.0;
-    for (int k = 0; k < nmix; ++k) s += h.coef[k] * h.Ht[(long long)k * h.L + e];
-    return s;
-}
-
 // energyCC r-ccsd of the unit: part[0] = sum F_ia t_ia (singles unit),
-// part[1] = the unit's share of sum L (t2 + t1 t1). With DIIS (from != 0) the
-// amplitudes come from the ring (the extrapolation) and are written to t1 and
-// both halves of t2; without, they are read from t1, t2.
+// part[1] = the unit's share of sum L (t2 + t1 t1), where element (a, b) of
+// block (i, j), i <= j, counts twice when i < j (it and its mirror) and once
+// on a diagonal block. With DIIS (from != 0) the amplitudes come from the
+// ring -- the newest vector, or sum_k c_k Ht[k] in slot order -- and are
+// written to t1 and both halves of t2; without, they are read from t1, t2.
 __global__ void __launch_bounds__(NT) k_amplitudes_energy(const CCMol *__restrict__ mols,
                                                           const DiisMol *__restrict__ diis,
                                                           const int *__restrict__ active,
@@ -484,17 +529,30 @@ __global__ void __launch_bounds__(NT) k_amplitudes_energy(const CCMol *__restric
 {
     extern __shared__ double sm[];
     __shared__ int bi[64], bj[64];
+    __shared__ double cf[HX_MAX_DIIS];
     const Unit w = unit_of(mols, start, nmol, true, bi, bj);
     if (active && !active[w.mol]) return;
     const CCMol &m = mols[w.mol];
     const DiisMol &h = diis[w.mol];
     const int o = m.o, v = m.v, n = m.N, ov = o * v;
     const int nmix = from ? (int)h.coef[HX_MAX_DIIS] : 0, slot = from ? (int)h.coef[HX_MAX_DIIS + 1] : 0;
+    for (int k = threadIdx.x; k < nmix; k += NT) cf[k] = h.coef[k];
+    __syncthreads();
+    const double *__restrict__ Ht = h.Ht;
+    const long long L = h.L;
+    auto combine = [&](long long e) {
+        if (nmix <= 1) return Ht[(long long)slot * L + e];
+        double s = 0.0;
+#pragma unroll 4
+        for (int k = 0; k < nmix; ++k) s += cf[k] * Ht[(long long)k * L + e];
+        return s;
+    };
     double *P = part + (long long)blockIdx.x * HX_PART_STRIDE;
     double acc = 0.0;
+    double *__restrict__ t2 = m.t2;
     if (w.u == 0) {
         for (int e = threadIdx.x; e < ov; e += NT) {
-            const double t = from ? combine(h, nmix, slot, e) : m.t1[e];
+            const double t = from ? combine(e) : m.t1[e];
             if (from) m.t1[e] = t;
             acc += m.Fmo[(e / v) * n + o + e % v] * t;
         }
@@ -503,31 +561,41 @@ __global__ void __launch_bounds__(NT) k_amplitudes_energy(const CCMol *__restric
         double *T1 = sm + hx_unit_tile(o, v);            // [block][2][v]
         for (int e = threadIdx.x; e < w.nb * 2 * v; e += NT) {
             const int lb = e / (2 * v), r = e % (2 * v), a = r % v, row = r < v ? bi[lb] : bj[lb];
-            T1[e] = from ? combine(h, nmix, slot, (long long)row * v + a) : m.t1[row * v + a];
+            T1[e] = from ? combine((long long)row * v + a) : m.t1[row * v + a];
         }
         __syncthreads();
-        const int ne = w.nb * v * v;
+        const int nrows = w.nb * v;
         const long long hoff = ov + (long long)w.k0 * v * v;
-        for (int e = threadIdx.x; e < ne; e += NT) {
-            const Elem x = elem(e, v);
-            const int i = bi[x.lb], j = bj[x.lb];
-            const long long f = pair_off(i, x.a, j, x.b, o, v);
-            double t;
-            if (from) {
-                t = combine(h, nmix, slot, hoff + e);
-                m.t2[f] = t;
-                sm[x.s] = t;
-            } else {
-                t = m.t2[f];
+#pragma unroll 2
+        ROW_LOOP(nrows) {
+            const int lb = row_ / v, a = row_ - lb * v, i = bi[lb], j = bj[lb];
+            const long long f0 = pair_off(i, a, j, 0, o, v);
+            double *trow = t2 + f0;
+            const double *Lrow = m.Lov + f0;
+            const double t1a = T1[lb * 2 * v + a];
+            const long long hrow = hoff + (long long)(lb * v + a) * v;
+            double *srow = sm + (lb * v + a) * (v + 1);
+            COL_LOOP(b, v) {
+                double t;
+                if (from) {
+                    t = combine(hrow + b);
+                    trow[b] = t;
+                    srow[b] = t;
+                } else {
+                    t = trow[b];
+                }
+                const double s = Lrow[b] * (t + t1a * T1[lb * 2 * v + v + b]);
+                acc += i < j ? 2.0 * s : s;
             }
-            acc += energy_term(m, i, j, x.a, x.b, t, T1[x.lb * 2 * v + x.a], T1[x.lb * 2 * v + v + x.b]);
         }
         if (from) {
             __syncthreads();
-            for (int e = threadIdx.x; e < ne; e += NT) {
-                const Elem x = elem(e, v);                 // x.a plays b, x.b plays a
-                const int i = bi[x.lb], j = bj[x.lb];
-                if (i < j) m.t2[pair_off(j, x.a, i, x.b, o, v)] = sm[(x.lb * v + x.b) * (v + 1) + x.a];
+            ROW_LOOP(nrows) {
+                const int lb = row_ / v, x = row_ - lb * v, i = bi[lb], j = bj[lb];   // x plays b
+                if (i < j) {
+                    double *dst = t2 + pair_off(j, x, i, 0, o, v);
+                    COL_LOOP(y, v) dst[y] = sm[(lb * v + y) * (v + 1) + x];
+                }
             }
         }
     }
@@ -536,23 +604,24 @@ __global__ void __launch_bounds__(NT) k_amplitudes_energy(const CCMol *__restric
 }
 
 // E = 2 sum F_ia t_ia + sum_(ia),(jb) L(ia,jb) (t2 + t1 t1)   (energyCC r-ccsd):
-// ordered sums of the units' partials
-__global__ void k_energy_finish(const CCMol *__restrict__ mols, const int *__restrict__ active,
-                                const int *__restrict__ start, const double *__restrict__ part)
+// the units' partials summed in a fixed order (strided per thread, fixed tree)
+__global__ void __launch_bounds__(NT) k_energy_finish(const CCMol *__restrict__ mols, const int *__restrict__ active,
+                                                      const int *__restrict__ start, const double *__restrict__ part)
 {
     const int mol = blockIdx.x;
     if (active && !active[mol]) return;
-    if (threadIdx.x != 0) return;
-    double a = 0.0, b = 0.0;
-    for (int u = start[mol]; u < start[mol + 1]; ++u) {
-        a += part[(long long)u * HX_PART_STRIDE + 0];
-        b += part[(long long)u * HX_PART_STRIDE + 1];
+    double x[2] = {0.0, 0.0};
+    for (int u = start[mol] + threadIdx.x; u < start[mol + 1]; u += NT) {
+        x[0] += part[(long long)u * HX_PART_STRIDE + 0];
+        x[1] += part[(long long)u * HX_PART_STRIDE + 1];
     }
+    block_sum_n<2>(x);
+    if (threadIdx.x != 0) return;
     const CCMol &m = mols[mol];
-    m.res[2] = 2.0 * a + b + m.eref;
+    m.res[2] = 2.0 * x[0] + x[1] + m.eref;
     m.res[3] = m.eref;
-    m.res[4] = 2.0 * a;
-    m.res[5] = b;
+    m.res[4] = 2.0 * x[0];
+    m.res[5] = x[1];
 }
 
 // ---------------------------------------------------------------- set-up
@@ -678,12 +747,12 @@ cudaError_t hx_tail(const CCMol *m, const DiisMol *h, const int *act, const HxSc
                                                                use_diis, part);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_diis_solve<<<S.nmol, 32, 0, s>>>(m, h, act, S.start[SK_UP], gate, part, use_diis);
+    k_diis_solve<<<S.nmol, NT, 0, s>>>(m, h, act, S.start[SK_UP], gate, part, use_diis);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     k_amplitudes_energy<<<(unsigned)S.blocks[SK_UP], NT, smem[1], s>>>(m, h, act, S.start[SK_UP], S.nmol, use_diis,
                                                                        part);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    k_energy_finish<<<S.nmol, 32, 0, s>>>(m, act, S.start[SK_UP], part);
+    k_energy_finish<<<S.nmol, NT, 0, s>>>(m, act, S.start[SK_UP], part);
     hx_count_launches(4);
     return cudaGetLastError();
 }
@@ -695,7 +764,7 @@ cudaError_t hx_energy(const CCMol *m, const DiisMol *h, const int *act, const Hx
     k_amplitudes_energy<<<(unsigned)S.blocks[SK_UP], NT, smem, s>>>(m, h, act, S.start[SK_UP], S.nmol, 0, part);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_energy_finish<<<S.nmol, 32, 0, s>>>(m, act, S.start[SK_UP], part);
+    k_energy_finish<<<S.nmol, NT, 0, s>>>(m, act, S.start[SK_UP], part);
     hx_count_launches(2);
     return cudaGetLastError();
 }
