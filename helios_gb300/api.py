@@ -76,7 +76,7 @@ def library():
         for name in ("hx_ccsd_create", "hx_ccsd_create_batch", "hx_ccsd_init", "hx_ccsd_set_guess",
                      "hx_ccsd_iterate", "hx_ccsd_energy", "hx_ccsd_solve", "hx_ccsd_solve_batch",
                      "hx_ccsd_get_amplitudes", "hx_ccsd_get_scf", "hx_ccsd_dims", "hx_ccsd_trace",
-                     "hx_gemm", "hx_ccsd_timing", "hx_last_error", "hx_ccsd_set_model", "hx_ccsd_training_rows",
+                     "hx_gemm", "hx_gemm_tile", "hx_ccsd_timing", "hx_last_error", "hx_ccsd_set_model", "hx_ccsd_training_rows",
                      "hx_mlp_nparam", "hx_mlp_predict", "hx_mlp_grad", "hx_mlp_train", "hx_ccsd_triples",
                      "hx_tile_table", "hx_tile_table_load", "hx_tile_variants", "hx_ccsd_tile_choices"):
             getattr(lib, name).restype = ctypes.c_int
@@ -92,7 +92,8 @@ TILE_TUNING = {"table": 0, "tune": 1, "default": 2}
 
 
 def tile_variants(mode: int):
-    """Output tile widths of the candidates of a precision mode (0..3: 3, 4, 5, 7 slices)."""
+    """Output tile widths of the candidates of a precision mode (0..3: 3, 4, 5, 7 slices);
+    candidates of equal width differ in their pipeline depth."""
     bn = (ctypes.c_int32 * 8)()
     n = _check(library().hx_tile_variants(int(mode), bn, 8))
     return [int(bn[k]) for k in range(n)]
@@ -128,17 +129,19 @@ def write_tile_table(path, entries, note=""):
         f.write(head[:-1] + ', "entries": [\n' + ",\n".join(json.dumps(list(e)) for e in entries) + "\n]}\n")
 
 
-def gemm(A, B, precision="fp64", reps=1):
+def gemm(A, B, precision="fp64", reps=1, variant=-1):
     """C = A @ B.T on the engine's FP64 ("fp64") or tensor-core GEMM ("mixed": 3 slices,
-    "mid": 4 slices, "high": 5 slices, "exact": 7 slices, FP64 emulated); returns (C, ms per launch)."""
+    "mid": 4 slices, "high": 5 slices, "exact": 7 slices, FP64 emulated), on tile candidate
+    `variant` of the mode (-1: the default); returns (C, ms per launch)."""
     A = np.ascontiguousarray(A, dtype=np.float64)
     B = np.ascontiguousarray(B, dtype=np.float64)
     M, K = A.shape
     N = B.shape[0]
     C = np.zeros((M, N))
     ms = ctypes.c_double()
-    _check(library().hx_gemm(A.ctypes.data_as(_c_d), B.ctypes.data_as(_c_d), C.ctypes.data_as(_c_d), M, N, K,
-                             {"fp64": 0, "mixed": 1, "high": 2, "mid": 3, "exact": 4}[precision], reps, ctypes.byref(ms)))
+    _check(library().hx_gemm_tile(A.ctypes.data_as(_c_d), B.ctypes.data_as(_c_d), C.ctypes.data_as(_c_d), M, N, K,
+                                  {"fp64": 0, "mixed": 1, "high": 2, "mid": 3, "exact": 4}[precision], int(variant),
+                                  reps, ctypes.byref(ms)))
     return C, ms.value
 
 

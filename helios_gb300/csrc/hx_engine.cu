@@ -1552,9 +1552,24 @@ int hx_ccsd_triples(hx_ccsd *h, int32_t mol, double e[4])
 int hx_gemm(const double *A, const double *B, double *C, int32_t M, int32_t N, int32_t K, int32_t precision,
             int32_t reps, double *ms)
 {
-    if (!A || !B || !C || M <= 0 || N <= 0 || K <= 0 || reps < 1 || precision < 0 || precision > 4) {
+    return hx_gemm_tile(A, B, C, M, N, K, precision, -1, reps, ms);
+}
+
+// The same with tile candidate `variant` of the precision's mode (-1: the default).
+int hx_gemm_tile(const double *A, const double *B, double *C, int32_t M, int32_t N, int32_t K, int32_t precision,
+                 int32_t variant, int32_t reps, double *ms)
+{
+    if (!A || !B || !C || M <= 0 || N <= 0 || K <= 0 || reps < 1 || precision < 0 || precision > 4 || variant < -1) {
         hx_set_error("hx_gemm: bad arguments");
         return HX_ERR_ARG;
+    }
+    if (variant >= 0 && precision > 0) {
+        int32_t bn[8];
+        const int mode = precision == 2 ? 2 : precision == 3 ? 1 : precision == 4 ? 3 : 0;
+        if (variant >= hx_tile_variants(mode, bn, 8)) {
+            hx_set_error("hx_gemm_tile: precision %d has no tile candidate %d", precision, variant);
+            return HX_ERR_ARG;
+        }
     }
     cudaStream_t st;
     HX_CU(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
@@ -1583,7 +1598,7 @@ int hx_gemm(const double *A, const double *B, double *C, int32_t M, int32_t N, i
         plan[0].h.push_back(tg(dA, dB, dC, 1, M, N, K, M, N, K, {0, K, 0, 1, 0}, {0, K, 0, 1, 0}, {0, N, 0, 1, 0}, 1.0, 1.0, 0));
         rc = upload_group(plan[0]);
     }
-    if (rc == HX_OK && precision != HX_PRECISION_FP64) rc = tc::create(&te, plan, st);
+    if (rc == HX_OK && precision != HX_PRECISION_FP64) rc = tc::create(&te, plan, st, 2, variant);
     if (rc == HX_OK) {
         auto launch = [&]() -> cudaError_t {
             if (te) return tc::run_group(te, plan[0].h.data(), 1, dact, st,

@@ -10,9 +10,14 @@
 // at most 15 significant bits, so a tensor-core accumulation of a few hundred
 // of them with equal weight is exact in FP32 (checked on the hardware:
 // integer inputs give bit-exact sums, while general bf16 inputs lose low bits
-// as K grows). The leading weights (q = i + j < NX) therefore get one exact
-// TMEM accumulator each; the rest share one accumulator whose rounding is
-// scaled down by 2^-8NX. Every chunk of KC k-blocks the accumulators are
+// as K grows). Every weight q = i + j gets its own TMEM accumulator block;
+// those of the leading weights (q < NX) are exact, the rounding of the others
+// is scaled down by 2^-8NX. The blocks of one buffer lie side by side in TMEM
+// in the order of q, and the B slices side by side in shared memory, so one
+// MMA multiplies slice i of A by slices j = 0..J of B stacked along N into the
+// blocks q = i..i+J: one MMA per A slice instead of one per slice pair, which
+// divides the shared-memory operand reads (the kernel's bound) by about the
+// number of pairs per A slice. Every chunk of KC k-blocks the accumulators are
 // summed by TwoSum and added into an FP32 (hi, lo) pair per output, so the
 // result carries the accuracy of the splitting relative to the operands' row
 // maxima without the tensor core's accumulation error. (A drain in FP64 would
@@ -29,7 +34,7 @@
 //      A producer warp streams 64-deep k-blocks of all slices with TMA
 //      (cp.async.bulk.tensor, 128-byte swizzle) through a ring of stages; one
 //      thread of the MMA warp issues tcgen05.mma (kind::f16, BF16 x BF16 ->
-//      FP32, M = 128, N = BN, K = 16) into the class accumulators, alternating
+//      FP32, M = 128, N = a multiple of BN, K = 16) into the class accumulators, alternating
 //      between two TMEM buffers per chunk; the epilogue warps drain a finished
 //      buffer with tcgen05.ld (a TMEM lane is an output row; the warps of a
 //      lane quarter split its columns) while the next chunk runs, then stage
@@ -58,27 +63,29 @@
 
 namespace tc {
 
-// Two precisions of the same kernel. Slice p of an operand is stored as
+// Four precisions of the same kernel. Slice p of an operand is stored as
 // s_p 2^-8p (exact in bf16), so the product of slices i and j weighs
 // 2^-8(i+j) by itself and a class accumulator needs no further weight.
 // Classes q = i + j < NX are kept exact (their partial sums are integers
-// times 2^-8q below 2^24 per chunk); all products with q >= NX share one
-// more accumulator, whose FP32 accumulation error (about K * 2^-32 relative
-// for a chunk of depth K) is scaled down by 2^-8NX.
-//   LOW:  3 slices, pairs i + j <= 3 (8 MMAs per k-step), NX = 1: about 2^-24
-//         of the row maxima; 128 x 96 tiles.
-//   MID:  4 slices, pairs i + j <= 3 (10 MMAs), NX = 2: about 2^-32; 128 x 80.
-//   HIGH: 5 slices, pairs i + j <= 4 (15 MMAs), NX = 3: about 2^-35 of the row
-//         maxima (3.3e-11 measured at 6400^3); 128 x 64 tiles fed by 32-deep
-//         k-blocks (64-byte swizzle). Six slices with pairs i + j <= 5 and
-//         NX = 4 reached 1.5e-13 but took 1.7x longer (21 MMAs on 128 x 48
-//         tiles), far more accuracy than the phase needs: it hands over to
-//         the 7-slice check at 0.1 eps, and the ladder sends any molecule
-//         whose residual stalls above that to 7-slice iterations.
+// times 2^-8q below 2^24 per chunk); the classes q >= NX are accumulated in
+// FP32 (error about K * 2^-32 relative for a chunk of depth K) and summed
+// in the epilogue, their rounding scaled down by 2^-8NX.
+//   LOW:  3 slices, pairs i + j <= 3 (8 products, 4 MMAs per k-step), NX = 1:
+//         about 2^-24 of the row maxima; 128 x 64 tiles.
+//   MID:  4 slices, pairs i + j <= 3 (10 products, 4 MMAs), NX = 2: about
+//         2^-32; 128 x 64.
+//   HIGH: 5 slices, pairs i + j <= 4 (15 products, 5 MMAs), NX = 3: about
+//         2^-35 of the row maxima (3.3e-11 measured at 6400^3); 128 x 48
+//         tiles fed by 32-deep k-blocks (64-byte swizzle). Six slices with
+//         pairs i + j <= 5 reached 1.5e-13 but cost 1.7x more, far more
+//         accuracy than the phase needs: it hands over to the 7-slice check
+//         at 0.1 eps, and the ladder sends any molecule whose residual stalls
+//         above that to 7-slice iterations.
 //   EXACT: 7 slices (48 fraction bits below the leading digit, past FP64's
-//         53-bit mantissa), pairs i + j <= 6 (28 MMAs), NX = 5: an emulation
-//         of an FP64 GEMM, its error that of the FP64 product itself; 128 x 32
-//         tiles, so that two buffers of six accumulators fit in TMEM.
+//         53-bit mantissa), pairs i + j <= 6 (28 products, 7 MMAs), NX = 5:
+//         an emulation of an FP64 GEMM, its error that of the FP64 product
+//         itself; 128 x 32 tiles, so that two buffers of seven accumulator
+//         blocks fit in TMEM.
 // These errors set the residual level a phase can reach (the GEMM outputs
 // are ~1e3-1e4 times the residual they cancel down to).
 template <int S_, int QMAX_, int NX_, int BN_, int STAGES_, int KC_, int EPIW_, int BK_, int STG_>
@@ -86,7 +93,7 @@ struct Cfg {
     static constexpr int S = S_;                     // integer slices per FP64 operand
     static constexpr int QMAX = QMAX_;               // slice pairs with i + j <= QMAX are multiplied
     static constexpr int NX = NX_;                   // exact classes q = 0 .. NX-1
-    static constexpr int NQ = QMAX_ >= NX_ ? NX_ + 1 : QMAX_ + 1;   // TMEM accumulators per buffer
+    static constexpr int NQ = QMAX_ + 1;             // TMEM accumulator blocks per buffer (q = 0..QMAX)
     static constexpr int BM = 128, BN = BN_, BK = BK_;   // BK: k-block depth (64 or 32)
     static constexpr uint64_t SWZ = BK_ == 64 ? 2 : 4;     // smem descriptor layout: 128- or 64-byte swizzle
     static constexpr int SBO = 8 * BK_ * 2;                 // bytes between 8-row core-matrix groups
@@ -107,7 +114,6 @@ struct Cfg {
     static constexpr bool INT_DRAIN = S_ >= 7;
     static constexpr float DRAIN_SCALE = (float)(1ull << (8 * (NX_ - 1)));
     static constexpr int PRODUCTS = [] { int n = 0; for (int i = 0; i < S_; ++i) for (int j = 0; j < S_; ++j) n += (i + j <= QMAX_); return n; }();
-    __host__ __device__ static constexpr int cls(int q) { return q < NX_ ? q : NX_; }
     // pairs in the largest exact class
     static constexpr int XPAIRS = [] { int m = 0; for (int q = 0; q < NX_; ++q) { int n = 0; for (int i = 0; i < S_; ++i) n += (q - i >= 0 && q - i < S_); m = n > m ? n : m; } return m; }();
     // exactness of a chunk: (pairs per exact class) * KC*64 * 2^14 < 2^24
@@ -123,9 +129,9 @@ struct Cfg {
     static_assert(!INT_DRAIN || 24 + 8 * (NX_ - 1) + 1 + 5 < 63, "int64 drain headroom");
 };
 // (the strip heights are what each ring leaves of the 227 KB per CTA)
-using Low = Cfg<3, 3, 1, 96, 2, 8, 12, 64, 64>;
-using Mid = Cfg<4, 3, 2, 80, 2, 6, 8, 64, 16>;
-using High = Cfg<5, 4, 3, 64, 3, 8, 8, 32, 64>;
+using Low = Cfg<3, 3, 1, 64, 2, 8, 8, 64, 64>;
+using Mid = Cfg<4, 3, 2, 64, 2, 6, 8, 64, 16>;
+using High = Cfg<5, 4, 3, 48, 3, 8, 8, 32, 64>;
 using Exact = Cfg<7, 6, 5, 32, 3, 6, 8, 32, 32>;
 constexpr int TMEM_COLS = 512;
 constexpr int BM = 128, KPAD = 64;   // K is padded to KPAD (the slicing tile depth)
@@ -562,7 +568,6 @@ __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restri
         }
     } else if (warp == WM) {
         if (lane == 0) {
-            const uint32_t idesc = idesc_bf16(BM, C::BN);
             long long g = 0, gc = 0;                          // k-blocks and chunks consumed so far
             for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
                 const TileWork w = tile_work<C>(descs, ndesc, tile);
@@ -588,26 +593,31 @@ __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restri
                         // only in the start-address field (address / 16, 14 bits:
                         // shared memory stays below 256 KB, so adding never carries)
                         const uint64_t a0 = smem_desc<C>(sa), b0 = smem_desc<C>(sb);
+                        // per k-step, for each A slice i: B slices j = 0..J_i (J_i =
+                        // min(S-1, QMAX-i)) stacked along N into blocks q = i..i+J_i.
+                        // Blocks 0..covered were written earlier in this k-step (the
+                        // ranges issued so far cover a prefix of the blocks) and
+                        // accumulate; the MMA of the new blocks overwrites them at
+                        // the chunk's first k-step.
 #pragma unroll
                         for (int kk = 0; kk < C::BK / 16; ++kk) {
+                            int covered = -1;
 #pragma unroll
                             for (int i = 0; i < C::S; ++i) {
-#pragma unroll
-                                for (int j = 0; j < C::S; ++j) {
-                                    const int q = i + j;
-                                    if (q > C::QMAX) continue;
-                                    const int cl = C::cls(q);
-                                    // the first product of a class in the chunk overwrites its
-                                    // accumulator: issue order is kk, i, j, so that is the pair
-                                    // with the smallest i of the class at kk = 0
-                                    const int i_first = cl < C::NX ? (cl < C::S ? 0 : cl - (C::S - 1))
-                                                                   : (C::NX < C::S ? 0 : C::NX - (C::S - 1));
-                                    const bool first = chunk_start && kk == 0 && i == i_first &&
-                                                       (cl < C::NX || j == C::NX - i_first);
-                                    const uint64_t ad = a0 + (uint64_t)((i * C::ATILE + kk * 32) >> 4);
-                                    const uint64_t bd = b0 + (uint64_t)((j * C::BTILE + kk * 32) >> 4);
-                                    mma_bf16(dbase + cl * C::BN, ad, bd, idesc, first ? 0u : 1u);
-                                }
+                                const int jmax = min(C::S - 1, C::QMAX - i);
+                                if (jmax < 0) continue;
+                                const uint64_t ad = a0 + (uint64_t)((i * C::ATILE + kk * 32) >> 4);
+                                const int jold = min(jmax, covered - i);        // j = 0..jold accumulate
+                                if (jold >= 0)
+                                    mma_bf16(dbase + i * C::BN, ad, b0 + (uint64_t)((kk * 32) >> 4),
+                                             idesc_bf16(BM, (jold + 1) * C::BN), 1u);
+                                const int jnew = max(0, covered - i + 1);       // j = jnew..jmax are new
+                                if (jnew <= jmax)
+                                    mma_bf16(dbase + (i + jnew) * C::BN, ad,
+                                             b0 + (uint64_t)((jnew * C::BTILE + kk * 32) >> 4),
+                                             idesc_bf16(BM, (jmax - jnew + 1) * C::BN),
+                                             (chunk_start && kk == 0) ? 0u : 1u);
+                                covered = max(covered, i + jmax);
                             }
                         }
                         mma_commit(&empty[st]);
@@ -662,7 +672,8 @@ __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restri
 #pragma unroll
                             for (int q = 0; q < C::NX; ++q) v += __float2ll_rn(a[q][e] * C::DRAIN_SCALE);
                             iacc[c0 + e] += v;
-                            if constexpr (C::NQ > C::NX) macc[c0 + e] += a[C::NX][e];
+#pragma unroll
+                            for (int q = C::NX; q < C::NQ; ++q) macc[c0 + e] += a[q][e];
                         }
                     } else {
 #pragma unroll
@@ -757,13 +768,12 @@ __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restri
 // Narrow tiles waste less on the thin operands of small molecules; wide ones
 // reuse each A tile over more columns. The autotuner (choose_variant) picks one
 // per plan group, precision mode and size class.
-using Low64 = Cfg<3, 3, 1, 64, 2, 8, 8, 64, 64>;
 using Low32 = Cfg<3, 3, 1, 32, 3, 8, 4, 64, 64>;
+using LowS3 = Cfg<3, 3, 1, 64, 3, 8, 8, 64, 16>;       // three stages (a 16-row staging strip)
 using Mid48 = Cfg<4, 3, 2, 48, 2, 6, 8, 64, 32>;
 using Mid32 = Cfg<4, 3, 2, 32, 2, 6, 4, 64, 64>;
 using High32 = Cfg<5, 4, 3, 32, 3, 8, 4, 32, 64>;
 using Exact16 = Cfg<7, 6, 5, 16, 3, 6, 4, 32, 32>;
-
 struct Variant {
     int S, BN, BK, products, smem;
     cudaError_t (*attr)();
@@ -788,7 +798,7 @@ constexpr int MAX_VARIANTS = 3;
 static const int kNumVariants[4] = {3, 3, 2, 2};
 static const Variant &variant_of(int mode, int k)
 {
-    static const Variant table[4][MAX_VARIANTS] = {{variant<Low>(), variant<Low64>(), variant<Low32>()},
+    static const Variant table[4][MAX_VARIANTS] = {{variant<Low>(), variant<Low32>(), variant<LowS3>()},
                                                    {variant<Mid>(), variant<Mid48>(), variant<Mid32>()},
                                                    {variant<High>(), variant<High32>(), variant<High32>()},
                                                    {variant<Exact>(), variant<Exact16>(), variant<Exact16>()}};
@@ -1329,7 +1339,7 @@ int variants(int mode, int *bn, int cap)
 // whose device memory belongs to their own pool allocator, or that must not
 // let a cudaFree synchronise the device. Every GPU that loads the library
 // holds the array until exit; its size bounds the problem: M, N, K <=
-// HX_NOALLOC_MAX_DIM (512), about 6.4 MB.
+// HX_NOALLOC_MAX_DIM (512), about 5.3 MB.
 namespace tc {
 namespace {
 

@@ -60,7 +60,7 @@ module helios_cc
     public :: hx_mlp_nparam, hx_ccsd_set_model, hx_ccsd_training_rows, hx_mlp_predict, hx_mlp_grad, hx_mlp_train
     public :: hx_ccsd_iterate, hx_ccsd_energy, hx_ccsd_solve, hx_ccsd_solve_batch, hx_ccsd_get_amplitudes
     public :: hx_ccsd_get_scf, hx_ccsd_trace, hx_ccsd_triples, hx_ccsd_timing, hx_ccsd_dims, hx_ccsd_cancel
-    public :: hx_ccsd_destroy, hx_gemm, hx_gemm_noalloc, hx_tile_table, hx_tile_table_load, hx_tile_variants
+    public :: hx_ccsd_destroy, hx_gemm, hx_gemm_tile, hx_gemm_noalloc, hx_tile_table, hx_tile_table_load, hx_tile_variants
     public :: hx_ccsd_tile_choices, hx_last_error
 
     interface
@@ -227,6 +227,14 @@ module helios_cc
             real(c_double), intent(in) :: a(*), b(*)
             real(c_double), intent(out) :: c(*)
             integer(c_int32_t), value :: m, n, k, precision, reps
+            real(c_double), intent(out) :: ms
+        end function
+
+        integer(c_int) function hx_gemm_tile(a, b, c, m, n, k, precision, variant, reps, ms) bind(c, name='hx_gemm_tile')
+            import :: c_int, c_int32_t, c_double
+            real(c_double), intent(in) :: a(*), b(*)
+            real(c_double), intent(out) :: c(*)
+            integer(c_int32_t), value :: m, n, k, precision, variant, reps
             real(c_double), intent(out) :: ms
         end function
 

@@ -253,6 +253,12 @@ void hx_ccsd_destroy(hx_ccsd *h);
  * *ms (if not NULL) receives the mean device time per launch. */
 int hx_gemm(const double *A, const double *B, double *C, int32_t M, int32_t N, int32_t K, int32_t precision,
             int32_t reps, double *ms);
+/* hx_gemm on tile candidate `variant` (0 .. hx_tile_variants(mode) - 1) of
+ * the tensor-core precision's mode, -1 for the default; no counterpart in the
+ * reference (it measures the candidates the tile autotuner chooses from).
+ * Every candidate forms the same sums. */
+int hx_gemm_tile(const double *A, const double *B, double *C, int32_t M, int32_t N, int32_t K, int32_t precision,
+                 int32_t variant, int32_t reps, double *ms);
 
 /* Allocation-free variant of hx_gemm; it has no counterpart in the
  * reference. For callers that cannot allocate device memory at call time: a
@@ -263,7 +269,7 @@ int hx_gemm(const double *A, const double *B, double *C, int32_t M, int32_t N, i
  * (A: M x K, B: N x K, C: M x N), always on the tcgen05 exact-slice GEMM
  * (precision 1: 3 slices, 2: 5 slices; FP64 is rejected). It calls no
  * allocator: the operand slices, row exponents, error word and descriptors
- * live in one static device array of about 6.4 MB, whose address is looked
+ * live in one static device array of about 5.3 MB, whose address is looked
  * up once per device (cudaGetSymbolAddress) on the first call; make that
  * first call before any stream capture. The address is kept for the life of
  * the library, so a device reset (cudaDeviceReset) while the library is

@@ -65,8 +65,8 @@ def test_tile_table_selection_logic(lib, tmp_path):
     # range checks, the shipped file format, and the keywords that steer it
     from helios_gb300 import api
     widths = [api.tile_variants(m) for m in range(4)]
-    assert [w[0] for w in widths] == [96, 80, 64, 32]            # the defaults come first
-    assert all(len(w) >= 2 and sorted(w, reverse=True) == w for w in widths)
+    assert [w[0] for w in widths] == [64, 64, 48, 32]            # the defaults come first
+    assert all(len(w) >= 2 and all(x % 16 == 0 for x in w) for w in widths)
     assert lib.hx_tile_variants(4, None, 0) == -100
     before = dict(((e[0], e[1], e[2], e[3]), e[4]) for e in api.tile_table())
     api.load_tile_table([(0, 900, 7, 20, 1), (3, 901, 4, 10, 1)])
