@@ -216,7 +216,7 @@ class Keywords:
     enable_stagnation_check: bool = True         # iteration:enable-stagnation-check
     stagnation_threshold: float = 60.0           # iteration:stagnation-threshold
     stagnation_check_after: int = 200            # iteration:stagnation-check-after
-    precision: str = "fp64"                      # engine: "fp64" or "mixed"
+    precision: str = "fp64"                      # engine: "fp64", "mixed" or "exact" (7-slice emulated FP64 throughout)
     guess: str = "reference"                     # engine: "reference" (guessCC) or "learned"
     model: object = None                         # engine: learned-guess parameters (None = the shipped model)
     mixed_switch: float = 1e-3                   # engine: residual where 3-slice hands over to 4-slice
@@ -246,7 +246,7 @@ class Keywords:
         p.check_stagnation = int(self.enable_stagnation_check)
         p.stagnation_threshold = self.stagnation_threshold
         p.stagnation_after = self.stagnation_check_after
-        p.precision = {"fp64": 0, "mixed": 1}[self.precision]
+        p.precision = {"fp64": 0, "mixed": 1, "exact": 2}[self.precision]
         p.guess = {"reference": 0, "learned": 1}[self.guess]
         p.mixed_switch = self.mixed_switch
         p.mixed_patience = self.mixed_patience

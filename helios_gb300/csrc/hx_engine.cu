@@ -406,7 +406,7 @@ static int upload_masks(hx_ccsd *h)
 static const int kMoLadderMaxV = 32;
 static bool mo_ladder(const hx_ccsd *h, int mi)
 {
-    return h->p.precision == HX_PRECISION_MIXED && h->v[mi] <= kMoLadderMaxV;
+    return h->p.precision != HX_PRECISION_FP64 && h->v[mi] <= kMoLadderMaxV;
 }
 
 // Descriptors of every contraction of one iteration, for every molecule.
@@ -683,7 +683,10 @@ int hx_ccsd_create_batch(const hx_ppp_model *ms, int32_t n, const hx_cc_params *
     *out = nullptr;
     if (p->projection_type != 1 && p->projection_type != 2) { hx_set_error("projection-type must be 1 or 2"); return HX_ERR_ARG; }
     if (p->diis_enabled && (p->diis_steps < 2 || p->diis_steps > HX_MAX_DIIS)) { hx_set_error("diis-steps outside 2..%d", HX_MAX_DIIS); return HX_ERR_ARG; }
-    if (p->precision != HX_PRECISION_FP64 && p->precision != HX_PRECISION_MIXED) { hx_set_error("unknown precision mode"); return HX_ERR_ARG; }
+    if (p->precision != HX_PRECISION_FP64 && p->precision != HX_PRECISION_MIXED && p->precision != HX_PRECISION_EXACT) {
+        hx_set_error("unknown precision mode");
+        return HX_ERR_ARG;
+    }
     if (p->mixed_check != 0 && p->mixed_check != 1) { hx_set_error("mixed_check must be 0 (7-slice emulated FP64) or 1 (FP64)"); return HX_ERR_ARG; }
     if (p->tile_tuning < 0 || p->tile_tuning > 2 || p->tile_force < -1) { hx_set_error("tile_tuning must be 0, 1 or 2 and tile_force >= -1"); return HX_ERR_ARG; }
     int dev = 0;
@@ -721,7 +724,7 @@ int hx_ccsd_create_batch(const hx_ppp_model *ms, int32_t n, const hx_cc_params *
         rc = upload_group(g);
         if (rc < 0) { hx_ccsd_destroy(h); return rc; }
     }
-    if (p->precision == HX_PRECISION_MIXED) {
+    if (p->precision != HX_PRECISION_FP64) {
         rc = tc::create(&h->tce, h->plan, h->st, p->tile_tuning, p->tile_force);
         if (rc < 0) { hx_ccsd_destroy(h); return rc; }
     }
@@ -980,7 +983,8 @@ static int solve_all(hx_ccsd *h, int maxiter, double eps)
     std::vector<CtlMol> c(n);
     for (int mi = 0; mi < n; ++mi) {
         remaining += h->active[mi];
-        h->phase[mi] = mixed ? PH_LOW : PH_FP64;
+        // HX_PRECISION_EXACT: every iteration is a 7-slice (FP64-emulating) check iteration
+        h->phase[mi] = !mixed ? PH_FP64 : h->p.precision == HX_PRECISION_EXACT ? PH_EXACT : PH_LOW;
         h->fin_scale[mi] = 1.0;                  // (the first iteration's DIIS gates)
         CtlMol &x = c[mi];
         memset(&x, 0, sizeof(x));
@@ -992,6 +996,7 @@ static int solve_all(hx_ccsd *h, int maxiter, double eps)
         x.phase = h->phase[mi];
         x.best = 1e300;
         x.fin_scale = 1.0;
+        if (mixed && h->p.precision == HX_PRECISION_EXACT) x.fp_returns = kMaxFp64Returns;   // never back to 5 slices
         x.dcount = h->dcount[mi];
         for (int k = 0; k < HX_MAX_DIIS; ++k)
             x.slot_phase[k] = (signed char)(k < (int)h->slot_phase[mi].size() ? h->slot_phase[mi][k] : -1);

@@ -64,4 +64,86 @@ __host__ __device__ __forceinline__ void slice_digits(double x, int e, int *s)
     s[S - 1] = (int)A;
 }
 
+// FP32 bits, FP64 from bits, leading zeros of a 64-bit word, a right shift
+// that gives 0 for shift counts of 32 or more (host and device).
+__host__ __device__ __forceinline__ unsigned fbits(float x)
+{
+#ifdef __CUDA_ARCH__
+    return __float_as_uint(x);
+#else
+    unsigned b;
+    memcpy(&b, &x, sizeof b);
+    return b;
+#endif
+}
+__host__ __device__ __forceinline__ double dfrom(unsigned long long b)
+{
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double((long long)b);
+#else
+    double x;
+    memcpy(&x, &b, sizeof x);
+    return x;
+#endif
+}
+__host__ __device__ __forceinline__ int clz64(unsigned long long x)
+{
+#ifdef __CUDA_ARCH__
+    return __clzll((long long)x);
+#else
+    return __builtin_clzll(x);
+#endif
+}
+__host__ __device__ __forceinline__ unsigned shr_clamped(unsigned m, unsigned s)
+{
+#ifdef __CUDA_ARCH__
+    unsigned n;
+    asm("shr.b32 %0, %1, %2;" : "=r"(n) : "r"(m), "r"(s));
+    return n;
+#else
+    return s >= 32u ? 0u : m >> s;
+#endif
+}
+
+// GB300 issues about two FP64 instructions per clock per SM, so a GEMM
+// epilogue that converts, scales and stores every output in FP64 costs
+// several times the MMAs of a short-K product. The conversions below use
+// integer arithmetic on the bit patterns instead.
+//
+// x 2^k as an FP64 value, exactly, for a normal FP32 x and |k| <= 896 (the
+// result stays normal): the exponent rebiased, the significand widened;
+// a sign flip by `negmask` (0 or 0x80000000). Zero and FP32 subnormals give
+// 0 (a subnormal accumulator is below 2^-126 of its row scale).
+__host__ __device__ __forceinline__ double f2d_pow2(float x, int k, unsigned negmask)
+{
+    const unsigned u = fbits(x);
+    const unsigned e = (u >> 23) & 255u;
+    const unsigned hi32 = ((u & 0x80000000u) ^ negmask) | ((e + 896u + (unsigned)k) << 20) | ((u >> 3) & 0xFFFFFu);
+    const unsigned lo32 = u << 29;
+    return e == 0u ? 0.0 : dfrom(((unsigned long long)hi32 << 32) | lo32);
+}
+
+// x 2^k for a normal FP64 x whose result stays normal (an exponent add);
+// `ok` cleared otherwise.
+__host__ __device__ __forceinline__ double pow2_int(double x, int k, bool &ok)
+{
+    const unsigned long long b = dbits(x);
+    const int ex = (int)((b >> 52) & 2047);
+    if ((b << 1) == 0ull) return x;
+    if (ex == 0 || ex == 2047 || ex + k <= 0 || ex + k >= 2047) { ok = false; return 0.0; }
+    return dfrom(b + ((unsigned long long)(long long)k << 52));
+}
+
+// The count n of an exact class sum a = n 2^-8q (|n| < 2^24, an integer by
+// the chunk rule of the tensor-core GEMM) from its bit pattern: the
+// significand shifted right by the exponent's distance from the units
+// place (a shift of 32 or more gives 0, which covers a == 0).
+__host__ __device__ __forceinline__ int class_count(float a, int q)
+{
+    const unsigned u = fbits(a);
+    const unsigned m = (u & 0x7FFFFFu) | 0x800000u;
+    const unsigned n = shr_clamped(m, (unsigned)(150 - 8 * q) - ((u >> 23) & 255u));
+    return (u >> 31) ? -(int)n : (int)n;
+}
+
 }  // namespace tc

@@ -37,9 +37,10 @@
 //      FP32, M = 128, N = a multiple of BN, K = 16) into the class accumulators, alternating
 //      between two TMEM buffers per chunk; the epilogue warps drain a finished
 //      buffer with tcgen05.ld (a TMEM lane is an output row; the warps of a
-//      lane quarter split its columns) while the next chunk runs, then stage
-//      the tile in the idle ring and write C = alpha*2^(e_m+f_n-14)*(hi+lo) +
-//      beta*C in FP64 with consecutive threads on consecutive columns.
+//      lane quarter split its columns) while the next chunk runs, then write
+//      C = alpha*2^(e_m+f_n-14)*(hi+lo) + beta*C from registers, the FP64
+//      value built from the FP32 pair and the power of two by integer
+//      arithmetic (GB300's FP64 pipe is a small fraction of its integer rate).
 //   Every mbarrier wait is bounded by wall time; a wait that runs out records
 //   a code in a device error word and the CTA still frees its TMEM.
 #include <cuda.h>
@@ -88,7 +89,7 @@ namespace tc {
 //         blocks fit in TMEM.
 // These errors set the residual level a phase can reach (the GEMM outputs
 // are ~1e3-1e4 times the residual they cancel down to).
-template <int S_, int QMAX_, int NX_, int BN_, int STAGES_, int KC_, int EPIW_, int BK_, int STG_>
+template <int S_, int QMAX_, int NX_, int BN_, int STAGES_, int KC_, int EPIW_, int BK_>
 struct Cfg {
     static constexpr int S = S_;                     // integer slices per FP64 operand
     static constexpr int QMAX = QMAX_;               // slice pairs with i + j <= QMAX are multiplied
@@ -105,8 +106,7 @@ struct Cfg {
     static constexpr int ATILE = BM * BK * 2;        // bytes per A slice tile
     static constexpr int BTILE = BN * BK * 2;        // bytes per B slice tile
     static constexpr int STAGE_BYTES = S * (ATILE + BTILE);
-    static constexpr int STG_ROWS = STG_;            // output rows staged at a time
-    static constexpr int STG_BYTES = STG_ * (BN_ + 1) * 8 + 128 * 12;   // strip + row offsets and exponents
+    static constexpr int STG_BYTES = 128 * 12;       // column offsets and exponents of C
     static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + STG_BYTES + 1024 + 256;
     static constexpr int EPI_COLS = BN / (EPIW_ / 4); // columns drained per epilogue thread
     // 7-slice mode: the exact classes are drained into an int64 per element
@@ -120,19 +120,16 @@ struct Cfg {
     static_assert((long long)XPAIRS * KC_ * BK_ * 16384LL < (1LL << 24), "chunk too deep for exact sums");
     static_assert(BK_ == 64 || BK_ == 32, "k-block depth");
     static_assert(2 * NQ * BN_ <= 512, "two TMEM buffers must fit in 512 columns");
-    static_assert(STAGES_ * S_ * (128 * BK_ * 2 + BN_ * BK_ * 2) + STG_ * (BN_ + 1) * 8 + 128 * 12 + 1280 <= 232448,
-                  "shared memory");
-    static_assert(128 % STG_ == 0 && STG_ >= 8, "staging strip");
+    static_assert(STAGES_ * S_ * (128 * BK_ * 2 + BN_ * BK_ * 2) + 128 * 12 + 1280 <= 232448, "shared memory");
     static_assert(EPIW_ % 4 == 0 && EPI_COLS % 8 == 0, "epilogue split");
     static_assert(EPIW_ * 32 >= 128 && EPIW_ * 32 >= BN_, "epilogue threads cover the tile's rows and columns");
     // int64 drain: a chunk adds below 2^(24 + 8(NX-1) + 1); 32 chunks stay below 2^63
     static_assert(!INT_DRAIN || 24 + 8 * (NX_ - 1) + 1 + 5 < 63, "int64 drain headroom");
 };
-// (the strip heights are what each ring leaves of the 227 KB per CTA)
-using Low = Cfg<3, 3, 1, 64, 2, 8, 8, 64, 64>;
-using Mid = Cfg<4, 3, 2, 64, 2, 6, 8, 64, 16>;
-using High = Cfg<5, 4, 3, 48, 3, 8, 8, 32, 64>;
-using Exact = Cfg<7, 6, 5, 32, 3, 6, 8, 32, 32>;
+using Low = Cfg<3, 3, 1, 64, 2, 8, 8, 64>;
+using Mid = Cfg<4, 3, 2, 64, 2, 6, 8, 64>;
+using High = Cfg<5, 4, 3, 48, 3, 8, 8, 32>;
+using Exact = Cfg<7, 6, 5, 32, 3, 6, 8, 32>;
 constexpr int TMEM_COLS = 512;
 constexpr int BM = 128, KPAD = 64;   // K is padded to KPAD (the slicing tile depth)
 constexpr unsigned long long WAIT_NS = 4000000000ull; // a wait longer than 4 s is declared failed
@@ -142,6 +139,8 @@ struct TcDesc {
     int Mi, Ni;
     long long c[5];
     double alpha, beta;
+    int alpha_e, alpha_neg;          // alpha = (-1)^alpha_neg 2^alpha_e when alpha_pow2
+    int alpha_pow2, beta_one;        // beta_one: beta == 1 (C += r without a multiply)
     double *C;
     int tiles_m, tiles_n;
     long long tile_start;
@@ -266,6 +265,20 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v)
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
     for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// The same without the wait: several loads in flight, then tmem_wait_ld
+// on their registers (the wait names them, so no use moves above it).
+__device__ __forceinline__ void tmem_ld8_issue(uint32_t taddr, uint32_t *r)
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tmem_tie8(uint32_t *r)
+{
+    asm volatile("" : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]));
 }
 
 __device__ __forceinline__ long long split_off(int x, int xi, long long s0, long long s1)
@@ -506,18 +519,16 @@ __device__ __forceinline__ bool epilogue_all(bool v)
 // Persistent: CTA b computes tiles b, b + gridDim.x, ... The producer warp
 // streams k-blocks through the TMA ring and the MMA warp fills the two TMEM
 // buffers with one running count each across tiles, so loads and MMAs of the
-// next tile overlap the epilogue of the previous one; the epilogue stages the
-// output in its own shared-memory strip, STG_ROWS rows at a time.
+// next tile overlap the epilogue of the previous one; every epilogue thread
+// stores its own output row's columns straight from registers.
 template <class C>
 __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restrict__ descs, int ndesc, long long ntiles,
                                                         const int *__restrict__ active, int *err)
 {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    constexpr int LD = C::BN + 1;
-    double *strip = (double *)(smem + C::STAGES * C::STAGE_BYTES);   // [STG_ROWS][BN + 1] output staging
-    long long *srow = (long long *)(strip + C::STG_ROWS * LD);       // [BM] row offsets into C
-    int *sexp = (int *)(srow + BM);                                   // [BM] row exponents of A
+    long long *scol = (long long *)(smem + C::STAGES * C::STAGE_BYTES);   // [BN] column offsets into C
+    int *sexp = (int *)(scol + BM);                                   // [BN] column exponents of B
     uint64_t *full = (uint64_t *)(sexp + BM);
     uint64_t *empty = full + C::STAGES;
     uint64_t *acc_full = empty + C::STAGES;      // [2] MMA -> epilogue: chunk done in buffer b
@@ -632,10 +643,6 @@ __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restri
         const int row = (warp & 3) * 32 + lane;
         const int col0 = (warp >> 2) * C::EPI_COLS;
         const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
-        // store: one fixed column per thread (consecutive threads on
-        // consecutive n), rows RSTEP apart, U rows of C read ahead
-        constexpr int RSTEP = C::EPI_THREADS / C::BN, U = 4;
-        const int nn = threadIdx.x % C::BN, rr = threadIdx.x / C::BN;
         long long gc = 0;                                     // chunks drained so far
         for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
             const TileWork w = tile_work<C>(descs, ndesc, tile);
@@ -661,16 +668,26 @@ __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restri
                 for (int c0 = 0; c0 < C::EPI_COLS; c0 += 8) {
                     // chunk value of 8 columns: the classes (exact ones first) summed
                     // by TwoSum, then added into (hi, lo); rounding errors go to lo
-                    float a[C::NQ][8];
+                    // all classes of the 8 columns in flight, one wait
+                    uint32_t ra[C::NQ][8];
 #pragma unroll
                     for (int q = 0; q < C::NQ; ++q)
-                        tmem_ld8(tmem + lane_base + (uint32_t)(buf * C::NQ * C::BN + q * C::BN + col0 + c0), a[q]);
+                        tmem_ld8_issue(tmem + lane_base + (uint32_t)(buf * C::NQ * C::BN + q * C::BN + col0 + c0), ra[q]);
+                    tmem_wait_ld();
+                    float a[C::NQ][8];
+#pragma unroll
+                    for (int q = 0; q < C::NQ; ++q) {
+                        tmem_tie8(ra[q]);
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) a[q][e] = __uint_as_float(ra[q][e]);
+                    }
                     if constexpr (C::INT_DRAIN) {
 #pragma unroll
                         for (int e = 0; e < 8; ++e) {
-                            long long v = 0;
+                            // sum of n_q 2^8(NX-1-q) (Horner), integer arithmetic only
+                            long long v = class_count(a[0][e], 0);
 #pragma unroll
-                            for (int q = 0; q < C::NX; ++q) v += __float2ll_rn(a[q][e] * C::DRAIN_SCALE);
+                            for (int q = 1; q < C::NX; ++q) v = v * 256 + class_count(a[q][e], q);
                             iacc[c0 + e] += v;
 #pragma unroll
                             for (int q = C::NX; q < C::NQ; ++q) macc[c0 + e] += a[q][e];
@@ -702,52 +719,67 @@ __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restri
                     }
                 }
             }
-            // the tile is drained: row offsets and exponents of C, then the
-            // valid rows STG_ROWS at a time through the strip
+            // the tile is drained: every thread stores its own row's columns
+            // straight from registers (C = alpha 2^(e_m + f_n - 14) x + beta C);
+            // the column exponents and offsets of C are staged in shared memory
             const int mv = min(BM, d.M - w.tm * BM), nv = min(C::BN, d.N - w.tn * C::BN);
-            if (threadIdx.x < mv) {
-                const int m = w.tm * BM + threadIdx.x;
-                srow[threadIdx.x] = split_off(m, d.Mi, d.c[0], d.c[1]);
-                sexp[threadIdx.x] = d.expA[(long long)w.bt * d.Mp + m];
+            if (threadIdx.x < nv) {
+                const int n = w.tn * C::BN + threadIdx.x;
+                scol[threadIdx.x] = (long long)w.bt * d.c[4] + split_off(n, d.Ni, d.c[2], d.c[3]);
+                sexp[threadIdx.x] = d.expB[(long long)w.bt * d.Np + n];
             }
-            int eb = 0;
-            double *Cn = nullptr;
-            if (rr < RSTEP && nn < nv) {
-                const int n = w.tn * C::BN + nn;
-                eb = d.expB[(long long)w.bt * d.Np + n];
-                Cn = d.C + (long long)w.bt * d.c[4] + split_off(n, d.Ni, d.c[2], d.c[3]);
-            }
-            const bool load_c = d.ksplit == 1 && d.beta != 0.0;
-            for (int r0 = 0; r0 < mv; r0 += C::STG_ROWS) {
-                if (row >= r0 && row < r0 + C::STG_ROWS) {
+            asm volatile("bar.sync 1, %0;" ::"r"(C::EPI_THREADS) : "memory");
+            if (ok && row < mv) {
+                const int m = w.tm * BM + row;
+                const int ea = d.expA[(long long)w.bt * d.Mp + m];
+                double *Crow = d.C + split_off(m, d.Mi, d.c[0], d.c[1]);
+                const bool load_c = d.ksplit == 1 && d.beta != 0.0;
+                const uint32_t negmask = d.alpha_neg ? 0x80000000u : 0u;
+                // beta != 0: the old values of C are read eight at a time, the
+                // next eight in flight while these are converted and stored
+                // (one load round trip per element would bound the epilogue)
+                constexpr int GE = 8, NG = C::EPI_COLS / GE;
+                double cur[GE], nxt[GE];
 #pragma unroll
-                    for (int e = 0; e < C::EPI_COLS; ++e)
-                        strip[(row - r0) * LD + col0 + e] =
-                            C::INT_DRAIN ? (dacc[e] + (double)iacc[e]) / (double)C::DRAIN_SCALE + (double)macc[e]
-                                         : (double)hi[e] + (double)lo[e];
+                for (int e = 0; e < GE; ++e) {
+                    const int col = col0 + e;
+                    cur[e] = (load_c && col < nv) ? Crow[scol[col]] : 0.0;
                 }
-                asm volatile("bar.sync 1, %0;" ::"r"(C::EPI_THREADS) : "memory");
-                const int rend = min(r0 + C::STG_ROWS, mv);
-                if (ok && Cn) {
-                    for (int m0 = r0 + rr; m0 < rend; m0 += RSTEP * U) {
-                        double old[U];
 #pragma unroll
-                        for (int u = 0; u < U; ++u) {
-                            const int mm = m0 + u * RSTEP;
-                            old[u] = (load_c && mm < rend) ? Cn[srow[mm]] : 0.0;
-                        }
+                for (int g = 0; g < NG; ++g) {
 #pragma unroll
-                        for (int u = 0; u < U; ++u) {
-                            const int mm = m0 + u * RSTEP;
-                            if (mm >= rend) break;
-                            const double r = d.alpha * scale_pow2(strip[(mm - r0) * LD + nn], sexp[mm], eb);
-                            double *p = Cn + srow[mm];
-                            if (d.ksplit > 1) atomicAdd(p, r);
-                            else *p = load_c ? r + d.beta * old[u] : r;
-                        }
+                    for (int e = 0; e < GE; ++e) {
+                        const int col = col0 + (g + 1) * GE + e;
+                        nxt[e] = (g + 1 < NG && load_c && col < nv) ? Crow[scol[col]] : 0.0;
                     }
+#pragma unroll
+                    for (int e = 0; e < GE; ++e) {
+                        const int ie = g * GE + e, col = col0 + ie;
+                        if (col >= nv) break;
+                        const int eb = sexp[col];
+                        double r = 0.0;
+                        if (ea != INT_MIN && eb != INT_MIN) {
+                            const int k = ea + eb - 14 + d.alpha_e;
+                            bool fast = d.alpha_pow2 != 0 && k >= -896 && k <= 896;
+                            if constexpr (C::INT_DRAIN) {
+                                const double v = (dacc[ie] + (double)iacc[ie]) * (1.0 / (double)C::DRAIN_SCALE) + (double)macc[ie];
+                                if (fast) {
+                                    r = pow2_int(v, k, fast);
+                                    if (d.alpha_neg) r = -r;
+                                }
+                                if (!fast) r = d.alpha * scale_pow2(v, ea, eb);
+                            } else {
+                                if (fast) r = f2d_pow2(hi[ie], k, negmask) + f2d_pow2(lo[ie], k, negmask);
+                                else r = d.alpha * scale_pow2((double)hi[ie] + (double)lo[ie], ea, eb);
+                            }
+                        }
+                        double *p = Crow + scol[col];
+                        if (d.ksplit > 1) atomicAdd(p, r);
+                        else *p = load_c ? (d.beta_one ? r + cur[e] : fma(d.beta, cur[e], r)) : r;
+                    }
+#pragma unroll
+                    for (int e = 0; e < GE; ++e) cur[e] = nxt[e];
                 }
-                asm volatile("bar.sync 1, %0;" ::"r"(C::EPI_THREADS) : "memory");
             }
             ok = epilogue_all<C::EPI_THREADS>(ok);
             if (!ok) break;
@@ -762,18 +794,18 @@ __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restri
 
 // ------------------------------------------------------------------ tile-shape candidates
 // Every precision mode has a few configurations that differ only in the
-// output tile width BN (with the pipeline depth, staging strip and epilogue
+// output tile width BN (with the pipeline depth and epilogue
 // warps that fit it); slices, slice pairs, exact classes, k-block depth and
 // chunk length are the mode's own, so every candidate forms the same sums.
 // Narrow tiles waste less on the thin operands of small molecules; wide ones
 // reuse each A tile over more columns. The autotuner (choose_variant) picks one
 // per plan group, precision mode and size class.
-using Low32 = Cfg<3, 3, 1, 32, 3, 8, 4, 64, 64>;
-using LowS3 = Cfg<3, 3, 1, 64, 3, 8, 8, 64, 16>;       // three stages (a 16-row staging strip)
-using Mid48 = Cfg<4, 3, 2, 48, 2, 6, 8, 64, 32>;
-using Mid32 = Cfg<4, 3, 2, 32, 2, 6, 4, 64, 64>;
-using High32 = Cfg<5, 4, 3, 32, 3, 8, 4, 32, 64>;
-using Exact16 = Cfg<7, 6, 5, 16, 3, 6, 4, 32, 32>;
+using Low32 = Cfg<3, 3, 1, 32, 3, 8, 4, 64>;
+using LowS3 = Cfg<3, 3, 1, 64, 3, 8, 8, 64>;       // three stages
+using Mid48 = Cfg<4, 3, 2, 48, 2, 6, 8, 64>;
+using Mid32 = Cfg<4, 3, 2, 32, 2, 6, 4, 64>;
+using High32 = Cfg<5, 4, 3, 32, 3, 8, 4, 32>;
+using Exact16 = Cfg<7, 6, 5, 16, 3, 6, 4, 32>;
 struct Variant {
     int S, BN, BK, products, smem;
     cudaError_t (*attr)();
@@ -904,6 +936,20 @@ static int make_map(CUtensorMap *map, void *base, long long rows, int kp, int bo
 
 static inline long long rup(long long x, long long m) { return (x + m - 1) / m * m; }
 
+// alpha and beta of a descriptor, with the flags of the epilogue's integer
+// route: alpha = +-2^e (every coefficient of the CCSD plan) and beta == 1.
+static void set_scalars(TcDesc &d, double alpha, double beta)
+{
+    d.alpha = alpha;
+    d.beta = beta;
+    int e = 0;
+    const double f = std::frexp(std::fabs(alpha), &e);
+    d.alpha_pow2 = (alpha != 0.0 && f == 0.5) ? 1 : 0;
+    d.alpha_e = d.alpha_pow2 ? e - 1 : 0;
+    d.alpha_neg = alpha < 0.0 ? 1 : 0;
+    d.beta_one = beta == 1.0 ? 1 : 0;
+}
+
 // Which dimension of a source is contiguous: the one whose consecutive
 // elements are closer in memory.
 static int prep_rfast(const PrepDesc &p)
@@ -992,7 +1038,8 @@ static int build_sub(Engine *e, int mode, int var, const Group &g, SubGroup &sg)
         d.Mp = (int)rup(t.M, BM); d.Np = (int)rup(t.N, BN); d.Kp = (int)rup(t.K, KPAD);
         d.Mi = t.Mi; d.Ni = t.Ni;
         for (int k = 0; k < 5; ++k) d.c[k] = t.c[k];
-        d.alpha = t.alpha; d.beta = t.beta; d.C = t.C; d.mol = t.mol;
+        set_scalars(d, t.alpha, t.beta);
+        d.C = t.C; d.mol = t.mol;
         d.tiles_m = d.Mp / BM; d.tiles_n = d.Np / BN;
         // long K over few output tiles: cut K into slices that fill the GPU
         const int nkb = d.Kp / V.BK, n64 = d.Kp / KPAD;
@@ -1442,7 +1489,8 @@ extern "C" int hx_gemm_noalloc(const double *dA, const double *dB, double *dC, i
     d.Mp = (int)rup(M, BM); d.Np = (int)rup(N, BN); d.Kp = (int)rup(K, KPAD);
     d.Mi = M; d.Ni = N;
     d.c[0] = 0; d.c[1] = N; d.c[2] = 0; d.c[3] = 1; d.c[4] = 0;
-    d.alpha = 1.0; d.beta = 1.0; d.C = dC; d.mol = 0;
+    set_scalars(d, 1.0, 1.0);
+    d.C = dC; d.mol = 0;
     d.tiles_m = d.Mp / BM; d.tiles_n = d.Np / BN;
     d.kb_per = d.Kp / BK;            // K <= 512: at most 16 k-blocks, never split
     d.ksplit = 1;

@@ -204,9 +204,12 @@ class DeviceSigma:
 
     STEPS = (1.0, -1.0, 2.0, -2.0)
 
-    def __init__(self, mol: Molecule, keywords: api.Keywords, t1, t2, C0, nvec=1, h=1e-2, engine=None):
-        # the residual comes back through the "2-1" step: t2' = x2 + 3 Omega2 / D2
-        kw = replace(keywords, precision="fp64", guess="reference", t1_step=1.0, t2_step=1.0, projection_type="2-1")
+    def __init__(self, mol: Molecule, keywords: api.Keywords, t1, t2, C0, nvec=1, h=1e-2, engine=None,
+                 precision="exact"):
+        # the residual comes back through the "2-1" step: t2' = x2 + 3 Omega2 / D2; its
+        # contractions run on the 7-slice tensor-core GEMM, whose error is below the FP64
+        # GEMM's (precision "exact"), or on the FP64 CUDA cores ("fp64")
+        kw = replace(keywords, precision=precision, guess="reference", t1_step=1.0, t2_step=1.0, projection_type="2-1")
         self.cc = (engine or api.CoupledCluster)([mol] * (4 * nvec), kw)
         self.cc.initCC()
         self.t1, self.t2, self.h, self.nvec = t1, t2, h, nvec

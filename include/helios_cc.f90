@@ -27,7 +27,8 @@ module helios_cc
         HX_ERR_UNSUPPORTED = -106
     integer(c_int32_t), parameter, public :: HX_COULOMB_OHNO_KLOPMAN = 0, HX_COULOMB_MATAGA_NISHIMOTO = 1, &
         HX_COULOMB_HUBBARD = 2, HX_BOND_SINGLE = 0, HX_BOND_DOUBLE = 1, HX_BOND_NONSET = -1, &
-        HX_PRECISION_FP64 = 0, HX_PRECISION_MIXED = 1, HX_NOALLOC_MAX_DIM = 512
+        HX_PRECISION_FP64 = 0, HX_PRECISION_MIXED = 1, HX_PRECISION_EXACT = 2, &
+        HX_NOALLOC_MAX_DIM = 512
 
     ! one molecule block (readMoleculeInformation.f90:20-117); pointers to arrays
     ! the caller keeps alive: coords(3, n_sites), alpha, gamma, nels (n_sites),

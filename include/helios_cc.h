@@ -60,6 +60,7 @@ extern "C" {
 
 #define HX_PRECISION_FP64 0
 #define HX_PRECISION_MIXED 1
+#define HX_PRECISION_EXACT 2   /* every iteration on the 7-slice tensor-core GEMM that emulates FP64 */
 
 /* One molecule block of a helios input (src/input/readMoleculeInformation.f90:20-117). */
 typedef struct hx_ppp_model {
@@ -95,7 +96,7 @@ typedef struct hx_cc_params {
     int32_t check_stagnation;     /* iteration:enable-stagnation-check (1) */
     double stagnation_threshold;  /* iteration:stagnation-threshold, percent (60) */
     int32_t stagnation_after;     /* iteration:stagnation-check-after (200) */
-    int32_t precision;            /* HX_PRECISION_FP64 (default) or HX_PRECISION_MIXED */
+    int32_t precision;            /* HX_PRECISION_FP64 (default), HX_PRECISION_MIXED or HX_PRECISION_EXACT */
     int32_t guess;                /* 0 reference guess (guessCC), 1 learned guess */
     double mixed_switch;          /* mixed precision: residual at which a molecule moves from
                                      3-slice to 4-slice tensor-core iterations (1e-3); 4-slice

@@ -142,6 +142,21 @@ def test_mixed_precision_reaches_fp64_energy(api, accuracy):
         assert abs(mx["energy"][0] - e64["energy"][0]) < 1e-6
 
 
+def test_exact_precision_follows_the_fp64_iteration(api):
+    """precision "exact": every iteration on the 7-slice GEMM, whose error is below the
+    FP64 GEMM's, so the solve follows the FP64 one: same iteration count, same energy."""
+    for mol in (molecules.polyene(20), molecules.ladder(24)):
+        e64 = api.get_energy(mol, _kw(api, accuracy=12))
+        cc = api.CoupledCluster(mol, _kw(api, precision="exact", accuracy=12))
+        cc.initCC()
+        r = cc.iterate()
+        tr = cc.trace(0)
+        cc.finalizeCC()
+        assert r["status"] == 1 and np.all(tr[:, 4] == 1.0)
+        assert abs(r["iterations"] - e64["iterations"]) <= 1
+        assert abs(r["energy"][0] - e64["energy"][0]) < 1e-9
+
+
 def test_mixed_trace_starts_on_tensor_cores(api):
     cc = api.CoupledCluster(molecules.polyene(24), _kw(api, precision="mixed"))
     cc.initCC()

@@ -228,3 +228,61 @@ def test_tensor_core_slicing_is_an_exact_digit_expansion(tmp_path):
             assert max(abs(d) for d in digits) <= 128
             recon = sum(np.ldexp(float(d), -8 * p) for p, d in enumerate(digits))
             assert abs(recon - a) <= np.ldexp(1.0, -8 * (S - 1) - 1) * (1 + 1e-12)
+
+
+def test_epilogue_integer_conversions(tmp_path):
+    """The GEMM epilogue's integer routes (hx_slice.h) on the host: f2d_pow2
+    of hi and of lo, added in FP64, give (hi + lo) 2^k to within one FP64 ulp
+    (checked in exact rational arithmetic; FP32 subnormals count as zero);
+    pow2_int is an exact power-of-two scale; class_count recovers the integer
+    count of an exact class sum."""
+    import shutil
+    import subprocess
+    from fractions import Fraction
+    if shutil.which("g++") is None:
+        pytest.skip("no host C++ compiler")
+    exe = tmp_path / "epilogue_harness"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "helios_gb300", "csrc"),
+                    os.path.join(ROOT, "tests", "epilogue_harness.cpp"), "-o", str(exe)], check=True)
+    rng = np.random.default_rng(11)
+    f32 = lambda x: float(np.float32(x))
+    cases = []
+    for _ in range(3000):
+        hi = f32(rng.normal() * 2.0 ** rng.integers(-30, 30))
+        # lo below half an ulp of hi (what TwoSum leaves), or a little more
+        lo = f32(hi * rng.uniform(-1, 1) * 2.0 ** -float(rng.integers(22, 60)))
+        cases.append((hi, lo, int(rng.integers(-896, 897)), int(rng.integers(0, 2))))
+    cases += [(0.0, 0.0, 3, 0), (0.0, 1.5, -2, 1), (1.0, 0.0, 0, 0), (-1.0, 2.0 ** -30, 5, 0),
+              (1.0, -(2.0 ** -25), 0, 0), (2.0 ** -126, 0.0, 0, 0), (1e-45, 0.0, 0, 0),
+              (1.0, 1.0, 0, 0), (3.0, 2.0 ** -100, 896, 0), (f32(3.4e38), 2.0 ** 100, 896, 0),
+              (2.0 ** -126, 2.0 ** -126, -896, 1)]
+    inp = "".join(f"f {hi.hex()} {lo.hex()} {k} {n}\n" for hi, lo, k, n in cases)
+    xs = [(float(rng.normal() * 10.0 ** rng.integers(-200, 200)), int(rng.integers(-300, 300))) for _ in range(500)]
+    xs += [(0.0, 7), (-0.0, -7), (5e-324, 3), (1e308, 100), (1.0, -1100)]
+    inp += "".join(f"p {x.hex()} {k}\n" for x, k in xs)
+    cs = []
+    for _ in range(2000):
+        q = int(rng.integers(0, 7))
+        n = int(rng.integers(-(2 ** 24) + 1, 2 ** 24))
+        cs.append((n, q))
+    cs += [(0, 0), (0, 6), (1, 6), (-1, 0), (2 ** 24 - 1, 3), (-(2 ** 24 - 1), 5)]
+    inp += "".join(f"c {float(np.ldexp(np.float32(n), -8 * q)).hex()} {q}\n" for n, q in cs)
+    out = subprocess.run([str(exe)], input=inp, capture_output=True, text=True, check=True).stdout.split("\n")
+    for (hi, lo, k, n), line in zip(cases, out):
+        ok, val = line.split()
+        flush = lambda x: 0.0 if abs(x) < 2.0 ** -126 else x
+        exact = (Fraction(flush(hi)) + Fraction(flush(lo))) * Fraction(2) ** k * (-1 if n else 1)
+        got = Fraction(float.fromhex(val))
+        assert abs(got - exact) <= abs(exact) * Fraction(2) ** -52, (hi, lo, k, n, val)
+    off = len(cases)
+    for (x, k), line in zip(xs, out[off:]):
+        ok, val = line.split()
+        with np.errstate(over="ignore"):
+            ref = np.ldexp(x, k)
+        if ok == "1":
+            assert float.fromhex(val) == ref
+        else:
+            assert not np.isfinite(ref) or abs(ref) < 2.3e-308 or abs(x) < 2.3e-308
+    off += len(xs)
+    for (n, q), line in zip(cs, out[off:]):
+        assert int(line) == n

@@ -24,7 +24,8 @@ def lr():
     return lrccsd
 
 
-def test_device_sigma_is_the_closed_shell_jacobian(lr):
+@pytest.mark.parametrize("precision", ["exact", "fp64"])
+def test_device_sigma_is_the_closed_shell_jacobian(lr, precision):
     from helios_gb300 import api
     from oracle import lrccsd as olr
     from oracle.ppp import build_model
@@ -37,7 +38,7 @@ def test_device_sigma_is_the_closed_shell_jacobian(lr):
     s = cc.scf(0)
     cc.finalizeCC()
     o, v = t1.shape
-    sig = lr.DeviceSigma(mol, kw, t1, t2, s["C"], nvec=2)
+    sig = lr.DeviceSigma(mol, kw, t1, t2, s["C"], nvec=2, precision=precision)
     rng = np.random.default_rng(5)
     vecs = []
     for _ in range(2):
