@@ -37,9 +37,10 @@
 //      FP32, M = 128, N = a multiple of BN, K = 16) into the class accumulators, alternating
 //      between two TMEM buffers per chunk; the epilogue warps drain a finished
 //      buffer with tcgen05.ld (a TMEM lane is an output row; the warps of a
-//      lane quarter split its columns) while the next chunk runs, then write
-//      C = alpha*2^(e_m+f_n-14)*(hi+lo) + beta*C from registers, the FP64
-//      value built from the FP32 pair and the power of two by integer
+//      lane quarter split its columns) while the next chunk runs, then stage
+//      the (hi, lo) pairs in shared memory and write C = alpha*2^(e_m+f_n-14)*
+//      (hi+lo) + beta*C with consecutive threads on consecutive columns, the
+//      FP64 value built from the FP32 pair and the power of two by integer
 //      arithmetic (GB300's FP64 pipe is a small fraction of its integer rate).
 //   Every mbarrier wait is bounded by wall time; a wait that runs out records
 //   a code in a device error word and the CTA still frees its TMEM.
@@ -106,7 +107,16 @@ struct Cfg {
     static constexpr int ATILE = BM * BK * 2;        // bytes per A slice tile
     static constexpr int BTILE = BN * BK * 2;        // bytes per B slice tile
     static constexpr int STAGE_BYTES = S * (ATILE + BTILE);
-    static constexpr int STG_BYTES = 128 * 12;       // column offsets and exponents of C
+    // output staging strip: (hi, lo) pairs of STG_ROWS rows (all 128 where the
+    // ring leaves room), row offsets and exponents of C
+    static constexpr int RING_BYTES = STAGES * S * (128 * BK * 2 + BN * BK * 2);
+    static constexpr int STG_ROWS = [] {
+        const int avail = 232448 - 1280 - 128 * 12 - STAGES_ * S_ * (128 * BK_ * 2 + BN_ * BK_ * 2);
+        int r = 128;
+        while (r > 8 && r * (BN_ + 1) * 8 > avail) r >>= 1;
+        return r;
+    }();
+    static constexpr int STG_BYTES = STG_ROWS * (BN_ + 1) * 8 + 128 * 12;
     static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + STG_BYTES + 1024 + 256;
     static constexpr int EPI_COLS = BN / (EPIW_ / 4); // columns drained per epilogue thread
     // 7-slice mode: the exact classes are drained into an int64 per element
@@ -120,7 +130,8 @@ struct Cfg {
     static_assert((long long)XPAIRS * KC_ * BK_ * 16384LL < (1LL << 24), "chunk too deep for exact sums");
     static_assert(BK_ == 64 || BK_ == 32, "k-block depth");
     static_assert(2 * NQ * BN_ <= 512, "two TMEM buffers must fit in 512 columns");
-    static_assert(STAGES_ * S_ * (128 * BK_ * 2 + BN_ * BK_ * 2) + 128 * 12 + 1280 <= 232448, "shared memory");
+    static_assert(RING_BYTES + STG_BYTES + 1280 <= 232448, "shared memory");
+    static_assert(STG_ROWS * (BN_ + 1) * 8 <= 232448 - 1280 - 128 * 12 - RING_BYTES, "staging strip");
     static_assert(EPIW_ % 4 == 0 && EPI_COLS % 8 == 0, "epilogue split");
     static_assert(EPIW_ * 32 >= 128 && EPIW_ * 32 >= BN_, "epilogue threads cover the tile's rows and columns");
     // int64 drain: a chunk adds below 2^(24 + 8(NX-1) + 1); 32 chunks stay below 2^63
@@ -312,9 +323,19 @@ struct PrepDesc {
     long long s[5];                  // r0, r1, k0, k1, batch strides of the FP64 source
     long long work_start;            // prefix of tiles (batch * ceil(Rp/PT_R) * Kp/PT_K) over the launch
     long long row_start;             // prefix of batch*Rp over the launch
+    long long band_start;            // prefix of bands (batch * ceil(Rp/rb)) over the launch
     int mol;
     int rfast;                       // rows (1) or k (0) are the contiguous dimension of the source
+    int rb;                          // rows per band (slice_band), 0: sliced by row_scale + split_gather
 };
+
+// Operands whose padded K is at most BAND_KP are sliced in one pass by
+// slice_band: rb rows x the whole K staged in shared memory (at most
+// BAND_ELEMS doubles), so the row maxima come from the staged band and the
+// FP64 source is read once; wider operands take row_scale + split_gather.
+constexpr int BAND_KP = 1024, BAND_ELEMS = 8192;
+constexpr int BAND_SMEM = (BAND_ELEMS + 64) * 8 + BAND_KP * 8 + 32 * 8 + 32 * 4 + 16;
+__host__ __device__ constexpr int band_rows(int Kp) { return Kp <= 256 ? 32 : Kp <= 512 ? 16 : Kp <= BAND_KP ? 8 : 0; }
 
 __device__ __forceinline__ int find_desc(const PrepDesc *pd, int n, long long w)
 {
@@ -341,6 +362,7 @@ __device__ __forceinline__ bool load_tile(const PrepDesc *__restrict__ pd, int n
     __syncthreads();
     const PrepDesc &d = pd[t.desc];
     if (active && !active[d.mol]) return false;
+    if (d.rb) return false;                              // sliced by slice_band (holds no tiles)
     if (skip_single && d.Kp == PT_K) return false;      // split_gather scales these rows itself
     long long local = u - d.work_start;
     const int tk = d.Kp / PT_K, tr = (d.Rp + PT_R - 1) / PT_R;
@@ -374,7 +396,7 @@ __global__ void rexp_init(const PrepDesc *__restrict__ pd, int n, long long rows
             if (pd[mid].row_start <= w) lo = mid; else hi = mid - 1;
         }
         const PrepDesc &d = pd[lo];
-        if (active && !active[d.mol]) continue;
+        if ((active && !active[d.mol]) || d.rb) continue;   // slice_band writes its own exponents
         d.rexp[w - d.row_start] = INT_MIN;
     }
 }
@@ -468,6 +490,100 @@ __global__ void __launch_bounds__(PT_THREADS) split_gather(const PrepDesc *__res
     }
 }
 
+// One pass for operands with Kp <= BAND_KP: each unit is a band of rb rows
+// over the whole K, staged in shared memory (reads coalesced along the
+// source's contiguous dimension); a warp per row takes the row's largest
+// magnitude (bit patterns, sign cleared) and its exponent, then the slices
+// are written for every (row, 8-k chunk) of the band, each slice of the
+// band one contiguous run of [rb][Kp] bf16.
+__device__ __forceinline__ int find_band(const PrepDesc *pd, int n, long long w)
+{
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (pd[mid].band_start <= w) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int S>
+__global__ void __launch_bounds__(PT_THREADS) slice_band(const PrepDesc *__restrict__ pd, int n, long long units,
+                                                         const int *__restrict__ active)
+{
+    extern __shared__ __align__(16) unsigned char band_raw[];
+    double *x = (double *)band_raw;                                   // [rb][Kp + 2] (rows padded: fewer bank conflicts)
+    long long *koff = (long long *)(x + BAND_ELEMS + 64);             // [Kp]
+    long long *roff = koff + BAND_KP;                                 // [rb]
+    int *rexp_s = (int *)(roff + 32);                                 // [rb]
+    int *sdesc = rexp_s + 32;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (long long u = blockIdx.x; u < units; u += gridDim.x) {
+        if (threadIdx.x == 0) *sdesc = find_band(pd, n, u);
+        __syncthreads();
+        const PrepDesc &d = pd[*sdesc];
+        if (d.rb == 0 || (active && !active[d.mol])) { __syncthreads(); continue; }
+        const int rb = d.rb, Kp = d.Kp, ld = Kp + 2;
+        const int nb = (d.Rp + rb - 1) / rb;
+        const long long local = u - d.band_start;
+        const int b = (int)(local / nb), r0 = (int)(local % nb) * rb;
+        for (int k = threadIdx.x; k < Kp; k += PT_THREADS) koff[k] = k < d.K ? split_off(k, d.Ki, d.s[2], d.s[3]) : 0;
+        if (threadIdx.x < rb) roff[threadIdx.x] = split_off(r0 + threadIdx.x, d.Ri, d.s[0], d.s[1]) + (long long)b * d.s[4];
+        __syncthreads();
+        const int rlim = min(rb, d.R - r0), total = rb * Kp;
+        for (int e = threadIdx.x; e < total; e += PT_THREADS) {
+            int r, k;
+            if (d.rfast) { r = e % rb; k = e / rb; } else { k = e % Kp; r = e / Kp; }
+            x[r * ld + k] = (r < rlim && k < d.K) ? __ldg(d.src + roff[r] + koff[k]) : 0.0;
+        }
+        __syncthreads();
+        for (int r = warp; r < rb; r += PT_THREADS / 32) {
+            unsigned long long mb = 0;
+            for (int k = lane; k < Kp; k += 32) {
+                const unsigned long long v = dbits(x[r * ld + k]) & 0x7FFFFFFFFFFFFFFFull;
+                mb = v > mb ? v : mb;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const unsigned long long v = __shfl_xor_sync(0xffffffffu, mb, o);
+                mb = v > mb ? v : mb;
+            }
+            if (lane == 0) {
+                rexp_s[r] = mb ? exp_of_bits(mb) : 0;
+                if (r < rlim) d.rexp[(long long)b * d.Rp + r0 + r] = mb ? exp_of_bits(mb) : INT_MIN;
+            }
+        }
+        __syncthreads();
+        const int chunks = total / 8, cpr = Kp / 8;
+        const long long plane = (long long)d.batch * d.Rp * Kp;
+        for (int c = threadIdx.x; c < chunks; c += PT_THREADS) {
+            const int r = c / cpr, k8 = (c % cpr) * 8;
+            if (r0 + r >= d.Rp) continue;                   // a last band past the padded rows
+            const int e = rexp_s[r];
+            double v[8];
+#pragma unroll
+            for (int q = 0; q < 8; q += 2) {
+                const double2 w2 = *reinterpret_cast<const double2 *>(x + r * ld + k8 + q);
+                v[q] = w2.x;
+                v[q + 1] = w2.y;
+            }
+            __align__(16) __nv_bfloat16 out[S][8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                int dg[S];
+                slice_digits<S>(v[q], e, dg);
+#pragma unroll
+                for (int p = 0; p < S; ++p)
+                    out[p][q] = __float2bfloat16_rn((float)dg[p] * (p == 0 ? 1.f : __int_as_float((127 - 8 * p) << 23)));
+            }
+            const long long off = ((long long)b * d.Rp + r0 + r) * Kp + k8;
+#pragma unroll
+            for (int p = 0; p < S; ++p)
+                *reinterpret_cast<uint4 *>(d.dst + p * plane + off) = *reinterpret_cast<const uint4 *>(out[p]);
+        }
+        __syncthreads();
+    }
+}
+
 // ------------------------------------------------------------------ the GEMM
 // Work of one output tile: its problem, batch entry, tile row and column,
 // k-block range and chunks (grouped rasterisation: 16 tile-rows per group
@@ -519,16 +635,20 @@ __device__ __forceinline__ bool epilogue_all(bool v)
 // Persistent: CTA b computes tiles b, b + gridDim.x, ... The producer warp
 // streams k-blocks through the TMA ring and the MMA warp fills the two TMEM
 // buffers with one running count each across tiles, so loads and MMAs of the
-// next tile overlap the epilogue of the previous one; every epilogue thread
-// stores its own output row's columns straight from registers.
+// next tile overlap the epilogue of the previous one; the epilogue stages the
+// tile's (hi, lo) pairs in its own shared-memory strip and stores C with
+// consecutive threads on consecutive columns.
 template <class C>
 __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restrict__ descs, int ndesc, long long ntiles,
                                                         const int *__restrict__ active, int *err)
 {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    long long *scol = (long long *)(smem + C::STAGES * C::STAGE_BYTES);   // [BN] column offsets into C
-    int *sexp = (int *)(scol + BM);                                   // [BN] column exponents of B
+    constexpr int LD = C::BN + 1;
+    float2 *strip = (float2 *)(smem + C::STAGES * C::STAGE_BYTES);   // [STG_ROWS][BN + 1] (hi, lo) of the outputs
+    double *dstrip = (double *)strip;                                 // the same, 7-slice values
+    long long *srow = (long long *)(strip + C::STG_ROWS * LD);       // [BM] row offsets into C
+    int *sexp = (int *)(srow + BM);                                   // [BM] row exponents of A
     uint64_t *full = (uint64_t *)(sexp + BM);
     uint64_t *empty = full + C::STAGES;
     uint64_t *acc_full = empty + C::STAGES;      // [2] MMA -> epilogue: chunk done in buffer b
@@ -643,6 +763,13 @@ __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restri
         const int row = (warp & 3) * 32 + lane;
         const int col0 = (warp >> 2) * C::EPI_COLS;
         const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+        // store: one fixed column per thread (consecutive threads on
+        // consecutive n), rows RSTEP apart; all of a thread's rows of a strip
+        // pass (up to 32) read from C before any is stored, so the reads of
+        // C cost one round trip per pass (the drain's registers are free then)
+        constexpr int RSTEP = C::EPI_THREADS / C::BN;
+        constexpr int U = (C::STG_ROWS + RSTEP - 1) / RSTEP < 32 ? (C::STG_ROWS + RSTEP - 1) / RSTEP : 32;
+        const int nn = threadIdx.x % C::BN, rr = threadIdx.x / C::BN;
         long long gc = 0;                                     // chunks drained so far
         for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
             const TileWork w = tile_work<C>(descs, ndesc, tile);
@@ -719,67 +846,76 @@ __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restri
                     }
                 }
             }
-            // the tile is drained: every thread stores its own row's columns
-            // straight from registers (C = alpha 2^(e_m + f_n - 14) x + beta C);
-            // the column exponents and offsets of C are staged in shared memory
+            // the tile is drained: the (hi, lo) pairs go through a shared-memory
+            // strip (STG_ROWS rows at a time, all 128 where the ring leaves room)
+            // so that consecutive threads store consecutive columns of C;
+            // C = alpha 2^(e_m + f_n - 14) x + beta C with the power of two and
+            // a power-of-two alpha applied by exponent arithmetic
             const int mv = min(BM, d.M - w.tm * BM), nv = min(C::BN, d.N - w.tn * C::BN);
-            if (threadIdx.x < nv) {
-                const int n = w.tn * C::BN + threadIdx.x;
-                scol[threadIdx.x] = (long long)w.bt * d.c[4] + split_off(n, d.Ni, d.c[2], d.c[3]);
-                sexp[threadIdx.x] = d.expB[(long long)w.bt * d.Np + n];
+            if (threadIdx.x < mv) {
+                const int m = w.tm * BM + threadIdx.x;
+                srow[threadIdx.x] = split_off(m, d.Mi, d.c[0], d.c[1]);
+                sexp[threadIdx.x] = d.expA[(long long)w.bt * d.Mp + m];
             }
-            asm volatile("bar.sync 1, %0;" ::"r"(C::EPI_THREADS) : "memory");
-            if (ok && row < mv) {
-                const int m = w.tm * BM + row;
-                const int ea = d.expA[(long long)w.bt * d.Mp + m];
-                double *Crow = d.C + split_off(m, d.Mi, d.c[0], d.c[1]);
-                const bool load_c = d.ksplit == 1 && d.beta != 0.0;
-                const uint32_t negmask = d.alpha_neg ? 0x80000000u : 0u;
-                // beta != 0: the old values of C are read eight at a time, the
-                // next eight in flight while these are converted and stored
-                // (one load round trip per element would bound the epilogue)
-                constexpr int GE = 8, NG = C::EPI_COLS / GE;
-                double cur[GE], nxt[GE];
+            int eb = INT_MIN;
+            double *Cn = nullptr;
+            if (rr < RSTEP && nn < nv) {
+                const int n = w.tn * C::BN + nn;
+                eb = d.expB[(long long)w.bt * d.Np + n];
+                Cn = d.C + (long long)w.bt * d.c[4] + split_off(n, d.Ni, d.c[2], d.c[3]);
+            }
+            const bool load_c = d.ksplit == 1 && d.beta != 0.0;
+            const uint32_t negmask = d.alpha_neg ? 0x80000000u : 0u;
+            for (int r0 = 0; r0 < mv; r0 += C::STG_ROWS) {
+                if (row >= r0 && row < r0 + C::STG_ROWS) {
 #pragma unroll
-                for (int e = 0; e < GE; ++e) {
-                    const int col = col0 + e;
-                    cur[e] = (load_c && col < nv) ? Crow[scol[col]] : 0.0;
-                }
-#pragma unroll
-                for (int g = 0; g < NG; ++g) {
-#pragma unroll
-                    for (int e = 0; e < GE; ++e) {
-                        const int col = col0 + (g + 1) * GE + e;
-                        nxt[e] = (g + 1 < NG && load_c && col < nv) ? Crow[scol[col]] : 0.0;
+                    for (int e = 0; e < C::EPI_COLS; ++e) {
+                        if constexpr (C::INT_DRAIN)
+                            dstrip[(row - r0) * LD + col0 + e] =
+                                (dacc[e] + (double)iacc[e]) * (1.0 / (double)C::DRAIN_SCALE) + (double)macc[e];
+                        else
+                            strip[(row - r0) * LD + col0 + e] = make_float2(hi[e], lo[e]);
                     }
+                }
+                asm volatile("bar.sync 1, %0;" ::"r"(C::EPI_THREADS) : "memory");
+                const int rend = min(r0 + C::STG_ROWS, mv);
+                if (ok && Cn) {
+                    for (int m0 = r0 + rr; m0 < rend; m0 += RSTEP * U) {
+                        double old[U];
 #pragma unroll
-                    for (int e = 0; e < GE; ++e) {
-                        const int ie = g * GE + e, col = col0 + ie;
-                        if (col >= nv) break;
-                        const int eb = sexp[col];
-                        double r = 0.0;
-                        if (ea != INT_MIN && eb != INT_MIN) {
-                            const int k = ea + eb - 14 + d.alpha_e;
-                            bool fast = d.alpha_pow2 != 0 && k >= -896 && k <= 896;
-                            if constexpr (C::INT_DRAIN) {
-                                const double v = (dacc[ie] + (double)iacc[ie]) * (1.0 / (double)C::DRAIN_SCALE) + (double)macc[ie];
-                                if (fast) {
-                                    r = pow2_int(v, k, fast);
-                                    if (d.alpha_neg) r = -r;
-                                }
-                                if (!fast) r = d.alpha * scale_pow2(v, ea, eb);
-                            } else {
-                                if (fast) r = f2d_pow2(hi[ie], k, negmask) + f2d_pow2(lo[ie], k, negmask);
-                                else r = d.alpha * scale_pow2((double)hi[ie] + (double)lo[ie], ea, eb);
-                            }
+                        for (int u = 0; u < U; ++u) {
+                            const int mm = m0 + u * RSTEP;
+                            old[u] = (load_c && mm < rend) ? Cn[srow[mm]] : 0.0;
                         }
-                        double *p = Crow + scol[col];
-                        if (d.ksplit > 1) atomicAdd(p, r);
-                        else *p = load_c ? (d.beta_one ? r + cur[e] : fma(d.beta, cur[e], r)) : r;
-                    }
 #pragma unroll
-                    for (int e = 0; e < GE; ++e) cur[e] = nxt[e];
+                        for (int u = 0; u < U; ++u) {
+                            const int mm = m0 + u * RSTEP;
+                            if (mm >= rend) break;
+                            const int ea = sexp[mm];
+                            double r = 0.0;
+                            if (ea != INT_MIN && eb != INT_MIN) {
+                                const int k = ea + eb - 14 + d.alpha_e;
+                                bool fast = d.alpha_pow2 != 0 && k >= -896 && k <= 896;
+                                if constexpr (C::INT_DRAIN) {
+                                    const double v = dstrip[(mm - r0) * LD + nn];
+                                    if (fast) {
+                                        r = pow2_int(v, k, fast);
+                                        if (d.alpha_neg) r = -r;
+                                    }
+                                    if (!fast) r = d.alpha * scale_pow2(v, ea, eb);
+                                } else {
+                                    const float2 v = strip[(mm - r0) * LD + nn];
+                                    if (fast) r = f2d_pow2(v.x, k, negmask) + f2d_pow2(v.y, k, negmask);
+                                    else r = d.alpha * scale_pow2((double)v.x + (double)v.y, ea, eb);
+                                }
+                            }
+                            double *p = Cn + srow[mm];
+                            if (d.ksplit > 1) atomicAdd(p, r);
+                            else *p = load_c ? (d.beta_one ? r + old[u] : fma(d.beta, old[u], r)) : r;
+                        }
+                    }
                 }
+                asm volatile("bar.sync 1, %0;" ::"r"(C::EPI_THREADS) : "memory");
             }
             ok = epilogue_all<C::EPI_THREADS>(ok);
             if (!ok) break;
@@ -838,10 +974,10 @@ static const Variant &variant_of(int mode, int k)
 }
 
 // ------------------------------------------------------------------ host side
-struct PrepList {                    // operands sliced by one pair of launches
+struct PrepList {                    // operands sliced by one set of launches
     std::vector<PrepDesc> h;
     PrepDesc *d = nullptr;
-    long long work = 0, rows = 0;
+    long long work = 0, rows = 0, bands = 0;
 };
 
 struct SubGroup {                    // one plan group in one precision mode and tile variant
@@ -958,21 +1094,48 @@ static int prep_rfast(const PrepDesc &p)
     return std::llabs(rs) < std::llabs(ks) ? 1 : 0;
 }
 
-// Row exponents then slices of one list of operands (n descriptors, `tiles`
+template <int S>
+static cudaError_t band_attr()
+{
+    return cudaFuncSetAttribute(slice_band<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, BAND_SMEM);
+}
+// shared memory of every slice_band instance (once per device)
+static cudaError_t band_attrs()
+{
+    cudaError_t r = band_attr<Low::S>();
+    if (r == cudaSuccess) r = band_attr<Mid::S>();
+    if (r == cudaSuccess) r = band_attr<High::S>();
+    if (r == cudaSuccess) r = band_attr<Exact::S>();
+    return r;
+}
+
+// Slices of one list of operands (n descriptors): the banded ones in one
+// pass (`bands` units), the others by row exponents then slices (`tiles`
 // PT_R x PT_K tiles, `rows` padded rows).
-static cudaError_t prep_launch(const PrepDesc *d, int n, long long tiles, long long rows, int S, const int *active,
-                               cudaStream_t s)
+static cudaError_t prep_launch(const PrepDesc *d, int n, long long tiles, long long rows, long long bands, int S,
+                               const int *active, cudaStream_t s, int nsm = 152)
 {
     if (n == 0) return cudaSuccess;
-    const unsigned rb = (unsigned)std::min<long long>((rows + 255) / 256, 1 << 14);
-    const unsigned tb = (unsigned)std::min<long long>(tiles, 1 << 16);
-    rexp_init<<<rb, 256, 0, s>>>(d, n, rows, active);
-    row_scale<<<tb, PT_THREADS, 0, s>>>(d, n, tiles, active);
-    if (S == Low::S) split_gather<Low::S><<<tb, PT_THREADS, 0, s>>>(d, n, tiles, active);
-    else if (S == Mid::S) split_gather<Mid::S><<<tb, PT_THREADS, 0, s>>>(d, n, tiles, active);
-    else if (S == High::S) split_gather<High::S><<<tb, PT_THREADS, 0, s>>>(d, n, tiles, active);
-    else split_gather<Exact::S><<<tb, PT_THREADS, 0, s>>>(d, n, tiles, active);
-    hx_count_launches(3);
+    if (tiles > 0) {
+        const unsigned rb = (unsigned)std::min<long long>((rows + 255) / 256, 1 << 14);
+        const unsigned tb = (unsigned)std::min<long long>(tiles, 1 << 16);
+        rexp_init<<<rb, 256, 0, s>>>(d, n, rows, active);
+        row_scale<<<tb, PT_THREADS, 0, s>>>(d, n, tiles, active);
+        if (S == Low::S) split_gather<Low::S><<<tb, PT_THREADS, 0, s>>>(d, n, tiles, active);
+        else if (S == Mid::S) split_gather<Mid::S><<<tb, PT_THREADS, 0, s>>>(d, n, tiles, active);
+        else if (S == High::S) split_gather<High::S><<<tb, PT_THREADS, 0, s>>>(d, n, tiles, active);
+        else split_gather<Exact::S><<<tb, PT_THREADS, 0, s>>>(d, n, tiles, active);
+        hx_count_launches(3);
+    }
+    if (bands > 0) {
+        // three bands of up to 64 KB per SM
+        const unsigned g = (unsigned)std::min<long long>(bands, 3LL * nsm);
+        if (S == Low::S) slice_band<Low::S><<<g, PT_THREADS, BAND_SMEM, s>>>(d, n, bands, active);
+        else if (S == Mid::S) slice_band<Mid::S><<<g, PT_THREADS, BAND_SMEM, s>>>(d, n, bands, active);
+        else if (S == High::S) slice_band<High::S><<<g, PT_THREADS, BAND_SMEM, s>>>(d, n, bands, active);
+        else slice_band<Exact::S><<<g, PT_THREADS, BAND_SMEM, s>>>(d, n, bands, active);
+        hx_count_launches(1);
+    }
     return cudaGetLastError();
 }
 
@@ -1078,8 +1241,11 @@ static int build_sub(Engine *e, int mode, int var, const Group &g, SubGroup &sg)
         auto add = [&](PrepList &L, PrepDesc p) {
             p.work_start = L.work;
             p.row_start = L.rows;
+            p.band_start = L.bands;
             p.rfast = prep_rfast(p);
-            L.work += (long long)p.batch * ((p.Rp + PT_R - 1) / PT_R) * (p.Kp / PT_K);
+            p.rb = band_rows(p.Kp);
+            if (p.rb) L.bands += (long long)p.batch * ((p.Rp + p.rb - 1) / p.rb);
+            else L.work += (long long)p.batch * ((p.Rp + PT_R - 1) / PT_R) * (p.Kp / PT_K);
             L.rows += (long long)p.batch * p.Rp;
             L.h.push_back(p);
         };
@@ -1128,12 +1294,13 @@ static cudaError_t run_sub(Engine *e, SubGroup &sg, int mode, const int *d_activ
     // constant slices are made once per initialisation, for every molecule
     // (molecules enter a mode at different iterations)
     if (sg.fixed_gen != e->generation) {
-        if ((r = prep_launch(sg.fixed.d, (int)sg.fixed.h.size(), sg.fixed.work, sg.fixed.rows, V.S, nullptr, s)) != cudaSuccess)
+        if ((r = prep_launch(sg.fixed.d, (int)sg.fixed.h.size(), sg.fixed.work, sg.fixed.rows, sg.fixed.bands, V.S,
+                             nullptr, s, e->nsm)) != cudaSuccess)
             return r;
         sg.fixed_gen = e->generation;
     }
-    if ((r = prep_launch(sg.var_ops.d, (int)sg.var_ops.h.size(), sg.var_ops.work, sg.var_ops.rows, V.S, d_active, s)) !=
-        cudaSuccess)
+    if ((r = prep_launch(sg.var_ops.d, (int)sg.var_ops.h.size(), sg.var_ops.work, sg.var_ops.rows, sg.var_ops.bands,
+                         V.S, d_active, s, e->nsm)) != cudaSuccess)
         return r;
     hx_count_launches(1);
     Engine::Pending pend{};
@@ -1273,6 +1440,11 @@ int create(Engine **out, const std::vector<Group> &plan, cudaStream_t s, int tun
                 hx_set_error("cannot reserve shared memory for tc_gemm");
                 return HX_ERR_CUDA;
             }
+    if (band_attrs() != cudaSuccess) {
+        destroy(e);
+        hx_set_error("cannot reserve shared memory for slice_band");
+        return HX_ERR_CUDA;
+    }
     for (int md = 0; md < 4; ++md)
         for (size_t gi = 0; gi < plan.size(); ++gi) {
             if (only_mode >= 0 && md != only_mode) { e->mode[md].groups.emplace_back(); continue; }
@@ -1306,7 +1478,7 @@ cudaError_t prepare_fixed(Engine *e, cudaStream_t s)
         for (SubGroup &sg : e->mode[md].groups) {
             if (sg.tiles == 0 || sg.fixed_gen == e->generation) continue;
             const cudaError_t r = prep_launch(sg.fixed.d, (int)sg.fixed.h.size(), sg.fixed.work, sg.fixed.rows,
-                                              variant_of(md, sg.var).S, nullptr, s);
+                                              sg.fixed.bands, variant_of(md, sg.var).S, nullptr, s, e->nsm);
             if (r != cudaSuccess) return r;
             sg.fixed_gen = e->generation;
         }
@@ -1434,7 +1606,8 @@ int na_setup(unsigned char **base)
             return HX_ERR_CUDA;
         }
         if (cudaFuncSetAttribute(tc_gemm<Low>, cudaFuncAttributeMaxDynamicSharedMemorySize, Low::SMEM_BYTES) != cudaSuccess ||
-            cudaFuncSetAttribute(tc_gemm<High>, cudaFuncAttributeMaxDynamicSharedMemorySize, High::SMEM_BYTES) != cudaSuccess) {
+            cudaFuncSetAttribute(tc_gemm<High>, cudaFuncAttributeMaxDynamicSharedMemorySize, High::SMEM_BYTES) != cudaSuccess ||
+            band_attrs() != cudaSuccess) {
             hx_set_error("hx_gemm_noalloc: cannot reserve shared memory for tc_gemm");
             return HX_ERR_CUDA;
         }
@@ -1507,12 +1680,13 @@ extern "C" int hx_gemm_noalloc(const double *dA, const double *dB, double *dC, i
     p[1].src = dB; p[1].dst = bbuf; p[1].rexp = bexp; p[1].R = N; p[1].Rp = d.Np; p[1].Ri = N;
     p[0].rfast = prep_rfast(p[0]);
     p[1].rfast = prep_rfast(p[1]);
-    const long long atiles = (long long)((d.Mp + PT_R - 1) / PT_R) * (d.Kp / PT_K);
-    const long long btiles = (long long)((d.Np + PT_R - 1) / PT_R) * (d.Kp / PT_K);
-    p[1].work_start = atiles;
+    // K <= 512: both operands are sliced in one pass, in bands of rb rows
+    const int rb = band_rows(d.Kp);
+    p[0].rb = p[1].rb = rb;
+    p[1].band_start = (d.Mp + rb - 1) / rb;
     p[1].row_start = d.Mp;
     const long long rows = (long long)d.Mp + d.Np;
-    const long long work = atiles + btiles;
+    const long long bands = p[1].band_start + (d.Np + rb - 1) / rb;
     const long long tiles = (long long)d.tiles_m * d.tiles_n;
 
     // what must start at zero: the error word and C (accumulated with beta = 1)
@@ -1521,7 +1695,7 @@ extern "C" int hx_gemm_noalloc(const double *dA, const double *dB, double *dC, i
     if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_tcd, &d, sizeof(d), cudaMemcpyHostToDevice, s);
     if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_prep, p, sizeof(p), cudaMemcpyHostToDevice, s);
     if (ce == cudaSuccess) {
-        ce = prep_launch(d_prep, 2, work, rows, S, nullptr, s);
+        ce = prep_launch(d_prep, 2, 0, rows, bands, S, nullptr, s);
         // one CTA per tile (the kernel's tile loop then runs once per CTA)
         if (ce == cudaSuccess && high) tc_gemm<High><<<(unsigned)tiles, High::NTHREADS, High::SMEM_BYTES, s>>>(d_tcd, 1, tiles, nullptr, err);
         else if (ce == cudaSuccess) tc_gemm<Low><<<(unsigned)tiles, Low::NTHREADS, Low::SMEM_BYTES, s>>>(d_tcd, 1, tiles, nullptr, err);
