@@ -64,6 +64,59 @@ __host__ __device__ __forceinline__ void slice_digits(double x, int e, int *s)
     s[S - 1] = (int)A;
 }
 
+// The same digits with fewer operations. The top-down peel leaves, below
+// every digit position 8j, the centered residue L_j of A modulo 2^8j (in
+// [-2^(8j-1), 2^(8j-1))), so digit k from the bottom is (L_(k+1) - L_k) 2^-8k
+// and the top digit (A - L_(S-1)) 2^-F: one residue per digit from A's
+// words (32-bit operations up to 8j = 32) instead of S-1 rounds of 64-bit
+// add, shift and subtract.
+template <int S>
+__host__ __device__ __forceinline__ void slice_digits_fast(double x, int e, int *s)
+{
+    constexpr int F = 8 * (S - 1);
+    const unsigned long long bits = dbits(x);
+    const int ex = (int)((bits >> 52) & 0x7FF);
+    const long long mant = (long long)(bits & 0xFFFFFFFFFFFFFull) | (ex ? (1LL << 52) : 0LL);
+    const int sh = (ex ? ex : 1) - 1075 + 7 - e + F;       // A = mant 2^sh = a 2^F
+    long long A;
+    if (mant == 0 || sh < -62) A = 0;
+    else if (sh >= 0) A = mant << sh;
+    else A = (mant + (1LL << (-sh - 1))) >> (-sh);
+    if (bits >> 63) A = -A;
+    const unsigned lo = (unsigned)A;
+    long long Lprev = 0;
+#pragma unroll
+    for (int k = 0; k < S - 1; ++k) {
+        const int w = 8 * (k + 1);                             // residue modulo 2^w
+        long long L;
+        if (w < 32) L = (long long)(int)((lo + (1u << (w - 1))) & ((1u << w) - 1u)) - (1LL << (w - 1));
+        else if (w == 32) L = (long long)(int)lo;
+        else L = ((A + (1LL << (w - 1))) & ((1LL << w) - 1)) - (1LL << (w - 1));
+        s[S - 1 - k] = w < 32 ? (int)((int)(L - Lprev) >> (8 * k)) : (int)((L - Lprev) >> (8 * k));
+        Lprev = L;
+    }
+    s[0] = (int)((A - Lprev) >> F);
+}
+
+// bf16 bit pattern of s 2^-8p for an integer |s| <= 128 (exact): s is
+// placed in the significand of the float 1.5 2^(23-8p), whose unit in the
+// last place is 2^-8p, and the offset subtracted -- an integer add and an
+// FP32 subtract instead of an int-to-float conversion.
+__host__ __device__ __forceinline__ float digit_value(int s, int p)
+{
+    const unsigned mb = (unsigned)(150 - 8 * p) << 23 | 0x400000u;    // bits of 1.5 2^(23-8p)
+    float m, v;
+    const unsigned b = mb + (unsigned)s;
+#ifdef __CUDA_ARCH__
+    m = __uint_as_float(mb);
+    v = __uint_as_float(b);
+#else
+    memcpy(&m, &mb, sizeof m);
+    memcpy(&v, &b, sizeof v);
+#endif
+    return v - m;
+}
+
 // FP32 bits, FP64 from bits, leading zeros of a 64-bit word, a right shift
 // that gives 0 for shift counts of 32 or more (host and device).
 __host__ __device__ __forceinline__ unsigned fbits(float x)

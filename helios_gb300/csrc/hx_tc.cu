@@ -308,6 +308,25 @@ __device__ __forceinline__ double scale_pow2(double x, int ea, int eb)
     return ldexp(x, e);
 }
 
+// Slices of eight consecutive values of a row with exponent e, as S
+// 16-byte groups of bf16 (s_p 2^-8p, exact): digits from the residue form,
+// values by an integer add and an FP32 subtract, packed two at a time.
+template <int S>
+__device__ __forceinline__ void slice8(const double *v, int e, uint4 *out)
+{
+    __nv_bfloat162 w[S][4];
+#pragma unroll
+    for (int q = 0; q < 8; q += 2) {
+        int d0[S], d1[S];
+        slice_digits_fast<S>(v[q], e, d0);
+        slice_digits_fast<S>(v[q + 1], e, d1);
+#pragma unroll
+        for (int p = 0; p < S; ++p) w[p][q / 2] = __floats2bfloat162_rn(digit_value(d0[p], p), digit_value(d1[p], p));
+    }
+#pragma unroll
+    for (int p = 0; p < S; ++p) out[p] = *reinterpret_cast<const uint4 *>(w[p]);
+}
+
 // ------------------------------------------------------------------ split + gather
 // Both kernels walk the operand in tiles of PT_R rows x PT_K k staged in
 // shared memory: the global reads run along whichever of the two dimensions
@@ -470,20 +489,15 @@ __global__ void __launch_bounds__(PT_THREADS) split_gather(const PrepDesc *__res
                 if (e == INT_MIN) e = 0;
             }
             if (in_rows) {
-                __align__(16) __nv_bfloat16 out[S][8];
+                double v[8];
 #pragma unroll
-                for (int q = 0; q < 8; ++q) {
-                    int dg[S];
-                    slice_digits<S>(t.x[rr][c8 + q], e, dg);
-#pragma unroll
-                    for (int p = 0; p < S; ++p)                     // s_p 2^-8p, exact in bf16
-                        out[p][q] = __float2bfloat16_rn((float)dg[p] * (p == 0 ? 1.f : __int_as_float((127 - 8 * p) << 23)));
-                }
+                for (int q = 0; q < 8; ++q) v[q] = t.x[rr][c8 + q];
+                uint4 out[S];
+                slice8<S>(v, e, out);
                 const long long plane = (long long)d.batch * d.Rp * d.Kp;
                 const long long off = ((long long)b * d.Rp + r0 + rr) * d.Kp + k0 + c8;
 #pragma unroll
-                for (int p = 0; p < S; ++p)
-                    *reinterpret_cast<uint4 *>(d.dst + p * plane + off) = *reinterpret_cast<const uint4 *>(out[p]);
+                for (int p = 0; p < S; ++p) *reinterpret_cast<uint4 *>(d.dst + p * plane + off) = out[p];
             }
         }
         __syncthreads();
@@ -529,11 +543,20 @@ __global__ void __launch_bounds__(PT_THREADS) slice_band(const PrepDesc *__restr
         for (int k = threadIdx.x; k < Kp; k += PT_THREADS) koff[k] = k < d.K ? split_off(k, d.Ki, d.s[2], d.s[3]) : 0;
         if (threadIdx.x < rb) roff[threadIdx.x] = split_off(r0 + threadIdx.x, d.Ri, d.s[0], d.s[1]) + (long long)b * d.s[4];
         __syncthreads();
-        const int rlim = min(rb, d.R - r0), total = rb * Kp;
-        for (int e = threadIdx.x; e < total; e += PT_THREADS) {
-            int r, k;
-            if (d.rfast) { r = e % rb; k = e / rb; } else { k = e % Kp; r = e / Kp; }
-            x[r * ld + k] = (r < rlim && k < d.K) ? __ldg(d.src + roff[r] + koff[k]) : 0.0;
+        const int rlim = min(rb, d.R - r0), total = rb * Kp, K = d.K;
+        const double *__restrict__ src = d.src;
+        if (d.rfast) {
+            // rows contiguous in the source: consecutive threads on consecutive rows
+            const int lrb = rb == 32 ? 5 : rb == 16 ? 4 : 3;
+            for (int e = threadIdx.x; e < total; e += PT_THREADS) {
+                const int r = e & (rb - 1), k = e >> lrb;
+                x[r * ld + k] = (r < rlim && k < K) ? __ldg(src + roff[r] + koff[k]) : 0.0;
+            }
+        } else {
+            // k contiguous: consecutive threads on consecutive k of a row
+            for (int r = 0; r < rb; ++r)
+                for (int k = threadIdx.x; k < Kp; k += PT_THREADS)
+                    x[r * ld + k] = (r < rlim && k < K) ? __ldg(src + roff[r] + koff[k]) : 0.0;
         }
         __syncthreads();
         for (int r = warp; r < rb; r += PT_THREADS / 32) {
@@ -553,12 +576,14 @@ __global__ void __launch_bounds__(PT_THREADS) slice_band(const PrepDesc *__restr
             }
         }
         __syncthreads();
-        const int chunks = total / 8, cpr = Kp / 8;
+        // (row, 8-k chunk) c of the band, walked without divisions: c advances by
+        // the block size, its row and k by the block size's quotient and rest
+        const int cpr = Kp / 8, rows_band = min(rb, d.Rp - r0);
+        const int dr = PT_THREADS / cpr, dk = (PT_THREADS % cpr) * 8;
         const long long plane = (long long)d.batch * d.Rp * Kp;
-        for (int c = threadIdx.x; c < chunks; c += PT_THREADS) {
-            const int r = c / cpr, k8 = (c % cpr) * 8;
-            if (r0 + r >= d.Rp) continue;                   // a last band past the padded rows
-            const int e = rexp_s[r];
+        __nv_bfloat16 *__restrict__ dst = d.dst + ((long long)b * d.Rp + r0) * Kp;
+        int r = threadIdx.x / cpr, k8 = (threadIdx.x % cpr) * 8;
+        while (r < rows_band) {
             double v[8];
 #pragma unroll
             for (int q = 0; q < 8; q += 2) {
@@ -566,19 +591,13 @@ __global__ void __launch_bounds__(PT_THREADS) slice_band(const PrepDesc *__restr
                 v[q] = w2.x;
                 v[q + 1] = w2.y;
             }
-            __align__(16) __nv_bfloat16 out[S][8];
+            uint4 out[S];
+            slice8<S>(v, rexp_s[r], out);
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                int dg[S];
-                slice_digits<S>(v[q], e, dg);
-#pragma unroll
-                for (int p = 0; p < S; ++p)
-                    out[p][q] = __float2bfloat16_rn((float)dg[p] * (p == 0 ? 1.f : __int_as_float((127 - 8 * p) << 23)));
-            }
-            const long long off = ((long long)b * d.Rp + r0 + r) * Kp + k8;
-#pragma unroll
-            for (int p = 0; p < S; ++p)
-                *reinterpret_cast<uint4 *>(d.dst + p * plane + off) = *reinterpret_cast<const uint4 *>(out[p]);
+            for (int p = 0; p < S; ++p) *reinterpret_cast<uint4 *>(dst + p * plane + (long long)r * Kp + k8) = out[p];
+            r += dr;
+            k8 += dk;
+            if (k8 >= Kp) { k8 -= Kp; ++r; }
         }
         __syncthreads();
     }
