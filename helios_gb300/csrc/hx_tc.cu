@@ -352,9 +352,9 @@ struct PrepDesc {
 // slice_band: rb rows x the whole K staged in shared memory (at most
 // BAND_ELEMS doubles), so the row maxima come from the staged band and the
 // FP64 source is read once; wider operands take row_scale + split_gather.
-constexpr int BAND_KP = 1024, BAND_ELEMS = 8192;
+constexpr int BAND_KP = 1024, BAND_ELEMS = 4096;
 constexpr int BAND_SMEM = (BAND_ELEMS + 64) * 8 + BAND_KP * 8 + 32 * 8 + 32 * 4 + 16;
-__host__ __device__ constexpr int band_rows(int Kp) { return Kp <= 256 ? 32 : Kp <= 512 ? 16 : Kp <= BAND_KP ? 8 : 0; }
+__host__ __device__ constexpr int band_rows(int Kp) { return Kp <= 128 ? 32 : Kp <= 256 ? 16 : Kp <= 512 ? 8 : Kp <= BAND_KP ? 4 : 0; }
 
 __device__ __forceinline__ int find_desc(const PrepDesc *pd, int n, long long w)
 {
@@ -521,7 +521,7 @@ __device__ __forceinline__ int find_band(const PrepDesc *pd, int n, long long w)
 }
 
 template <int S>
-__global__ void __launch_bounds__(PT_THREADS) slice_band(const PrepDesc *__restrict__ pd, int n, long long units,
+__global__ void __launch_bounds__(PT_THREADS, 4) slice_band(const PrepDesc *__restrict__ pd, int n, long long units,
                                                          const int *__restrict__ active)
 {
     extern __shared__ __align__(16) unsigned char band_raw[];
@@ -545,18 +545,31 @@ __global__ void __launch_bounds__(PT_THREADS) slice_band(const PrepDesc *__restr
         __syncthreads();
         const int rlim = min(rb, d.R - r0), total = rb * Kp, K = d.K;
         const double *__restrict__ src = d.src;
-        if (d.rfast) {
-            // rows contiguous in the source: consecutive threads on consecutive rows
-            const int lrb = rb == 32 ? 5 : rb == 16 ? 4 : 3;
-            for (int e = threadIdx.x; e < total; e += PT_THREADS) {
-                const int r = e & (rb - 1), k = e >> lrb;
-                x[r * ld + k] = (r < rlim && k < K) ? __ldg(src + roff[r] + koff[k]) : 0.0;
+        // element e of the band: rows contiguous in the source (rfast): row e % rb,
+        // k e / rb (consecutive threads on consecutive rows); else row e / Kp, k
+        // e % Kp. Walked by the block size without divisions, the loads of
+        // eight steps in flight before their values go to shared memory.
+        {
+            const int lrb = rb == 32 ? 5 : rb == 16 ? 4 : rb == 8 ? 3 : 2;
+            int r = d.rfast ? (threadIdx.x & (rb - 1)) : threadIdx.x / Kp;
+            int k = d.rfast ? (threadIdx.x >> lrb) : threadIdx.x % Kp;
+            const int dr = d.rfast ? 0 : PT_THREADS / Kp, dk = d.rfast ? (PT_THREADS >> lrb) : PT_THREADS % Kp;
+            for (int e0 = 0; e0 < total; e0 += 8 * PT_THREADS) {
+                double buf[8];
+                int at[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const bool in = e0 + j * PT_THREADS + (int)threadIdx.x < total;
+                    at[j] = in ? r * ld + k : -1;
+                    buf[j] = (in && r < rlim && k < K) ? __ldg(src + roff[r] + koff[k]) : 0.0;
+                    r += dr;
+                    k += dk;
+                    if (!d.rfast && k >= Kp) { k -= Kp; ++r; }
+                }
+#pragma unroll
+                for (int j = 0; j < 8; ++j)
+                    if (at[j] >= 0) x[at[j]] = buf[j];
             }
-        } else {
-            // k contiguous: consecutive threads on consecutive k of a row
-            for (int r = 0; r < rb; ++r)
-                for (int k = threadIdx.x; k < Kp; k += PT_THREADS)
-                    x[r * ld + k] = (r < rlim && k < K) ? __ldg(src + roff[r] + koff[k]) : 0.0;
         }
         __syncthreads();
         for (int r = warp; r < rb; r += PT_THREADS / 32) {
@@ -1147,8 +1160,8 @@ static cudaError_t prep_launch(const PrepDesc *d, int n, long long tiles, long l
         hx_count_launches(3);
     }
     if (bands > 0) {
-        // three bands of up to 64 KB per SM
-        const unsigned g = (unsigned)std::min<long long>(bands, 3LL * nsm);
+        // four bands of up to 32 KB per SM
+        const unsigned g = (unsigned)std::min<long long>(bands, 4LL * nsm);
         if (S == Low::S) slice_band<Low::S><<<g, PT_THREADS, BAND_SMEM, s>>>(d, n, bands, active);
         else if (S == Mid::S) slice_band<Mid::S><<<g, PT_THREADS, BAND_SMEM, s>>>(d, n, bands, active);
         else if (S == High::S) slice_band<High::S><<<g, PT_THREADS, BAND_SMEM, s>>>(d, n, bands, active);
