@@ -18,11 +18,15 @@
 // the molecule's device state inside the kernel and the result goes straight
 // into t2.
 //
-// Training (hx_mlp_grad / hx_mlp_train): FP32 SIMT GEMMs with the same bf16
-// roundings as inference (W2, W3 and the activations entering layers 2 and
-// 3; straight-through in the backward pass), mean-squared error in units of
-// y_scale, Adam with a cosine learning-rate decay. The gradients are those
-// of the CPU reference in oracle/mlp.py.
+// Training (hx_mlp_grad / hx_mlp_train): the six 256-wide products of a step
+// (layers 2 and 3 forward, their weight gradients and the gradients of their
+// inputs) on the tensor cores (bgemm: bf16 operands brought in by TMA, FP32
+// accumulation in TMEM), with the same bf16 roundings as inference (W2, W3
+// and the activations entering layers 2 and 3) plus the loss gradients
+// entering those products (straight-through in the backward pass); the
+// 8-wide first layer, the output unit and the bias sums on the CUDA cores.
+// Mean-squared error in units of y_scale, Adam with a cosine learning-rate
+// decay. The gradients are those of the CPU reference in oracle/mlp.py.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
@@ -328,6 +332,157 @@ __global__ void __launch_bounds__(MLP_THREADS, 1) mlp_infer(InferArgs a, const _
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(H));
 }
 
+// ------------------------------------------------------------------ tcgen05 training GEMM
+// C[M x 256] = A[M x K] B[256 x K]^T (+ bias[n]) from bf16 operands, both
+// K-major (row m of A, row n of B, K contiguous), FP32 accumulation in 256
+// TMEM columns. CTA (x, y) = 128-row tile x a split of kb_per 64-deep
+// K-blocks; with more than one split the CTAs add into C with atomics (C
+// cleared first). Thread 0 streams the K-blocks with TMA through two
+// stages and issues the MMAs (M = 128, N = 256, K = 16); the four warps
+// then drain TMEM (a lane per row). Every wait is bounded; a CTA that gives
+// up records a code, waits (bounded) for the loads it issued and still
+// frees its TMEM.
+constexpr int BG_STAGE = A_KB + B_KB;                 // 16 KB of A + 32 KB of B per K-block
+constexpr int BG_SMEM = 1024 + 2 * BG_STAGE;
+constexpr int BG_THREADS = 128;
+
+__global__ void __launch_bounds__(BG_THREADS, 1) bgemm(const __grid_constant__ CUtensorMap mapA,
+                                                       const __grid_constant__ CUtensorMap mapB, float *C, int ldc,
+                                                       const float *bias, int nkb, int kb_per, int *err)
+{
+    extern __shared__ __align__(1024) uint8_t bg_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)bg_raw + 1023) & ~(uintptr_t)1023);
+    __shared__ __align__(8) uint64_t full[2], freed[2], done;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int s_abort;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int m0 = blockIdx.x * TILE;
+    const int kb0 = blockIdx.y * kb_per, n = min(nkb, kb0 + kb_per) - kb0;
+    if (tid == 0) {
+        s_abort = 0;
+        for (int q = 0; q < 2; ++q) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full[q])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&freed[q])));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&done)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(H));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+    if (tid == 0) {
+        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(H >> 3) << 17) | ((uint32_t)(TILE >> 4) << 24);
+        auto load = [&](int i) {
+            uint8_t *sa = smem + (i & 1) * BG_STAGE, *sb = sa + A_KB;
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&full[i & 1])),
+                         "r"(BG_STAGE)
+                         : "memory");
+            asm volatile(
+                "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+                    smem_u32(sa)),
+                "l"(&mapA), "r"(smem_u32(&full[i & 1])), "r"((kb0 + i) * 64), "r"(m0)
+                : "memory");
+            asm volatile(
+                "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+                    smem_u32(sb)),
+                "l"(&mapB), "r"(smem_u32(&full[i & 1])), "r"((kb0 + i) * 64), "r"(0)
+                : "memory");
+        };
+        int issued = 0, consumed = 0;
+        for (; issued < n && issued < 2; ++issued) load(issued);
+        bool ok = true;
+        for (int i = 0; i < n && ok; ++i) {
+            ok = wait_bar(&full[i & 1], (uint32_t)((i >> 1) & 1), err, 21);
+            if (!ok) break;
+            ++consumed;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t sa = smem_u32(smem + (i & 1) * BG_STAGE), sb = sa + A_KB;
+            for (int kk = 0; kk < 4; ++kk) {
+                const uint64_t ad = sw128_desc(sa + kk * 32), bd = sw128_desc(sb + kk * 32);
+                const uint32_t acc = (i | kk) ? 1u : 0u;
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_u32(&freed[i & 1]))
+                         : "memory");
+            if (issued < n) {                  // stage i & 1 is free once these MMAs complete
+                ok = wait_bar(&freed[i & 1], (uint32_t)((i >> 1) & 1), err, 22);
+                if (ok) load(issued++);
+            }
+        }
+        if (!ok) {
+            s_abort = 1;
+            for (int j = consumed; j < issued; ++j) wait_bar(&full[j & 1], (uint32_t)((j >> 1) & 1), nullptr, 0);
+        }
+        // arrives once every MMA issued above has completed
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(&done))
+                     : "memory");
+    }
+    const bool fin = wait_bar(&done, 0u, err, 23);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (fin && !s_abort) {
+        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+        float *crow = C + (long long)(m0 + tid) * ldc;
+        const bool atomic = gridDim.y > 1;
+        for (int c0 = 0; c0 < H; c0 += 16) {
+            uint32_t r[16];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                : "r"(tmem + lane_base + (uint32_t)c0));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            float v[16];
+#pragma unroll
+            for (int e = 0; e < 16; ++e) v[e] = __uint_as_float(r[e]) + (bias ? bias[c0 + e] : 0.f);
+            if (atomic) {
+#pragma unroll
+                for (int e = 0; e < 16; ++e) atomicAdd(crow + c0 + e, v[e]);
+            } else {
+#pragma unroll
+                for (int e = 0; e < 16; e += 4) *reinterpret_cast<float4 *>(crow + c0 + e) = make_float4(v[e], v[e + 1], v[e + 2], v[e + 3]);
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(H));
+}
+
+// bf16 copies of an FP32 [rows x cols] matrix (cols a multiple of 32): row-major
+// (dst) and transposed (dstT, [cols x rows]), through 32 x 32 shared tiles so
+// that both are written coalesced.
+__global__ void k_bf16_copies(const float *src, int rows, int cols, __nv_bfloat16 *dst, __nv_bfloat16 *dstT)
+{
+    __shared__ float t[32][33];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;          // 32 x 8 threads
+    const int ct = cols / 32, tiles = ((rows + 31) / 32) * ct;
+    for (int u = blockIdx.x; u < tiles; u += gridDim.x) {
+        const int r0 = (u / ct) * 32, c0 = (u % ct) * 32;
+        for (int y = ty; y < 32; y += 8) {
+            const int r = r0 + y;
+            const float v = r < rows ? src[(long long)r * cols + c0 + tx] : 0.f;
+            t[y][tx] = v;
+            if (dst && r < rows) dst[(long long)r * cols + c0 + tx] = __float2bfloat16_rn(v);
+        }
+        __syncthreads();
+        if (dstT)
+            for (int y = ty; y < 32; y += 8)
+                if (r0 + tx < rows) dstT[(long long)(c0 + y) * rows + r0 + tx] = __float2bfloat16_rn(t[tx][y]);
+        __syncthreads();
+    }
+}
+
 __global__ void k_to_bf16(const float *src, __nv_bfloat16 *dst, int n)
 {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) dst[k] = __float2bfloat16_rn(src[k]);
@@ -459,67 +614,6 @@ static void gemm(cudaStream_t s, int M, int N, int K, const float *A, long long 
     sgemm<<<g, 256, 0, s>>>(M, N, K, 1.f, A, ar, ac, B, br, bc, 0.f, C, ldc, bias, round_b);
 }
 
-// device workspace for batches of up to M rows
-struct Work {
-    int M = 0;
-    float *x = nullptr, *t = nullptr, *z1 = nullptr, *h1 = nullptr, *z2 = nullptr, *h2 = nullptr, *z3 = nullptr,
-          *h3 = nullptr, *y = nullptr, *dy = nullptr, *dz = nullptr, *dh = nullptr, *G = nullptr, *loss = nullptr,
-          *ones = nullptr;
-    int alloc(int m)
-    {
-        M = m;
-        const size_t act = (size_t)m * H * 4;
-        float **big[] = {&z1, &h1, &z2, &h2, &z3, &h3, &dz, &dh};
-        for (float **b : big)
-            if (cudaMalloc(b, act) != cudaSuccess) return HX_ERR_NOMEM;
-        if (cudaMalloc(&x, (size_t)m * F * 4) != cudaSuccess || cudaMalloc(&t, (size_t)m * 4) != cudaSuccess ||
-            cudaMalloc(&y, (size_t)m * 4) != cudaSuccess || cudaMalloc(&dy, (size_t)m * 4) != cudaSuccess ||
-            cudaMalloc(&G, (size_t)NPARAM * 4) != cudaSuccess || cudaMalloc(&loss, 4) != cudaSuccess ||
-            cudaMalloc(&ones, (size_t)m * 4) != cudaSuccess)
-            return HX_ERR_NOMEM;
-        std::vector<float> one(m, 1.f);
-        return cudaMemcpy(ones, one.data(), (size_t)m * 4, cudaMemcpyHostToDevice) == cudaSuccess ? HX_OK : HX_ERR_CUDA;
-    }
-    ~Work()
-    {
-        float *all[] = {x, t, z1, h1, z2, h2, z3, h3, y, dy, dz, dh, G, loss, ones};
-        for (float *b : all) cudaFree(b);
-    }
-};
-
-// forward + backward of one batch already normalised in w.x / w.t (M rows);
-// gradients into w.G (overwritten), mean squared error added to w.loss
-static void fwd_bwd(cudaStream_t s, Work &w, const float *P, int M)
-{
-    const long long MH = (long long)M * H;
-    gemm(s, M, H, F, w.x, F, 1, P + O_W1, 1, F, w.z1, H, P + O_B1);
-    k_silu<<<nblocks(MH), 256, 0, s>>>(w.z1, w.h1, MH, 1);
-    gemm(s, M, H, H, w.h1, H, 1, P + O_W2, 1, H, w.z2, H, P + O_B2, 1);
-    k_silu<<<nblocks(MH), 256, 0, s>>>(w.z2, w.h2, MH, 1);
-    gemm(s, M, H, H, w.h2, H, 1, P + O_W3, 1, H, w.z3, H, P + O_B3, 1);
-    k_silu<<<nblocks(MH), 256, 0, s>>>(w.z3, w.h3, MH, 0);
-    gemm(s, M, 1, H, w.h3, H, 1, P + O_W4, 1, 0, w.y, 1);
-    k_loss<<<nblocks(M), 256, 0, s>>>(w.y, w.t, P, w.dy, w.loss, M);
-    // output layer
-    gemm(s, 1, H, M, w.dy, 0, 1, w.h3, H, 1, w.G + O_W4, H);              // dw4 = h3^T dy
-    gemm(s, 1, 1, M, w.dy, 0, 1, w.ones, 1, 0, w.G + O_B4, 1);             // db4 = sum dy
-    k_dsilu<<<nblocks(MH), 256, 0, s>>>(nullptr, w.dy, P + O_W4, w.z3, w.dz, M);
-    // layer 3
-    gemm(s, H, H, M, w.dz, 1, H, w.h2, H, 1, w.G + O_W3, H);               // dW3 = dz3^T h2
-    gemm(s, 1, H, M, w.ones, 0, 1, w.dz, H, 1, w.G + O_B3, H);             // db3
-    gemm(s, M, H, H, w.dz, H, 1, P + O_W3, H, 1, w.dh, H, nullptr, 1);     // dh2 = dz3 bf16(W3)
-    k_dsilu<<<nblocks(MH), 256, 0, s>>>(w.dh, nullptr, nullptr, w.z2, w.dz, M);
-    // layer 2
-    gemm(s, H, H, M, w.dz, 1, H, w.h1, H, 1, w.G + O_W2, H);
-    gemm(s, 1, H, M, w.ones, 0, 1, w.dz, H, 1, w.G + O_B2, H);
-    gemm(s, M, H, H, w.dz, H, 1, P + O_W2, H, 1, w.dh, H, nullptr, 1);
-    k_dsilu<<<nblocks(MH), 256, 0, s>>>(w.dh, nullptr, nullptr, w.z1, w.dz, M);
-    // layer 1
-    gemm(s, H, F, M, w.dz, 1, H, w.x, F, 1, w.G + O_W1, F);
-    gemm(s, 1, H, M, w.ones, 0, 1, w.dz, H, 1, w.G + O_B1, H);
-    hx_count_launches(22);
-}
-
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
 {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -532,6 +626,155 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
     }
     return fn;
 }
+
+// 2D map over a bf16 [rows x cols] matrix: 64 x box_rows boxes, 128-byte swizzle
+static int map_bf16(CUtensorMap *map, const void *base, long long rows, int cols, int box_rows)
+{
+    auto fn = encode_fn();
+    if (!fn) { hx_set_error("cuTensorMapEncodeTiled is unavailable"); return HX_ERR_CUDA; }
+    cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
+    cuuint32_t box[2] = {64, (cuuint32_t)box_rows};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) { hx_set_error("cuTensorMapEncodeTiled failed (%d)", (int)r); return HX_ERR_CUDA; }
+    return HX_OK;
+}
+
+// device workspace for batches of up to M rows (padded to Mp, a multiple of
+// the 128-row tile: the padded rows have zero inputs and zero loss gradient)
+struct Work {
+    int M = 0, Mp = 0;
+    float *x = nullptr, *t = nullptr, *z1 = nullptr, *h1 = nullptr, *z2 = nullptr, *h2 = nullptr, *z3 = nullptr,
+          *h3 = nullptr, *y = nullptr, *dy = nullptr, *dz = nullptr, *dh = nullptr, *G = nullptr, *loss = nullptr,
+          *ones = nullptr;
+    // bf16 operands of the tensor-core GEMMs: activations and gradients (and
+    // their transposes, [H x Mp]) and the two hidden weight matrices
+    __nv_bfloat16 *h1b = nullptr, *h2b = nullptr, *h1T = nullptr, *h2T = nullptr, *dzb = nullptr, *dzT = nullptr,
+                  *W2b = nullptr, *W3b = nullptr, *W2T = nullptr, *W3T = nullptr;
+    CUtensorMap mH1b, mH2b, mW2b, mW3b, mDzT, mH1T, mH2T, mDzb, mW2T, mW3T;
+    int *err = nullptr;
+    int alloc(int m)
+    {
+        M = m;
+        Mp = (m + TILE - 1) / TILE * TILE;
+        const size_t act = (size_t)Mp * H * 4, actb = (size_t)Mp * H * 2, wb = (size_t)H * H * 2;
+        float **big[] = {&z1, &h1, &z2, &h2, &z3, &h3, &dz, &dh};
+        for (float **b : big)
+            if (cudaMalloc(b, act) != cudaSuccess) return HX_ERR_NOMEM;
+        __nv_bfloat16 **bb[] = {&h1b, &h2b, &h1T, &h2T, &dzb, &dzT};
+        for (__nv_bfloat16 **b : bb)
+            if (cudaMalloc(b, actb) != cudaSuccess) return HX_ERR_NOMEM;
+        __nv_bfloat16 **wbs[] = {&W2b, &W3b, &W2T, &W3T};
+        for (__nv_bfloat16 **b : wbs)
+            if (cudaMalloc(b, wb) != cudaSuccess) return HX_ERR_NOMEM;
+        if (cudaMalloc(&x, (size_t)Mp * F * 4) != cudaSuccess || cudaMalloc(&t, (size_t)Mp * 4) != cudaSuccess ||
+            cudaMalloc(&y, (size_t)Mp * 4) != cudaSuccess || cudaMalloc(&dy, (size_t)Mp * 4) != cudaSuccess ||
+            cudaMalloc(&G, (size_t)NPARAM * 4) != cudaSuccess || cudaMalloc(&loss, 4) != cudaSuccess ||
+            cudaMalloc(&ones, (size_t)Mp * 4) != cudaSuccess || cudaMalloc(&err, 4) != cudaSuccess)
+            return HX_ERR_NOMEM;
+        // padded rows: zero inputs and targets, and a zero loss gradient (k_loss writes the first M only)
+        if (cudaMemset(x, 0, (size_t)Mp * F * 4) != cudaSuccess || cudaMemset(t, 0, (size_t)Mp * 4) != cudaSuccess ||
+            cudaMemset(dy, 0, (size_t)Mp * 4) != cudaSuccess || cudaMemset(err, 0, 4) != cudaSuccess)
+            return HX_ERR_CUDA;
+        int rc = HX_OK;
+        if (rc == HX_OK) rc = map_bf16(&mH1b, h1b, Mp, H, TILE);
+        if (rc == HX_OK) rc = map_bf16(&mH2b, h2b, Mp, H, TILE);
+        if (rc == HX_OK) rc = map_bf16(&mDzb, dzb, Mp, H, TILE);
+        if (rc == HX_OK) rc = map_bf16(&mDzT, dzT, H, Mp, TILE);
+        if (rc == HX_OK) rc = map_bf16(&mH1T, h1T, H, Mp, H);
+        if (rc == HX_OK) rc = map_bf16(&mH2T, h2T, H, Mp, H);
+        if (rc == HX_OK) rc = map_bf16(&mW2b, W2b, H, H, H);
+        if (rc == HX_OK) rc = map_bf16(&mW3b, W3b, H, H, H);
+        if (rc == HX_OK) rc = map_bf16(&mW2T, W2T, H, H, H);
+        if (rc == HX_OK) rc = map_bf16(&mW3T, W3T, H, H, H);
+        if (rc != HX_OK) return rc;
+        if (cudaFuncSetAttribute(bgemm, cudaFuncAttributeMaxDynamicSharedMemorySize, BG_SMEM) != cudaSuccess) {
+            hx_set_error("cannot reserve shared memory for the training GEMM");
+            return HX_ERR_CUDA;
+        }
+        std::vector<float> one(Mp, 1.f);
+        return cudaMemcpy(ones, one.data(), (size_t)Mp * 4, cudaMemcpyHostToDevice) == cudaSuccess ? HX_OK : HX_ERR_CUDA;
+    }
+    int error_word() const
+    {
+        int v = 0;
+        if (err) cudaMemcpy(&v, err, 4, cudaMemcpyDeviceToHost);
+        return v;
+    }
+    ~Work()
+    {
+        float *all[] = {x, t, z1, h1, z2, h2, z3, h3, y, dy, dz, dh, G, loss, ones};
+        for (float *b : all) cudaFree(b);
+        __nv_bfloat16 *allb[] = {h1b, h2b, h1T, h2T, dzb, dzT, W2b, W3b, W2T, W3T};
+        for (__nv_bfloat16 *b : allb) cudaFree(b);
+        cudaFree(err);
+    }
+};
+
+// bf16 copies (row-major and transposed) of an FP32 [rows x H] matrix
+static void copies(cudaStream_t s, const float *src, int rows, __nv_bfloat16 *dst, __nv_bfloat16 *dstT)
+{
+    k_bf16_copies<<<nblocks((long long)((rows + 31) / 32) * (H / 32), 1), 256, 0, s>>>(src, rows, H, dst, dstT);
+}
+// tensor-core GEMM C[rows x H] = A B^T (+ bias) over nkb 64-deep K-blocks; splits > 1
+// add into C (cleared first) from that many K ranges
+static void bf16_gemm(cudaStream_t s, const CUtensorMap &a, const CUtensorMap &b, int rows, int nkb, int splits,
+                    float *C, const float *bias, int *err)
+{
+    const int kb_per = (nkb + splits - 1) / splits;
+    const dim3 grid(rows / TILE, (nkb + kb_per - 1) / kb_per);
+    if (grid.y > 1) cudaMemsetAsync(C, 0, (size_t)rows * H * 4, s);
+    bgemm<<<grid, BG_THREADS, BG_SMEM, s>>>(a, b, C, H, bias, nkb, kb_per, err);
+}
+
+// forward + backward of one batch already normalised in w.x / w.t (M rows);
+// gradients into w.G (overwritten), mean squared error added to w.loss. The
+// six 256-wide products (layers 2 and 3 forward, their weight gradients and
+// the gradients of their inputs) run on the tensor cores in BF16 with FP32
+// accumulation (bgemm); the 8-wide first layer, the 1-wide output and the
+// bias sums stay on the CUDA cores. The loss gradient dz entering a bf16
+// product is rounded to bf16 (oracle/mlp.py applies the same roundings).
+static void fwd_bwd(cudaStream_t s, Work &w, const float *P, int M)
+{
+    const int Mp = w.Mp, nk = H / 64, nkm = Mp / 64;
+    const long long MH = (long long)Mp * H;
+    k_bf16_copies<<<64, 256, 0, s>>>(P + O_W2, H, H, w.W2b, w.W2T);
+    k_bf16_copies<<<64, 256, 0, s>>>(P + O_W3, H, H, w.W3b, w.W3T);
+    gemm(s, Mp, H, F, w.x, F, 1, P + O_W1, 1, F, w.z1, H, P + O_B1);
+    k_silu<<<nblocks(MH), 256, 0, s>>>(w.z1, w.h1, MH, 1);
+    copies(s, w.h1, Mp, w.h1b, w.h1T);
+    bf16_gemm(s, w.mH1b, w.mW2b, Mp, nk, 1, w.z2, P + O_B2, w.err);
+    k_silu<<<nblocks(MH), 256, 0, s>>>(w.z2, w.h2, MH, 1);
+    copies(s, w.h2, Mp, w.h2b, w.h2T);
+    bf16_gemm(s, w.mH2b, w.mW3b, Mp, nk, 1, w.z3, P + O_B3, w.err);
+    k_silu<<<nblocks(MH), 256, 0, s>>>(w.z3, w.h3, MH, 0);
+    gemm(s, Mp, 1, H, w.h3, H, 1, P + O_W4, 1, 0, w.y, 1);
+    k_loss<<<nblocks(M), 256, 0, s>>>(w.y, w.t, P, w.dy, w.loss, M);
+    // output layer
+    gemm(s, 1, H, Mp, w.dy, 0, 1, w.h3, H, 1, w.G + O_W4, H);             // dw4 = h3^T dy
+    gemm(s, 1, 1, Mp, w.dy, 0, 1, w.ones, 1, 0, w.G + O_B4, 1);            // db4 = sum dy
+    k_dsilu<<<nblocks(MH), 256, 0, s>>>(nullptr, w.dy, P + O_W4, w.z3, w.dz, Mp);
+    copies(s, w.dz, Mp, w.dzb, w.dzT);
+    // layer 3
+    bf16_gemm(s, w.mDzT, w.mH2T, H, nkm, std::max(1, nkm / 4), w.G + O_W3, nullptr, w.err);   // dW3 = bf16(dz3)^T h2
+    gemm(s, 1, H, Mp, w.ones, 0, 1, w.dz, H, 1, w.G + O_B3, H);            // db3
+    bf16_gemm(s, w.mDzb, w.mW3T, Mp, nk, 1, w.dh, nullptr, w.err);          // dh2 = bf16(dz3) bf16(W3)
+    k_dsilu<<<nblocks(MH), 256, 0, s>>>(w.dh, nullptr, nullptr, w.z2, w.dz, Mp);
+    copies(s, w.dz, Mp, w.dzb, w.dzT);
+    // layer 2
+    bf16_gemm(s, w.mDzT, w.mH1T, H, nkm, std::max(1, nkm / 4), w.G + O_W2, nullptr, w.err);
+    gemm(s, 1, H, Mp, w.ones, 0, 1, w.dz, H, 1, w.G + O_B2, H);
+    bf16_gemm(s, w.mDzb, w.mW2T, Mp, nk, 1, w.dh, nullptr, w.err);
+    k_dsilu<<<nblocks(MH), 256, 0, s>>>(w.dh, nullptr, nullptr, w.z1, w.dz, Mp);
+    // layer 1
+    gemm(s, H, F, Mp, w.dz, 1, H, w.x, F, 1, w.G + O_W1, F);
+    gemm(s, 1, H, Mp, w.ones, 0, 1, w.dz, H, 1, w.G + O_B1, H);
+    hx_count_launches(30);
+}
+
 
 int Model::load(const float *host_blob)
 {
@@ -659,6 +902,7 @@ int hx_mlp_grad(const float *params, const float *X, const float *T, int32_t n, 
         fwd_bwd(0, w, dP, n);
         cudaError_t e = cudaDeviceSynchronize();
         if (e != cudaSuccess) { hx_set_error("hx_mlp_grad: %s", cudaGetErrorString(e)); rc = HX_ERR_CUDA; }
+        else if (int we = w.error_word()) { hx_set_error("hx_mlp_grad: a tensor-core wait timed out (%d)", we); rc = HX_ERR_KERNEL; }
         else {
             if (loss) cudaMemcpy(loss, w.loss, 4, cudaMemcpyDeviceToHost);
             if (grad) {
@@ -720,6 +964,7 @@ int hx_mlp_train(float *params, const float *X, const float *T, int64_t n, int32
             float l = 0.f;
             cudaError_t e = cudaMemcpy(&l, w.loss, 4, cudaMemcpyDeviceToHost);
             if (e != cudaSuccess) { hx_set_error("hx_mlp_train: %s", cudaGetErrorString(e)); rc = HX_ERR_CUDA; }
+            else if (int we = w.error_word()) { hx_set_error("hx_mlp_train: a tensor-core wait timed out (%d)", we); rc = HX_ERR_KERNEL; }
             if (epoch_loss) epoch_loss[ep] = l / (float)(nb > 0 ? nb : 1);
         }
         if (rc == HX_OK && cudaMemcpy(params, dP, (size_t)ntrain * 4, cudaMemcpyDeviceToHost) != cudaSuccess) rc = HX_ERR_CUDA;

@@ -395,11 +395,20 @@ __device__ __forceinline__ bool load_tile(const PrepDesc *__restrict__ pd, int n
     }
     __syncthreads();
     const int rlim = d.R - r0, klim = d.K - k0;
+    // the tile's eight loads per thread all in flight before their shared-memory stores
+    constexpr int NL = PT_R * PT_K / PT_THREADS;
+    double v[NL];
 #pragma unroll
-    for (int e = threadIdx.x; e < PT_R * PT_K; e += PT_THREADS) {
-        int rr, kk;
-        if (d.rfast) { rr = e % PT_R; kk = e / PT_R; } else { kk = e % PT_K; rr = e / PT_K; }
-        t.x[rr][kk] = (rr < rlim && kk < klim) ? __ldg(d.src + t.roff[rr] + t.koff[kk]) : 0.0;
+    for (int j = 0; j < NL; ++j) {
+        const int e = threadIdx.x + j * PT_THREADS;
+        const int rr = d.rfast ? e % PT_R : e / PT_K, kk = d.rfast ? e / PT_R : e % PT_K;
+        v[j] = (rr < rlim && kk < klim) ? __ldg(d.src + t.roff[rr] + t.koff[kk]) : 0.0;
+    }
+#pragma unroll
+    for (int j = 0; j < NL; ++j) {
+        const int e = threadIdx.x + j * PT_THREADS;
+        const int rr = d.rfast ? e % PT_R : e / PT_K, kk = d.rfast ? e / PT_R : e % PT_K;
+        t.x[rr][kk] = v[j];
     }
     __syncthreads();
     return true;

@@ -4,7 +4,8 @@ Forward and backward of the 4-layer MLP (8 -> 256 -> 256 -> 256 -> 1, SiLU)
 used by the GPU engine's learned guess, in float64 numpy with the same
 roundings the GPU kernels apply: weights of layers 2 and 3 and the
 activations entering them are rounded to bfloat16 (round to nearest even),
-everything is accumulated in higher precision. The GPU gradients are
+and so are the loss gradients entering the backward products of those
+layers; everything is accumulated in higher precision. The GPU gradients are
 checked against ``grads``.
 
 Parameter layout (one flat float32 vector, the blob the engine consumes):
@@ -80,13 +81,16 @@ def loss_and_grads(p, X, T, rounding=True):
     g = {}
     g["w4"] = h3.T @ dy
     g["b4"] = np.array([dy.sum()])
+    # the gradients entering the bf16 tensor-core products of layers 3 and 2 are
+    # rounded to bf16 there (weight gradients and input gradients); the bias sums
+    # and the first layer use them unrounded
     dz3 = np.outer(dy, p["w4"]) * dsilu(z3)
-    g["W3"] = dz3.T @ h2
+    g["W3"] = rnd(dz3).T @ h2
     g["b3"] = dz3.sum(0)
-    dz2 = (dz3 @ rnd(p["W3"])) * dsilu(z2)
-    g["W2"] = dz2.T @ h1
+    dz2 = (rnd(dz3) @ rnd(p["W3"])) * dsilu(z2)
+    g["W2"] = rnd(dz2).T @ h1
     g["b2"] = dz2.sum(0)
-    dz1 = (dz2 @ rnd(p["W2"])) * dsilu(z1)
+    dz1 = (rnd(dz2) @ rnd(p["W2"])) * dsilu(z1)
     g["W1"] = dz1.T @ x
     g["b1"] = dz1.sum(0)
     return loss, g
