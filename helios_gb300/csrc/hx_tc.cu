@@ -137,8 +137,8 @@ struct Cfg {
     // int64 drain: a chunk adds below 2^(24 + 8(NX-1) + 1); 32 chunks stay below 2^63
     static_assert(!INT_DRAIN || 24 + 8 * (NX_ - 1) + 1 + 5 < 63, "int64 drain headroom");
 };
-using Low = Cfg<3, 3, 1, 64, 2, 8, 8, 64>;
-using Mid = Cfg<4, 3, 2, 64, 2, 6, 8, 64>;
+using Low = Cfg<3, 3, 1, 64, 2, 8, 16, 64>;
+using Mid = Cfg<4, 3, 2, 64, 2, 6, 16, 64>;
 using High = Cfg<5, 4, 3, 48, 3, 8, 8, 32>;
 using Exact = Cfg<7, 6, 5, 32, 3, 6, 8, 32>;
 constexpr int TMEM_COLS = 512;
@@ -643,17 +643,19 @@ __device__ __forceinline__ TileWork tile_work(const TcDesc *__restrict__ descs, 
     }
     w.di = lo;
     const TcDesc &d = descs[lo];
-    long long local = tile - d.tile_start;
-    const int ks = (int)(local % d.ksplit);
+    // a problem's tiles number below 2^31: 32-bit divisions (64-bit ones are
+    // emulated, and every epilogue thread does this for every tile)
+    int local = (int)(tile - d.tile_start);
+    const int ks = local % d.ksplit;
     local /= d.ksplit;
-    const long long per_batch = (long long)d.tiles_m * d.tiles_n;
-    w.bt = (int)(local / per_batch);
+    const int per_batch = d.tiles_m * d.tiles_n;
+    w.bt = local / per_batch;
     local -= w.bt * per_batch;
     const int GM = 16;
-    const int group = (int)(local / (GM * d.tiles_n));
+    const int group = local / (GM * d.tiles_n);
     const int first_m = group * GM;
     const int gsz = min(d.tiles_m - first_m, GM);
-    const int in_g = (int)(local % (GM * d.tiles_n));
+    const int in_g = local % (GM * d.tiles_n);
     w.tm = first_m + in_g % gsz;
     w.tn = in_g / gsz;
     w.kb0 = ks * d.kb_per;
@@ -978,7 +980,7 @@ __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restri
 // reuse each A tile over more columns. The autotuner (choose_variant) picks one
 // per plan group, precision mode and size class.
 using Low32 = Cfg<3, 3, 1, 32, 3, 8, 4, 64>;
-using LowS3 = Cfg<3, 3, 1, 64, 3, 8, 8, 64>;       // three stages
+using LowS3 = Cfg<3, 3, 1, 64, 3, 8, 16, 64>;      // three stages
 using Mid48 = Cfg<4, 3, 2, 48, 2, 6, 8, 64>;
 using Mid32 = Cfg<4, 3, 2, 32, 2, 6, 4, 64>;
 using High32 = Cfg<5, 4, 3, 32, 3, 8, 4, 32>;
