@@ -139,8 +139,8 @@ struct Cfg {
 };
 using Low = Cfg<3, 3, 1, 64, 2, 8, 16, 64>;
 using Mid = Cfg<4, 3, 2, 64, 2, 6, 16, 64>;
-using High = Cfg<5, 4, 3, 48, 3, 8, 8, 32>;
-using Exact = Cfg<7, 6, 5, 32, 3, 6, 8, 32>;
+using High = Cfg<5, 4, 3, 48, 3, 8, 12, 32>;
+using Exact = Cfg<7, 6, 5, 32, 3, 6, 16, 32>;
 constexpr int TMEM_COLS = 512;
 constexpr int BM = 128, KPAD = 64;   // K is padded to KPAD (the slicing tile depth)
 constexpr unsigned long long WAIT_NS = 4000000000ull; // a wait longer than 4 s is declared failed
@@ -979,12 +979,12 @@ __global__ void __launch_bounds__(C::NTHREADS, 1) tc_gemm(const TcDesc *__restri
 // Narrow tiles waste less on the thin operands of small molecules; wide ones
 // reuse each A tile over more columns. The autotuner (choose_variant) picks one
 // per plan group, precision mode and size class.
-using Low32 = Cfg<3, 3, 1, 32, 3, 8, 4, 64>;
+using Low32 = Cfg<3, 3, 1, 32, 3, 8, 8, 64>;
 using LowS3 = Cfg<3, 3, 1, 64, 3, 8, 16, 64>;      // three stages
-using Mid48 = Cfg<4, 3, 2, 48, 2, 6, 8, 64>;
-using Mid32 = Cfg<4, 3, 2, 32, 2, 6, 4, 64>;
-using High32 = Cfg<5, 4, 3, 32, 3, 8, 4, 32>;
-using Exact16 = Cfg<7, 6, 5, 16, 3, 6, 4, 32>;
+using Mid48 = Cfg<4, 3, 2, 48, 2, 6, 12, 64>;
+using Mid32 = Cfg<4, 3, 2, 32, 2, 6, 8, 64>;
+using High32 = Cfg<5, 4, 3, 32, 3, 8, 8, 32>;
+using Exact16 = Cfg<7, 6, 5, 16, 3, 6, 8, 32>;
 struct Variant {
     int S, BN, BK, products, smem;
     cudaError_t (*attr)();
