@@ -498,11 +498,16 @@ __global__ void __launch_bounds__(PT_THREADS) split_gather(const PrepDesc *__res
                 if (e == INT_MIN) e = 0;
             }
             if (in_rows) {
-                double v[8];
-#pragma unroll
-                for (int q = 0; q < 8; ++q) v[q] = t.x[rr][c8 + q];
                 uint4 out[S];
-                slice8<S>(v, e, out);
+                if (r0 + rr < d.R && k0 + c8 < d.K) {
+                    double v[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) v[q] = t.x[rr][c8 + q];
+                    slice8<S>(v, e, out);
+                } else {                                         // zero padding: no digits to compute
+#pragma unroll
+                    for (int p = 0; p < S; ++p) out[p] = make_uint4(0u, 0u, 0u, 0u);
+                }
                 const long long plane = (long long)d.batch * d.Rp * d.Kp;
                 const long long off = ((long long)b * d.Rp + r0 + rr) * d.Kp + k0 + c8;
 #pragma unroll
@@ -605,16 +610,22 @@ __global__ void __launch_bounds__(PT_THREADS, 4) slice_band(const PrepDesc *__re
         const long long plane = (long long)d.batch * d.Rp * Kp;
         __nv_bfloat16 *__restrict__ dst = d.dst + ((long long)b * d.Rp + r0) * Kp;
         int r = threadIdx.x / cpr, k8 = (threadIdx.x % cpr) * 8;
+        const int rlive = min(rows_band, rlim);                 // rows past R and k past K are zero padding
         while (r < rows_band) {
-            double v[8];
-#pragma unroll
-            for (int q = 0; q < 8; q += 2) {
-                const double2 w2 = *reinterpret_cast<const double2 *>(x + r * ld + k8 + q);
-                v[q] = w2.x;
-                v[q + 1] = w2.y;
-            }
             uint4 out[S];
-            slice8<S>(v, rexp_s[r], out);
+            if (r < rlive && k8 < K) {
+                double v[8];
+#pragma unroll
+                for (int q = 0; q < 8; q += 2) {
+                    const double2 w2 = *reinterpret_cast<const double2 *>(x + r * ld + k8 + q);
+                    v[q] = w2.x;
+                    v[q + 1] = w2.y;
+                }
+                slice8<S>(v, rexp_s[r], out);
+            } else {
+#pragma unroll
+                for (int p = 0; p < S; ++p) out[p] = make_uint4(0u, 0u, 0u, 0u);
+            }
 #pragma unroll
             for (int p = 0; p < S; ++p) *reinterpret_cast<uint4 *>(dst + p * plane + (long long)r * Kp + k8) = out[p];
             r += dr;

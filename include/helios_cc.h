@@ -172,7 +172,11 @@ int hx_mlp_grad(const float *params, const float *X, const float *T, int32_t n, 
 
 /* Train the network on the GPU: Adam (cosine-decayed learning rate lr) over
  * `epochs` passes of shuffled mini-batches of `batch` rows; params is updated
- * in place and epoch_loss[e] (if not NULL) receives each epoch's mean loss. */
+ * in place and epoch_loss[e] (if not NULL) receives each epoch's mean loss.
+ * The 256-wide products of each step run on the BF16 tensor cores with FP32
+ * accumulation (weights, activations and the loss gradients entering them
+ * rounded to bf16); the weight gradients are summed with split-K atomics, so
+ * two runs differ in the last bits. */
 int hx_mlp_train(float *params, const float *X, const float *T, int64_t n, int32_t epochs, int32_t batch, float lr,
                  uint64_t seed, float *epoch_loss);
 
