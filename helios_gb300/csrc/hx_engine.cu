@@ -378,6 +378,15 @@ static double diis_gate(const hx_ccsd *h, int mi)
     return h->gate_eps;
 }
 
+// The phase of iterations driven from the host (hx_ccsd_iterate) and the one a
+// handle returns to after a solve: the 7-slice phase for HX_PRECISION_EXACT
+// (every iteration of such a handle is one), FP64 otherwise (the mixed ladder
+// belongs to hx_ccsd_solve).
+static int idle_phase(const hx_ccsd *h)
+{
+    return h->p.precision == HX_PRECISION_EXACT ? PH_EXACT : PH_FP64;
+}
+
 static int upload_masks(hx_ccsd *h)
 {
     for (int mi = 0; mi < h->nmol; ++mi) h->gate[mi] = diis_gate(h, mi);
@@ -621,7 +630,7 @@ static int allocate(hx_ccsd *h)
     h->gate.assign(h->nmol, 0.0);
     h->active.assign(h->nmol, 1);
     h->scf_failed.assign(h->nmol, 0);
-    h->phase.assign(h->nmol, PH_FP64);
+    h->phase.assign(h->nmol, idle_phase(h));
     h->dcount.assign(h->nmol, 0);
     h->slot_phase.assign(h->nmol, {});
     h->ph_end.assign(h->nmol, {});
@@ -1201,7 +1210,7 @@ static int solve_all(hx_ccsd *h, int maxiter, double eps)
     HX_TRY(fetch_results(h));
     if (h->tce) tc::collect(h->tce, h->prof);
     // keep every molecule addressable for getters / energy after the solve
-    for (int mi = 0; mi < n; ++mi) { h->active[mi] = !h->scf_failed[mi]; h->phase[mi] = PH_FP64; }
+    for (int mi = 0; mi < n; ++mi) { h->active[mi] = !h->scf_failed[mi]; h->phase[mi] = idle_phase(h); }
     HX_TRY(upload_masks(h));
     return HX_OK;
 }

@@ -215,21 +215,9 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, u
         "l"(map), "r"(smem_u32(bar)), "r"(x), "r"(y)
         : "memory");
 }
-// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row
-// groups 1024 bytes apart (SBO), tcgen05 descriptor version 1.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr)
-{
-    uint64_t d = 0;
-    d |= (uint64_t)((addr & 0x3FFFF) >> 4);
-    d |= (uint64_t)1 << 16;                    // leading byte offset (unused for swizzled K-major)
-    d |= (uint64_t)(1024 >> 4) << 32;          // stride byte offset
-    d |= (uint64_t)1 << 46;                    // descriptor version
-    d |= (uint64_t)2 << 61;                    // SWIZZLE_128B
-    return d;
-}
-// The same for a configuration's k-block depth: 128-byte rows (BK = 64,
-// SWIZZLE_128B) or 64-byte rows (BK = 32, SWIZZLE_64B); K-major, 8-row groups
-// SBO bytes apart, descriptor version 1.
+// Shared-memory matrix descriptor of a configuration's k-block depth: K-major,
+// 128-byte rows (BK = 64, SWIZZLE_128B) or 64-byte rows (BK = 32,
+// SWIZZLE_64B), 8-row groups SBO bytes apart, descriptor version 1.
 template <class C>
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr)
 {
@@ -254,32 +242,9 @@ __device__ __forceinline__ void mma_commit(uint64_t *bar)
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                  : "memory");
 }
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v)
-{
-    uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v)
-{
-    uint32_t r[8];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-                 : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-// The same without the wait: several loads in flight, then tmem_wait_ld
-// on their registers (the wait names them, so no use moves above it).
+// TMEM loads of eight columns without a wait: several loads in flight, then
+// tmem_wait_ld and tmem_tie8 on their registers (the tie names them after the
+// wait, so no use moves above it).
 __device__ __forceinline__ void tmem_ld8_issue(uint32_t taddr, uint32_t *r)
 {
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"

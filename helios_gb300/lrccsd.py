@@ -212,33 +212,46 @@ class DeviceSigma:
         kw = replace(keywords, precision=precision, guess="reference", t1_step=1.0, t2_step=1.0, projection_type="2-1")
         self.cc = (engine or api.CoupledCluster)([mol] * (4 * nvec), kw)
         self.cc.initCC()
-        self.t1, self.t2, self.h, self.nvec = t1, t2, h, nvec
+        # arrays in the engine's column-major layout, so that no call transposes
+        self.t1 = np.asfortranarray(t1, dtype=np.float64)
+        self.t2 = np.asfortranarray(t2, dtype=np.float64)
+        self.h, self.nvec = h, nvec
         self.calls = 0                                      # engine iterations (one per call)
         self.eps = 10.0 ** (-keywords.accuracy)
         o = t1.shape[0]
-        self.signs, self.D1, self.D2 = [], [], []
+        # each copy's orbital signs as +-1 tensors (copies with the same signs share them)
+        self.signs, self.D1, self.D2, self._sign_tensors = [], [], [], {}
         for k in range(4 * nvec):
             s = self.cc.scf(k)
             sg = _align(C0, s["C"])
             if np.abs(s["C"] * sg[None, :] - C0).max() > 1e-8:
                 raise RuntimeError("the evaluator's orbitals differ from the ground state's beyond a sign")
-            self.signs.append((sg[:o], sg[o:]))
+            key = sg.tobytes()
+            if key not in self._sign_tensors:
+                so, sv = sg[:o], sg[o:]
+                self._sign_tensors[key] = (
+                    np.asfortranarray(so[:, None] * sv[None, :]),
+                    np.asfortranarray(so[:, None, None, None] * so[None, :, None, None]
+                                      * sv[None, None, :, None] * sv[None, None, None, :]))
+            self.signs.append(key)
             e = np.diag(s["F"])
             eo, ev = e[:o], e[o:]
-            self.D1.append(eo[:, None] - ev[None, :])
-            self.D2.append(eo[:, None, None, None] + eo[None, :, None, None]
-                           - ev[None, None, :, None] - ev[None, None, None, :])
+            self.D1.append(np.asfortranarray(eo[:, None] - ev[None, :]))
+            self.D2.append(np.asfortranarray(eo[:, None, None, None] + eo[None, :, None, None]
+                                             - ev[None, None, :, None] - ev[None, None, None, :]))
 
     def _basis(self, k, x1, x2):
-        so, sv = self.signs[k]
-        return (x1 * so[:, None] * sv[None, :],
-                x2 * so[:, None, None, None] * so[None, :, None, None] * sv[None, None, :, None] * sv[None, None, None, :])
+        """Amplitudes between the ground state's orbital signs and copy k's (a product with +-1)."""
+        S1, S2 = self._sign_tensors[self.signs[k]]
+        return x1 * S1, x2 * S2
 
     def __call__(self, vecs):
         if len(vecs) > self.nvec:
             raise ValueError(f"{len(vecs)} vectors for an evaluator of {self.nvec}")
         points = []
         for q, (r1, r2) in enumerate(vecs):
+            r1 = np.asfortranarray(r1, dtype=np.float64)
+            r2 = np.asfortranarray(r2, dtype=np.float64)
             for m, c in enumerate(self.STEPS):
                 x1, x2 = self.t1 + c * self.h * r1, self.t2 + c * self.h * r2
                 self.cc.set_guess(4 * q + m, *self._basis(4 * q + m, x1, x2))
@@ -256,7 +269,9 @@ class DeviceSigma:
                 x1, x2 = points[k]
                 om.append(((a1 - x1) * self.D1[k], (a2 - x2) * self.D2[k] / 3.0))
             s1, s2 = ((8.0 * (om[0][p] - om[1][p]) - (om[2][p] - om[3][p])) / (12.0 * self.h) for p in range(2))
-            out.append((s1, pair_symmetric(s2)))
+            # row-major like the caller's vectors: numpy products of arrays in different
+            # layouts run strided (the solvers' dot products took twice as long)
+            out.append((np.ascontiguousarray(s1), pair_symmetric(np.ascontiguousarray(s2))))
         return out
 
     def close(self):

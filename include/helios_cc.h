@@ -182,7 +182,9 @@ int hx_mlp_train(float *params, const float *X, const float *T, int64_t n, int32
 
 /* iterationCC (mod_cc.f90:820-891) for every active molecule: residuals,
  * Jacobi step, DIIS. acc[0] = max|d1|, acc[1] = max|d2| of molecule 0
- * (acc[2..4] = -1, as the reference fills them). */
+ * (acc[2..4] = -1, as the reference fills them). The contractions run on the
+ * 7-slice tensor-core GEMM for HX_PRECISION_EXACT handles and on the FP64
+ * CUDA cores otherwise (the mixed-precision ladder is hx_ccsd_solve's). */
 int hx_ccsd_iterate(hx_ccsd *h, int32_t iteration, double eps, double acc[5]);
 
 /* energyCC r-ccsd (mod_cc.f90:1916-1952) of molecule 0: e[0] total,
