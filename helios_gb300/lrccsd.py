@@ -371,6 +371,60 @@ def iterate_states(sigma, seeds, kw: api.Keywords, lr: LRKeywords, held=()):
     return states
 
 
+class _Basis:
+    """Davidson basis vectors V and their sigma vectors W stacked as rows of
+    contiguous arrays, so that projections, the projected matrix and Ritz
+    vectors are matrix products (the W doubles also kept with a and b swapped,
+    for the x2.y2^ab part of ``inner``)."""
+
+    def __init__(self, o, v, cap):
+        self.o, self.v, self.cap, self.m = o, v, cap, 0
+        n1, n2 = o * v, o * o * v * v
+        self.V1, self.V2 = np.empty((cap, n1)), np.empty((cap, n2))
+        self.W1, self.W2, self.W2s = np.empty((cap, n1)), np.empty((cap, n2)), np.empty((cap, n2))
+
+    def vec(self, j):
+        o, v = self.o, self.v
+        return self.V1[j].reshape(o, v), self.V2[j].reshape(o, o, v, v)
+
+    def coeffs(self, x):
+        """inner(V_j, x) for every basis vector."""
+        m = self.m
+        x1, x2 = x[0].reshape(-1), x[1].reshape(-1)
+        x2s = np.ascontiguousarray(swap_ab(x[1])).reshape(-1)
+        return 2.0 * (self.V1[:m] @ x1) + 2.0 * (self.V2[:m] @ x2) - self.V2[:m] @ x2s
+
+    def orthonormal(self, x):
+        """x orthonormalised against the basis in ``inner`` (twice, as classical Gram-Schmidt
+        needs), or None when nothing of it is left."""
+        n0 = np.sqrt(max(inner(x, x), 0.0))
+        if n0 == 0.0:
+            return None
+        x1, x2 = np.array(x[0], dtype=np.float64) / n0, np.array(x[1], dtype=np.float64) / n0
+        for _ in range(2):
+            if self.m:
+                c = self.coeffs((x1, x2))
+                x1 -= (c @ self.V1[:self.m]).reshape(x1.shape)
+                x2 -= (c @ self.V2[:self.m]).reshape(x2.shape)
+        n = np.sqrt(max(inner((x1, x2), (x1, x2)), 0.0))
+        return None if n < 1e-10 else (x1 / n, x2 / n)
+
+    def add(self, y):
+        j = self.m
+        self.V1[j], self.V2[j] = y[0].reshape(-1), y[1].reshape(-1)
+        self.m += 1
+        return j
+
+    def set_sigma(self, j, w):
+        self.W1[j], self.W2[j] = w[0].reshape(-1), w[1].reshape(-1)
+        self.W2s[j] = np.ascontiguousarray(swap_ab(w[1])).reshape(-1)
+
+    def projected(self, rows, cols):
+        """inner(V_i, W_j) for i in rows, j in cols."""
+        return (2.0 * (self.V1[rows] @ self.W1[cols].T) + 2.0 * (self.V2[rows] @ self.W2[cols].T)
+                - self.V2[rows] @ self.W2s[cols].T)
+
+
 def davidson_states(sigma, seeds, nroots, F, kw: api.Keywords, lr: LRKeywords, track=None, max_space=None):
     """The lowest ``nroots`` roots of J by block Davidson (not the reference's iteration).
 
@@ -393,29 +447,18 @@ def davidson_states(sigma, seeds, nroots, F, kw: api.Keywords, lr: LRKeywords, t
     D2 = (ev[None, None, :, None] + ev[None, None, None, :] - eo[:, None, None, None] - eo[None, :, None, None])
     max_space = max_space or max(8 * k, 2 * len(seeds), 16)
     targets = [10.0 ** (-lr.accuracy) * 2.0 ** min(q, nroots - 1) for q in range(k)]
-    V, W = [], []
-
-    def orthonormal(x):
-        n0 = np.sqrt(max(inner(x, x), 0.0))
-        if n0 == 0.0:
-            return None
-        x = (x[0] / n0, x[1] / n0)
-        for _ in range(2):
-            for b in V:
-                c = inner(b, x)
-                x = (x[0] - c * b[0], x[1] - c * b[1])
-        n = np.sqrt(max(inner(x, x), 0.0))
-        return None if n < 1e-10 else (x[0] / n, x[1] / n)
+    B = _Basis(o, v, max_space + len(seeds) + k)
 
     def extend(vectors):
         new = []
         for x in vectors:
-            y = orthonormal(x)
+            y = B.orthonormal(x)
             if y is not None:
-                V.append(y)
-                new.append(y)
+                new.append(B.add(y))
         for lo in range(0, len(new), sigma.nvec):
-            W.extend(sigma(new[lo:lo + sigma.nvec]))
+            block = new[lo:lo + sigma.nvec]
+            for j, w in zip(block, sigma([B.vec(j) for j in block])):
+                B.set_sigma(j, w)
         return len(new)
 
     extend(list(seeds))
@@ -424,20 +467,22 @@ def davidson_states(sigma, seeds, nroots, F, kw: api.Keywords, lr: LRKeywords, t
     H = np.zeros((0, 0))
     while True:
         iteration += 1
-        m, m0 = len(V), H.shape[0]
+        m, m0 = B.m, H.shape[0]
         Hn = np.zeros((m, m))                          # projected matrix, new rows and columns only
         Hn[:m0, :m0] = H
-        for i in range(m):
-            for j in range(m0 if i < m0 else 0, m):
-                Hn[i, j] = inner(V[i], W[j])
+        if m > m0:
+            Hn[m0:, :] = B.projected(slice(m0, m), slice(0, m))
+            Hn[:m0, m0:] = B.projected(slice(0, m0), slice(m0, m))
         H = Hn
         theta, Y = np.linalg.eig(H)
         order = np.argsort(theta.real)[:k]
+        Yk = np.ascontiguousarray(Y[:, order].real.T)  # k x m
+        X1, X2 = Yk @ B.V1[:m], Yk @ B.V2[:m]
+        S1, S2 = Yk @ B.W1[:m], Yk @ B.W2[:m]
         ritz = []
         for q, idx in enumerate(order):
-            y = Y[:, idx].real
-            x = (sum(y[j] * V[j][0] for j in range(m)), sum(y[j] * V[j][1] for j in range(m)))
-            s = (sum(y[j] * W[j][0] for j in range(m)), sum(y[j] * W[j][1] for j in range(m)))
+            x = (X1[q].reshape(o, v), X2[q].reshape(o, o, v, v))
+            s = (S1[q].reshape(o, v), S2[q].reshape(o, o, v, v))
             n = np.sqrt(inner(x, x))
             x, s = (x[0] / n, x[1] / n), (s[0] / n, s[1] / n)
             w = float(theta[idx].real)
@@ -460,17 +505,10 @@ def davidson_states(sigma, seeds, nroots, F, kw: api.Keywords, lr: LRKeywords, t
                 d1 = np.where(np.abs(d1) < 1e-3, 1e-3, d1)
                 d2 = np.where(np.abs(d2) < 1e-3, 1e-3, d2)
                 corr.append((res[0] / d1, pair_symmetric(res[1] / d2)))
-        if len(V) + len(corr) > max_space:             # restart on the Ritz vectors
-            V.clear(); W.clear()
+        if B.m + len(corr) > max_space:                # restart on the Ritz vectors
+            B.m = 0
             H = np.zeros((0, 0))
-            keep = []
-            for (w, x, s, res, acc) in ritz:
-                y = orthonormal(x)
-                if y is not None:
-                    keep.append(y)
-                    V.append(y)
-            for lo in range(0, len(keep), sigma.nvec):
-                W.extend(sigma(keep[lo:lo + sigma.nvec]))
+            extend([x for (w, x, s, res, acc) in ritz])
         if extend(corr) == 0:
             for st in states:
                 st.status = st.status or STATUS_STAGNATED
