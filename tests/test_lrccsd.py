@@ -81,6 +81,32 @@ def test_fake_engine_sigma_is_the_closed_shell_jacobian():
     for (s1, s2), r in zip(sig(vecs), vecs):
         want1, want2 = olr.closed_shell_unpack(J @ olr.closed_shell_pack(*r), o, v)
         assert np.abs(s1 - want1).max() < 1e-10 and np.abs(s2 - want2).max() < 1e-10
+        # the Davidson basis stores rows of flattened vectors: the sigma hands back row-major arrays
+        assert s1.flags.c_contiguous and s2.flags.c_contiguous
+
+
+def test_stacked_basis_is_the_inner_metric():
+    """The Davidson basis keeps V and W as rows of stacked arrays; its projections, projected
+    matrix and Gram-Schmidt must be the ones the pairwise ``inner`` gives."""
+    o, v = 3, 4
+    rng = np.random.default_rng(11)
+    B = lrccsd._Basis(o, v, 6)
+    kept = []
+    for _ in range(4):
+        y = B.orthonormal(_random_singlet(rng, o, v))
+        assert y is not None
+        kept.append(y)
+        B.set_sigma(B.add(y), _random_singlet(rng, o, v))
+    G = np.array([[lrccsd.inner(a, b) for b in kept] for a in kept])
+    assert np.abs(G - np.eye(4)).max() < 1e-12
+    x = _random_singlet(rng, o, v)
+    assert np.allclose(B.coeffs(x), [lrccsd.inner(y, x) for y in kept], rtol=0, atol=1e-12)
+    W = [(B.W1[j].reshape(o, v), B.W2[j].reshape(o, o, v, v)) for j in range(4)]
+    want = np.array([[lrccsd.inner(kept[i], W[j]) for j in range(4)] for i in range(4)])
+    assert np.allclose(B.projected(slice(0, 4), slice(0, 4)), want, rtol=0, atol=1e-12)
+    assert np.allclose(B.projected([1, 3], [0, 2]), want[np.ix_([1, 3], [0, 2])], rtol=0, atol=1e-12)
+    assert B.orthonormal(kept[2]) is None
+    assert B.orthonormal((np.zeros((o, v)), np.zeros((o, o, v, v)))) is None
 
 
 def _spectrum_and_problem(mol):
