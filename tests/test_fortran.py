@@ -54,6 +54,15 @@ def test_module_declares_every_c_function():
     assert bound == _c_functions()
 
 
+def test_module_parameters_are_the_header_constants():
+    want = {k: int(v) for k, v in re.findall(r"^#define (HX_[A-Z0-9_]+) \(?(-?\d+)\)?", open(HEADER).read(), re.M)}
+    text = re.sub(r"&\s*\n\s*", " ", open(MODULE).read())
+    got = {}
+    for decl in re.findall(r"parameter, public :: (.*)", text):
+        got.update({k: int(v) for k, v in re.findall(r"(HX_[A-Z0-9_]+) = (-?\d+)", decl)})
+    assert want and got == want
+
+
 @pytest.mark.parametrize("name", ["hx_ppp_model", "hx_cc_params"])
 def test_module_types_match_the_c_structs(name):
     assert _type_fields(name) == _struct_fields(name)
