@@ -12,6 +12,7 @@
 
 #include "../../include/helios_cc.h"
 #include "hx_kernels.h"
+#include "hx_layout.h"
 #include "hx_mlp.h"
 #include "hx_tc.h"
 
@@ -230,6 +231,8 @@ struct hx_ccsd {
     long long phase_nodes[5] = {};       // kernels captured in each phase's conditional bodies
     int *d_cancel = nullptr;             // device address of h_pinned[8] (mapped host memory)
     unsigned long long *d_t0 = nullptr;
+    double *h_amp = nullptr;             // pinned staging of hx_ccsd_set_guess / hx_ccsd_get_amplitudes
+    size_t h_amp_elems = 0;
     int *h_pinned = nullptr;             // pinned, mapped: [0..7] mirror of that block ([0] molecules
                                          // still running, [2..6] per phase next), [8] the stop request
                                          // (read by the device)
@@ -1248,24 +1251,38 @@ int hx_ccsd_solve_batch(hx_ccsd *h, int32_t *status, int32_t *iters, double *e)
     return HX_OK;
 }
 
+// Pinned host staging for the amplitude transfers, grown to the largest
+// molecule asked for (pageable memory would go through the driver's bounce
+// buffer and fault its pages in on every call); NULL if it cannot be pinned.
+static double *amp_stage(hx_ccsd *h, size_t elems)
+{
+    if (elems > h->h_amp_elems) {
+        if (h->h_amp) cudaFreeHost(h->h_amp);
+        h->h_amp = nullptr;
+        h->h_amp_elems = 0;
+        if (cudaMallocHost(&h->h_amp, sizeof(double) * elems) != cudaSuccess) {
+            cudaGetLastError();
+            h->h_amp = nullptr;
+            return nullptr;
+        }
+        h->h_amp_elems = elems;
+    }
+    return h->h_amp;
+}
+
 int hx_ccsd_get_amplitudes(hx_ccsd *h, int32_t mol, double *t1, double *t2)
 {
     if (!h || mol < 0 || mol >= h->nmol) { hx_set_error("bad handle or molecule index"); return HX_ERR_ARG; }
     const int o = h->o[mol], v = h->v[mol];
     const size_t ov = (size_t)o * v;
-    std::vector<double> a(ov), b(ov * ov);
-    HX_CU(cudaMemcpyAsync(a.data(), h->cc[mol].t1, sizeof(double) * ov, cudaMemcpyDeviceToHost, h->st));
-    HX_CU(cudaMemcpyAsync(b.data(), h->cc[mol].t2, sizeof(double) * ov * ov, cudaMemcpyDeviceToHost, h->st));
+    std::vector<double> pageable;
+    double *buf = amp_stage(h, ov + ov * ov);
+    if (!buf) { pageable.resize(ov + ov * ov); buf = pageable.data(); }
+    HX_CU(cudaMemcpyAsync(buf, h->cc[mol].t1, sizeof(double) * ov, cudaMemcpyDeviceToHost, h->st));
+    HX_CU(cudaMemcpyAsync(buf + ov, h->cc[mol].t2, sizeof(double) * ov * ov, cudaMemcpyDeviceToHost, h->st));
     HX_CU(cudaStreamSynchronize(h->st));
-    if (t1)
-        for (int i = 0; i < o; ++i)
-            for (int x = 0; x < v; ++x) t1[i + (size_t)o * x] = a[(size_t)i * v + x];
-    if (t2)
-        for (int i = 0; i < o; ++i)
-            for (int x = 0; x < v; ++x)
-                for (int j = 0; j < o; ++j)
-                    for (int y = 0; y < v; ++y)
-                        t2[i + (size_t)o * (j + (size_t)o * (x + (size_t)v * y))] = b[(((size_t)i * v + x) * o + j) * v + y];
+    if (t1) hx::t1_from_engine(buf, t1, o, v);
+    if (t2) hx::t2_from_engine(buf + ov, t2, o, v);
     return HX_OK;
 }
 
@@ -1274,16 +1291,13 @@ int hx_ccsd_set_guess(hx_ccsd *h, int32_t mol, const double *t1, const double *t
     if (!h || !h->initialized || mol < 0 || mol >= h->nmol || !t1 || !t2) { hx_set_error("hx_ccsd_set_guess: bad arguments or state"); return HX_ERR_ARG; }
     const int o = h->o[mol], v = h->v[mol];
     const size_t ov = (size_t)o * v;
-    std::vector<double> a(ov), b(ov * ov);
-    for (int i = 0; i < o; ++i)
-        for (int x = 0; x < v; ++x) a[(size_t)i * v + x] = t1[i + (size_t)o * x];
-    for (int i = 0; i < o; ++i)
-        for (int x = 0; x < v; ++x)
-            for (int j = 0; j < o; ++j)
-                for (int y = 0; y < v; ++y)
-                    b[(((size_t)i * v + x) * o + j) * v + y] = t2[i + (size_t)o * (j + (size_t)o * (x + (size_t)v * y))];
-    HX_CU(cudaMemcpyAsync(h->cc[mol].t1, a.data(), sizeof(double) * ov, cudaMemcpyHostToDevice, h->st));
-    HX_CU(cudaMemcpyAsync(h->cc[mol].t2, b.data(), sizeof(double) * ov * ov, cudaMemcpyHostToDevice, h->st));
+    std::vector<double> pageable;
+    double *buf = amp_stage(h, ov + ov * ov);
+    if (!buf) { pageable.resize(ov + ov * ov); buf = pageable.data(); }
+    hx::t1_to_engine(t1, buf, o, v);
+    hx::t2_to_engine(t2, buf + ov, o, v);
+    HX_CU(cudaMemcpyAsync(h->cc[mol].t1, buf, sizeof(double) * ov, cudaMemcpyHostToDevice, h->st));
+    HX_CU(cudaMemcpyAsync(h->cc[mol].t2, buf + ov, sizeof(double) * ov * ov, cudaMemcpyHostToDevice, h->st));
     HX_CU(cudaMemsetAsync(h->diis[mol].count, 0, sizeof(int), h->st));
     diis_mirror_reset(h, mol);
     HX_CU(cudaStreamSynchronize(h->st));
@@ -1400,6 +1414,7 @@ void hx_ccsd_destroy(hx_ccsd *h)
     cudaFree(h->d_remaining);
     cudaFree(h->d_t0);
     if (h->h_pinned) cudaFreeHost(h->h_pinned);
+    if (h->h_amp) cudaFreeHost(h->h_amp);
     if (h->st2) cudaStreamDestroy(h->st2);
     cudaFree(h->d_gate);
     cudaFree(h->d_part);

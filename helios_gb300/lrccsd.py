@@ -202,8 +202,6 @@ def seed_vector(sel, o, v):
 class DeviceSigma:
     """J r for up to ``nvec`` vectors per call: four residual evaluations per vector in one batch."""
 
-    STEPS = (1.0, -1.0, 2.0, -2.0)
-
     def __init__(self, mol: Molecule, keywords: api.Keywords, t1, t2, C0, nvec=1, h=1e-2, engine=None,
                  precision="exact"):
         # the residual comes back through the "2-1" step: t2' = x2 + 3 Omega2 / D2; its
@@ -219,8 +217,10 @@ class DeviceSigma:
         self.calls = 0                                      # engine iterations (one per call)
         self.eps = 10.0 ** (-keywords.accuracy)
         o = t1.shape[0]
-        # each copy's orbital signs as +-1 tensors (copies with the same signs share them)
-        self.signs, self.D1, self.D2, self._sign_tensors = [], [], [], {}
+        # each copy's orbital signs as +-1 tensors (None where every sign is +1; copies with
+        # the same signs share them) and its denominators times those signs, which turn a
+        # copy's step in its own signs, stepCC(x) - x, into the ground state's residual
+        self.signs, self._sign_tensors, self._t_in, self.DS1, self.DS2 = [], {}, {}, [], []
         for k in range(4 * nvec):
             s = self.cc.scf(k)
             sg = _align(C0, s["C"])
@@ -229,35 +229,46 @@ class DeviceSigma:
             key = sg.tobytes()
             if key not in self._sign_tensors:
                 so, sv = sg[:o], sg[o:]
-                self._sign_tensors[key] = (
+                self._sign_tensors[key] = None if np.all(sg == 1.0) else (
                     np.asfortranarray(so[:, None] * sv[None, :]),
                     np.asfortranarray(so[:, None, None, None] * so[None, :, None, None]
                                       * sv[None, None, :, None] * sv[None, None, None, :]))
+                self._t_in[key] = self._basis_of(key, self.t1, self.t2)
             self.signs.append(key)
             e = np.diag(s["F"])
             eo, ev = e[:o], e[o:]
-            self.D1.append(np.asfortranarray(eo[:, None] - ev[None, :]))
-            self.D2.append(np.asfortranarray(eo[:, None, None, None] + eo[None, :, None, None]
-                                             - ev[None, None, :, None] - ev[None, None, None, :]))
+            D1 = np.asfortranarray(eo[:, None] - ev[None, :])
+            D2 = np.asfortranarray(eo[:, None, None, None] + eo[None, :, None, None]
+                                   - ev[None, None, :, None] - ev[None, None, None, :])
+            DS1, DS2 = self._basis_of(key, D1, D2)
+            self.DS1.append(np.asfortranarray(DS1))
+            self.DS2.append(np.asfortranarray(DS2))
 
-    def _basis(self, k, x1, x2):
-        """Amplitudes between the ground state's orbital signs and copy k's (a product with +-1)."""
-        S1, S2 = self._sign_tensors[self.signs[k]]
-        return x1 * S1, x2 * S2
+    def _basis_of(self, key, x1, x2):
+        """Amplitudes between the ground state's orbital signs and a copy's (a product with +-1)."""
+        S = self._sign_tensors[key]
+        return (x1, x2) if S is None else (x1 * S[0], x2 * S[1])
 
     def __call__(self, vecs):
+        """J r for each r: the five-point stencil (8 (O(+h) - O(-h)) - (O(+2h) - O(-2h))) / 12 h
+        of the residual O(t + c h r) = (stepCC(x) - x) D for t1 and (stepCC(x) - x) D / 3 for t2,
+        formed in place (the signs are exact: (a - x s) s d = (a s - x) d bit for bit)."""
         if len(vecs) > self.nvec:
             raise ValueError(f"{len(vecs)} vectors for an evaluator of {self.nvec}")
-        points = []
+        guesses = []
         for q, (r1, r2) in enumerate(vecs):
-            r1 = np.asfortranarray(r1, dtype=np.float64)
-            r2 = np.asfortranarray(r2, dtype=np.float64)
-            for m, c in enumerate(self.STEPS):
-                x1, x2 = self.t1 + c * self.h * r1, self.t2 + c * self.h * r2
-                self.cc.set_guess(4 * q + m, *self._basis(4 * q + m, x1, x2))
-                points.append((x1, x2))
+            hr1 = self.h * np.asfortranarray(r1, dtype=np.float64)
+            hr2 = self.h * np.asfortranarray(r2, dtype=np.float64)
+            hr1x2, hr2x2 = hr1 + hr1, hr2 + hr2                         # (2 h) r, exactly
+            points = ((self.t1 + hr1, self.t2 + hr2), (self.t1 - hr1, self.t2 - hr2),
+                      (self.t1 + hr1x2, self.t2 + hr2x2), (self.t1 - hr1x2, self.t2 - hr2x2))
+            for m, (x1, x2) in enumerate(points):
+                k = 4 * q + m
+                xb = self._basis_of(self.signs[k], x1, x2)
+                self.cc.set_guess(k, *xb)
+                guesses.append(xb)
         for k in range(4 * len(vecs), 4 * self.nvec):      # idle copies restart from t every call
-            self.cc.set_guess(k, *self._basis(k, self.t1, self.t2))
+            self.cc.set_guess(k, *self._t_in[self.signs[k]])
         self.cc.iterationCC(1, self.eps)
         self.calls += 1
         out = []
@@ -265,13 +276,25 @@ class DeviceSigma:
             om = []
             for m in range(4):
                 k = 4 * q + m
-                a1, a2 = self._basis(k, *self.cc.amplitudes(k))
-                x1, x2 = points[k]
-                om.append(((a1 - x1) * self.D1[k], (a2 - x2) * self.D2[k] / 3.0))
-            s1, s2 = ((8.0 * (om[0][p] - om[1][p]) - (om[2][p] - om[3][p])) / (12.0 * self.h) for p in range(2))
+                a1, a2 = self.cc.amplitudes(k)
+                a1 -= guesses[k][0]
+                a1 *= self.DS1[k]
+                a2 -= guesses[k][1]
+                a2 *= self.DS2[k]
+                a2 /= 3.0
+                om.append((a1, a2))
+            res = []
+            for p in range(2):
+                d, e = om[0][p], om[2][p]
+                d -= om[1][p]
+                d *= 8.0
+                e -= om[3][p]
+                d -= e
+                d /= 12.0 * self.h
+                res.append(d)
             # row-major like the caller's vectors: numpy products of arrays in different
             # layouts run strided (the solvers' dot products took twice as long)
-            out.append((np.ascontiguousarray(s1), pair_symmetric(np.ascontiguousarray(s2))))
+            out.append((np.ascontiguousarray(res[0]), pair_symmetric(np.ascontiguousarray(res[1]))))
         return out
 
     def close(self):

@@ -237,6 +237,34 @@ def test_tensor_core_slicing_is_an_exact_digit_expansion(tmp_path):
             assert abs(recon - a) <= np.ldexp(1.0, -8 * (S - 1) - 1) * (1 + 1e-12)
 
 
+def test_amplitude_layout_conversions(tmp_path):
+    """hx_layout.h on the host: the reference's column-major t1(o, v) and
+    t2(o, o, v, v) become the engine's row-major t1 [i][a] and pair-ordered
+    t2 [i][a][j][b] (numpy's transposes of the same arrays), and back."""
+    import shutil
+    import subprocess
+    if shutil.which("g++") is None:
+        pytest.skip("no host C++ compiler")
+    exe = tmp_path / "layout_harness"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "helios_gb300", "csrc"),
+                    os.path.join(ROOT, "tests", "layout_harness.cpp"), "-o", str(exe)], check=True)
+    shapes = [(1, 1), (1, 3), (4, 1), (3, 5), (6, 2), (16, 16), (7, 33)]
+    out = subprocess.run([str(exe)], input="".join(f"{o} {v}\n" for o, v in shapes),
+                         capture_output=True, text=True, check=True).stdout.split()
+    pos = 0
+    for o, v in shapes:
+        n1, n2 = o * v, (o * v) ** 2
+        f1 = np.arange(n1).reshape((o, v), order="F")
+        f2 = np.arange(n2).reshape((o, o, v, v), order="F")
+        e1 = np.array(out[pos:pos + n1], dtype=np.int64)
+        e2 = np.array(out[pos + n1:pos + n1 + n2], dtype=np.int64)
+        assert np.array_equal(e1, f1.reshape(-1))
+        assert np.array_equal(e2, f2.transpose(0, 2, 1, 3).reshape(-1))
+        assert out[pos + n1 + n2] == "1"
+        pos += n1 + n2 + 1
+    assert pos == len(out)
+
+
 def test_epilogue_integer_conversions(tmp_path):
     """The GEMM epilogue's integer routes (hx_slice.h) on the host: f2d_pow2
     of hi and of lo, added in FP64, give (hi + lo) 2^k to within one FP64 ulp
