@@ -138,7 +138,10 @@ int hx_ccsd_create_batch(const hx_ppp_model *ms, int32_t n, const hx_cc_params *
  * and the call fails only if no SCF converged. */
 int hx_ccsd_init(hx_ccsd *h);
 
-/* Replace molecule mol's amplitudes (reference layout, see above). */
+/* Replace molecule mol's amplitudes (reference layout, see above). This call
+ * and hx_ccsd_get_amplitudes stage the arrays in a pinned host buffer the
+ * handle keeps (o*v + (o*v)^2 doubles of the largest molecule asked for, freed
+ * by hx_ccsd_destroy; pageable memory if pinning fails). */
 int hx_ccsd_set_guess(hx_ccsd *h, int32_t mol, const double *t1, const double *t2);
 
 /* ---- Learned T2 guess (no counterpart in the reference; it replaces the
