@@ -397,14 +397,15 @@ def iterate_states(sigma, seeds, kw: api.Keywords, lr: LRKeywords, held=()):
 class _Basis:
     """Davidson basis vectors V and their sigma vectors W stacked as rows of
     contiguous arrays, so that projections, the projected matrix and Ritz
-    vectors are matrix products (the W doubles also kept with a and b swapped,
-    for the x2.y2^ab part of ``inner``)."""
+    vectors are matrix products. The doubles of V are also kept with the
+    metric applied, G = 2 V2 - V2^ab (a and b swapped): inner(x, y) =
+    2 x1.y1 + (2 x2 - x2^ab).y2, so a projection is one product per part."""
 
     def __init__(self, o, v, cap):
         self.o, self.v, self.cap, self.m = o, v, cap, 0
         n1, n2 = o * v, o * o * v * v
-        self.V1, self.V2 = np.empty((cap, n1)), np.empty((cap, n2))
-        self.W1, self.W2, self.W2s = np.empty((cap, n1)), np.empty((cap, n2)), np.empty((cap, n2))
+        self.V1, self.V2, self.G2 = np.empty((cap, n1)), np.empty((cap, n2)), np.empty((cap, n2))
+        self.W1, self.W2 = np.empty((cap, n1)), np.empty((cap, n2))
 
     def vec(self, j):
         o, v = self.o, self.v
@@ -413,9 +414,7 @@ class _Basis:
     def coeffs(self, x):
         """inner(V_j, x) for every basis vector."""
         m = self.m
-        x1, x2 = x[0].reshape(-1), x[1].reshape(-1)
-        x2s = np.ascontiguousarray(swap_ab(x[1])).reshape(-1)
-        return 2.0 * (self.V1[:m] @ x1) + 2.0 * (self.V2[:m] @ x2) - self.V2[:m] @ x2s
+        return 2.0 * (self.V1[:m] @ x[0].reshape(-1)) + self.G2[:m] @ x[1].reshape(-1)
 
     def orthonormal(self, x):
         """x orthonormalised against the basis in ``inner`` (twice, as classical Gram-Schmidt
@@ -435,17 +434,16 @@ class _Basis:
     def add(self, y):
         j = self.m
         self.V1[j], self.V2[j] = y[0].reshape(-1), y[1].reshape(-1)
+        self.G2[j] = (2.0 * y[1] - swap_ab(y[1])).reshape(-1)
         self.m += 1
         return j
 
     def set_sigma(self, j, w):
         self.W1[j], self.W2[j] = w[0].reshape(-1), w[1].reshape(-1)
-        self.W2s[j] = np.ascontiguousarray(swap_ab(w[1])).reshape(-1)
 
     def projected(self, rows, cols):
         """inner(V_i, W_j) for i in rows, j in cols."""
-        return (2.0 * (self.V1[rows] @ self.W1[cols].T) + 2.0 * (self.V2[rows] @ self.W2[cols].T)
-                - self.V2[rows] @ self.W2s[cols].T)
+        return 2.0 * (self.V1[rows] @ self.W1[cols].T) + self.G2[rows] @ self.W2[cols].T
 
 
 def davidson_states(sigma, seeds, nroots, F, kw: api.Keywords, lr: LRKeywords, track=None, max_space=None):
@@ -500,14 +498,14 @@ def davidson_states(sigma, seeds, nroots, F, kw: api.Keywords, lr: LRKeywords, t
         theta, Y = np.linalg.eig(H)
         order = np.argsort(theta.real)[:k]
         Yk = np.ascontiguousarray(Y[:, order].real.T)  # k x m
+        # unit Ritz vectors: the basis is orthonormal in inner, so inner(x, x) = |y|^2
+        Yk /= np.linalg.norm(Yk, axis=1)[:, None]
         X1, X2 = Yk @ B.V1[:m], Yk @ B.V2[:m]
         S1, S2 = Yk @ B.W1[:m], Yk @ B.W2[:m]
         ritz = []
         for q, idx in enumerate(order):
             x = (X1[q].reshape(o, v), X2[q].reshape(o, o, v, v))
             s = (S1[q].reshape(o, v), S2[q].reshape(o, o, v, v))
-            n = np.sqrt(inner(x, x))
-            x, s = (x[0] / n, x[1] / n), (s[0] / n, s[1] / n)
             w = float(theta[idx].real)
             res = (s[0] - w * x[0], s[1] - w * x[1])
             ritz.append((w, x, s, res, max(max_abs(res))))
