@@ -357,8 +357,8 @@ class CoupledCluster:
     def amplitudes(self, mol: int = 0):
         """t1 (o, v) and t2 (o, o, v, v) as numpy arrays indexed like the reference."""
         N, o, v, _ = self.dims[mol]
-        t1 = np.zeros((o, v), order="F")
-        t2 = np.zeros((o, o, v, v), order="F")
+        t1 = np.empty((o, v), order="F")                  # every element is written
+        t2 = np.empty((o, o, v, v), order="F")
         _check(library().hx_ccsd_get_amplitudes(self._h, int(mol), t1.ctypes.data_as(_c_d), t2.ctypes.data_as(_c_d)))
         return t1, t2
 

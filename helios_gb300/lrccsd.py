@@ -257,8 +257,8 @@ class DeviceSigma:
             raise ValueError(f"{len(vecs)} vectors for an evaluator of {self.nvec}")
         guesses = []
         for q, (r1, r2) in enumerate(vecs):
-            hr1 = self.h * np.asfortranarray(r1, dtype=np.float64)
-            hr2 = self.h * np.asfortranarray(r2, dtype=np.float64)
+            hr1 = np.multiply(self.h, r1, dtype=np.float64, order="F")
+            hr2 = np.multiply(self.h, r2, dtype=np.float64, order="F")
             hr1x2, hr2x2 = hr1 + hr1, hr2 + hr2                         # (2 h) r, exactly
             points = ((self.t1 + hr1, self.t2 + hr2), (self.t1 - hr1, self.t2 - hr2),
                       (self.t1 + hr1x2, self.t2 + hr2x2), (self.t1 - hr1x2, self.t2 - hr2x2))
