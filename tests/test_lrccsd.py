@@ -85,6 +85,31 @@ def test_fake_engine_sigma_is_the_closed_shell_jacobian():
         assert s1.flags.c_contiguous and s2.flags.c_contiguous
 
 
+def test_sigma_in_flipped_orbital_signs():
+    """Amplitudes and vectors given in orbitals some of whose signs differ from the
+    evaluator's own SCF: the sigma carries them across and is the Jacobian in the caller's
+    signs (S J S for the diagonal +-1 sign change S)."""
+    mol = molecules.polyene(6)
+    model, scf, F, o, out = _problem(mol)
+    kw = api.Keywords(bond_alternation=0.1, accuracy=12)
+    n = F.shape[0]
+    v = n - o
+    sg = np.ones(n)
+    sg[[0, 2, o + 1]] = -1.0
+    so, sv = sg[:o], sg[o:]
+    S1 = so[:, None] * sv[None, :]
+    S2 = so[:, None, None, None] * so[None, :, None, None] * sv[None, None, :, None] * sv[None, None, None, :]
+    sig = lrccsd.DeviceSigma(mol, kw, out["t1"] * S1, out["t2"] * S2, scf["V"] * sg[None, :], nvec=2,
+                             engine=FakeCoupledCluster)
+    assert any(sig._sign_tensors[k] is not None for k in sig.signs)
+    J = olr.closed_shell_jacobian(F, scf["V"], model["G"], o, out["t1"], out["t2"])
+    rng = np.random.default_rng(8)
+    vecs = [_random_singlet(rng, o, v)]                           # one vector: the second copy set idles
+    for (s1, s2), (r1, r2) in zip(sig(vecs), vecs):
+        want1, want2 = olr.closed_shell_unpack(J @ olr.closed_shell_pack(r1 * S1, r2 * S2), o, v)
+        assert np.abs(s1 - want1 * S1).max() < 1e-10 and np.abs(s2 - want2 * S2).max() < 1e-10
+
+
 def test_stacked_basis_is_the_inner_metric():
     """The Davidson basis keeps V and W as rows of stacked arrays; its projections, projected
     matrix and Gram-Schmidt must be the ones the pairwise ``inner`` gives."""
