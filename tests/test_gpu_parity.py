@@ -116,6 +116,28 @@ def test_batch_matches_individual_oracle(api):
         assert abs((out["energy"][k, 0] - out["energy"][k, 1]) - ref["ecorr"]) < 1e-8
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_smallest_molecule_and_a_ragged_batch(api, precision):
+    """Ethylene (two sites, o = v = 1: the smallest problem, where two-electron CCSD is exact)
+    alone and in one batch with molecules of 4 and 14 sites, against the literal oracle."""
+    from oracle.literal import solve_literal
+    tol = 1e-8 if precision == "fp64" else 1e-6
+    mols = [molecules.polyene(2), molecules.polyene(4), molecules.random_molecule(12, 14, 14)]
+    refs = [solve_literal(m, alternation=0.1, eps=1e-10)["ecorr"] for m in mols]
+    cc = api.CoupledCluster(mols[0], _kw(api, precision=precision))
+    cc.initCC()
+    out = cc.iterate()
+    cc.finalizeCC()
+    assert out["status"] == 1 and abs((out["energy"][0] - out["energy"][1]) - refs[0]) < tol
+    cc = api.CoupledCluster(mols, _kw(api, precision=precision))
+    cc.initCC()
+    out = cc.solve_batch()
+    cc.finalizeCC()
+    for k in range(len(mols)):
+        assert out["status"][k] == 1
+        assert abs((out["energy"][k, 0] - out["energy"][k, 1]) - refs[k]) < tol
+
+
 def test_larger_molecule_against_factorised_oracle(api):
     from oracle import ccsd_fact
     from oracle.ppp import build_model
