@@ -60,6 +60,29 @@ def test_create_rejects_bad_input_without_a_gpu_call(lib):
     assert lib.hx_last_error(buf, 256) > 0
 
 
+@pytest.mark.parametrize("field,value", [("projection_type", 3), ("projection_type", 0), ("diis_steps", 1),
+                                         ("diis_steps", 51), ("precision", 3), ("mixed_check", 2),
+                                         ("tile_tuning", 3), ("tile_force", -2)])
+def test_create_rejects_bad_keywords_without_a_gpu_call(lib, field, value):
+    """Keyword values outside the ranges definebd.f90 accepts (and the engine options' ranges)
+    are refused before any device is touched, with the error text set."""
+    from helios_gb300 import api, molecules
+    p = api.Keywords().to_c()
+    setattr(p, field, value)
+    arrays = api._ModelArrays(molecules.polyene(4))
+    models = (api.PPPModel * 1)(arrays.c)
+    h = ctypes.c_void_p()
+    good = api.Keywords().to_c()                  # control: only the device is missing (or present)
+    rc = lib.hx_ccsd_create_batch(models, 1, ctypes.byref(good), ctypes.byref(h))
+    assert rc in (-101, 0)
+    if rc == 0:
+        lib.hx_ccsd_destroy(h)
+        h = ctypes.c_void_p()
+    assert lib.hx_ccsd_create_batch(models, 1, ctypes.byref(p), ctypes.byref(h)) == -100
+    buf = ctypes.create_string_buffer(256)
+    assert lib.hx_last_error(buf, 256) > 0 and not h.value
+
+
 def test_tile_table_selection_logic(lib, tmp_path):
     # the autotuner's table on the host (no GPU call): candidates per mode, merging,
     # range checks, the shipped file format, and the keywords that steer it
